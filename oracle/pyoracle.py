@@ -1,0 +1,178 @@
+"""ctypes front end of the CPU oracle library (test infrastructure only).
+
+Loads oracle/_build/liboracle.so (built from oracle/cns_oracle.cpp) and,
+when present, oracle/_ref/libcnsref.so (the reference's own kernel sources
+compiled here).  Both expose the same call shapes for one box:
+  rhs(U_ghosted) -> dSdt_valid, advance(...), fill_halo(...), est_timestep(...)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+NG = 3
+NCONS = 5
+
+
+class CClosures(ctypes.Structure):
+    _fields_ = [("gamma", ctypes.c_double), ("cv", ctypes.c_double), ("cp", ctypes.c_double),
+                ("Rspec", ctypes.c_double), ("visc_law", ctypes.c_int32), ("cond_law", ctypes.c_int32),
+                ("visc_ref", ctypes.c_double), ("Tvisc_ref", ctypes.c_double),
+                ("cond_ref", ctypes.c_double), ("Tcond_ref", ctypes.c_double),
+                ("Cshock", ctypes.c_double), ("Cdamp", ctypes.c_double)]
+
+
+class CScheme(ctypes.Structure):
+    _fields_ = [("rhs_euler", ctypes.c_int32), ("rhs_visc", ctypes.c_int32),
+                ("flux_euler", ctypes.c_int32), ("order_keep", ctypes.c_int32),
+                ("art_diss", ctypes.c_int32)]
+
+
+def c_closures(cl):
+    return CClosures(cl.gamma, cl.cv, cl.cp, cl.Rspec, int(cl.visc_law), int(cl.cond_law),
+                     cl.visc_ref, cl.Tvisc_ref, cl.cond_ref, cl.Tcond_ref, cl.Cshock, cl.Cdamp)
+
+
+def c_scheme(sc):
+    return CScheme(int(sc.rhs_euler), int(sc.rhs_visc), int(sc.flux_euler), int(sc.order_keep),
+                   int(sc.art_diss))
+
+
+def _i3(v):
+    return (ctypes.c_int * 3)(*[int(x) for x in v])
+
+
+def _d3(v):
+    return (ctypes.c_double * 3)(*[float(x) for x in v])
+
+
+def _ptr(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Oracle:
+    """One loaded oracle library (the restatement or the reference build)."""
+
+    def __init__(self, path):
+        self.path = path
+        self.lib = ctypes.CDLL(path)
+        L = self.lib
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.orc_compute_rhs.argtypes = [ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ip, ip, dp,
+                                      dp, dp, ctypes.c_int]
+        L.orc_compute_rhs.restype = ctypes.c_int
+        L.orc_fill_halo.argtypes = [ip, ip, ip, ip, dp, ctypes.c_int]
+        L.orc_fill_halo.restype = ctypes.c_int
+        L.orc_est_timestep.argtypes = [ctypes.POINTER(CClosures), ip, ip, dp, dp, ctypes.c_int,
+                                       ctypes.c_double]
+        L.orc_est_timestep.restype = ctypes.c_double
+        L.orc_advance.argtypes = [ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ip, ip, dp, ip, ip,
+                                  ctypes.c_int, ctypes.c_int, ctypes.c_double, dp, dp, ctypes.c_int]
+        L.orc_advance.restype = ctypes.c_int
+        self.has_jvp = hasattr(L, "orc_compute_rhs_jvp")
+        if self.has_jvp:
+            L.orc_compute_rhs_jvp.argtypes = [ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ip, ip,
+                                              dp, dp, dp, dp, dp, ctypes.c_int]
+            L.orc_compute_rhs_jvp.restype = ctypes.c_int
+            L.orc_compute_rhs_count.argtypes = [ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ip,
+                                                ip, dp, dp, ctypes.POINTER(ctypes.c_longlong)]
+            L.orc_compute_rhs_count.restype = ctypes.c_int
+
+    # -------------------------------------------------------------- calls --
+    def rhs(self, scheme, closures, U, dxinv, lo=(0, 0, 0), nthreads=1):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        nz, ny, nx = (s - 2 * NG for s in U.shape[1:])
+        hi = (lo[0] + nx - 1, lo[1] + ny - 1, lo[2] + nz - 1)
+        out = np.empty((NCONS, nz, ny, nx))
+        sc, cl = c_scheme(scheme), c_closures(closures)
+        rc = self.lib.orc_compute_rhs(ctypes.byref(sc), ctypes.byref(cl), _i3(lo), _i3(hi), _d3(dxinv),
+                                      _ptr(U), _ptr(out), int(nthreads))
+        if rc:
+            raise RuntimeError("orc_compute_rhs failed: %d" % rc)
+        return out
+
+    def rhs_jvp(self, scheme, closures, U, W, dxinv, lo=(0, 0, 0), nthreads=1):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        W = np.ascontiguousarray(W, dtype=np.float64)
+        nz, ny, nx = (s - 2 * NG for s in U.shape[1:])
+        hi = (lo[0] + nx - 1, lo[1] + ny - 1, lo[2] + nz - 1)
+        R = np.empty((NCONS, nz, ny, nx))
+        JW = np.empty((NCONS, nz, ny, nx))
+        sc, cl = c_scheme(scheme), c_closures(closures)
+        rc = self.lib.orc_compute_rhs_jvp(ctypes.byref(sc), ctypes.byref(cl), _i3(lo), _i3(hi), _d3(dxinv),
+                                          _ptr(U), _ptr(W), _ptr(R), _ptr(JW), int(nthreads))
+        if rc:
+            raise RuntimeError("orc_compute_rhs_jvp failed: %d" % rc)
+        return R, JW
+
+    def rhs_counts(self, scheme, closures, U, dxinv, lo=(0, 0, 0)):
+        """{add, mul, div, sqrt, cmp} operation counts of one RHS of this box."""
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        nz, ny, nx = (s - 2 * NG for s in U.shape[1:])
+        hi = (lo[0] + nx - 1, lo[1] + ny - 1, lo[2] + nz - 1)
+        cnt = (ctypes.c_longlong * 5)()
+        sc, cl = c_scheme(scheme), c_closures(closures)
+        rc = self.lib.orc_compute_rhs_count(ctypes.byref(sc), ctypes.byref(cl), _i3(lo), _i3(hi),
+                                            _d3(dxinv), _ptr(U), cnt)
+        if rc:
+            raise RuntimeError("orc_compute_rhs_count failed: %d" % rc)
+        return dict(zip(("add", "mul", "div", "sqrt", "cmp"), list(cnt)))
+
+    def fill_halo(self, U, bc_lo, bc_hi, lo=(0, 0, 0)):
+        """In-place ghost fill of a single-box domain."""
+        assert U.flags.c_contiguous
+        nz, ny, nx = (s - 2 * NG for s in U.shape[1:])
+        hi = (lo[0] + nx - 1, lo[1] + ny - 1, lo[2] + nz - 1)
+        rc = self.lib.orc_fill_halo(_i3(lo), _i3(hi), _i3(bc_lo), _i3(bc_hi), _ptr(U), int(U.shape[0]))
+        if rc:
+            raise RuntimeError("orc_fill_halo failed: %d" % rc)
+        return U
+
+    def est_timestep(self, closures, U, dx, cfl, nghost=NG, lo=(0, 0, 0)):
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        nz, ny, nx = (s - 2 * nghost for s in U.shape[1:])
+        hi = (lo[0] + nx - 1, lo[1] + ny - 1, lo[2] + nz - 1)
+        cl = c_closures(closures)
+        return float(self.lib.orc_est_timestep(ctypes.byref(cl), _i3(lo), _i3(hi), _d3(dx), _ptr(U),
+                                               int(nghost), float(cfl)))
+
+    def advance(self, scheme, closures, S1, dxinv, bc_lo, bc_hi, dt, order_rk=3, stages_rk=3,
+                lo=(0, 0, 0), nthreads=1):
+        """One CNS::advance step; returns S2 (ghosted; valid cells meaningful)."""
+        S1 = np.ascontiguousarray(S1, dtype=np.float64).copy()
+        S2 = np.zeros_like(S1)
+        nz, ny, nx = (s - 2 * NG for s in S1.shape[1:])
+        hi = (lo[0] + nx - 1, lo[1] + ny - 1, lo[2] + nz - 1)
+        sc, cl = c_scheme(scheme), c_closures(closures)
+        rc = self.lib.orc_advance(ctypes.byref(sc), ctypes.byref(cl), _i3(lo), _i3(hi), _d3(dxinv),
+                                  _i3(bc_lo), _i3(bc_hi), int(order_rk), int(stages_rk), float(dt),
+                                  _ptr(S1), _ptr(S2), int(nthreads))
+        if rc:
+            raise RuntimeError("orc_advance failed: %d" % rc)
+        return S2
+
+
+_cache = {}
+
+
+def oracle():
+    """The restatement (always available; built on first use)."""
+    if "orc" not in _cache:
+        _cache["orc"] = Oracle(_build.build_oracle())
+    return _cache["orc"]
+
+
+def reference(closures):
+    """The reference's own sources compiled here for this closure family
+    (constant or Sutherland transport), or None when not built."""
+    key = "ref_const" if int(closures.visc_law) == 0 else "ref_suth"
+    if key not in _cache:
+        p = os.path.join(os.path.dirname(_build.REF_LIB), "libcnsref_%s.so" % key[4:])
+        _cache[key] = Oracle(p) if os.path.exists(p) else None
+    return _cache[key]

@@ -1,0 +1,39 @@
+"""The CPU restatement against the reference build on fresh random inputs.
+
+Runs only where oracle/_ref exists (the reference sources compiled by
+oracle/build_ref.sh); it checks bit-for-bit agreement on inputs the golden
+fixtures do not cover.
+"""
+import numpy as np
+import pytest
+
+from amrsolver_gb300 import problems as P
+from oracle import pyoracle
+
+CL = P.Closures.nondimensional(1.0 / 800.0)
+REF = pyoracle.reference(CL)
+pytestmark = pytest.mark.skipif(REF is None, reason="reference build (oracle/_ref) not present")
+
+SCHEMES = [dict(flux_euler=1, order_keep=o, rhs_visc=v, art_diss=a) for o in (2, 4, 6) for v in (0, 1)
+           for a in (0, 1)] + [dict(flux_euler=f, rhs_visc=v) for f in (0, 2) for v in (0, 1)]
+
+
+@pytest.mark.parametrize("skw", SCHEMES, ids=lambda d: "-".join("%s%s" % kv for kv in d.items()))
+def test_rhs_bitexact(orc, skw):
+    sc = P.Scheme(**skw)
+    rng = np.random.default_rng(len(str(skw)))
+    n = tuple(int(v) for v in rng.integers(3, 9, 3))
+    U = P.random_state(n, seed=int(rng.integers(1 << 30)), amp=0.2)
+    lo = tuple(int(v) for v in rng.integers(-5, 5, 3))
+    dxinv = tuple(float(v) for v in rng.uniform(1.0, 5.0, 3))
+    np.testing.assert_array_equal(orc.rhs(sc, CL, U, dxinv, lo=lo), REF.rhs(sc, CL, U, dxinv, lo=lo))
+
+
+@pytest.mark.parametrize("ork,srk", [(3, 3), (3, 4), (2, 2), (2, 4), (1, 1), (0, 1), (-2, 2)])
+def test_advance_bitexact(orc, ork, srk):
+    sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1)
+    U, dx = P.tgv(10, mach=0.2)
+    dxinv = [1.0 / h for h in dx]
+    a = orc.advance(sc, CL, U, dxinv, (-1, -1, -1), (-1, -1, -1), 3e-3, ork, srk)
+    b = REF.advance(sc, CL, U, dxinv, (-1, -1, -1), (-1, -1, -1), 3e-3, ork, srk)
+    np.testing.assert_array_equal(P.valid(a), P.valid(b))

@@ -1,0 +1,297 @@
+"""ctypes binding of the C ABI in include/amrs_gb300.h.
+
+Device memory comes from torch (cuda float64 tensors in the Array4 layout
+(ncomp, nz+2g, ny+2g, nx+2g)); only raw pointers, strides and sizes cross
+the boundary.  Every call raises AmrsError on a non-zero status.  There is
+no CPU fallback: without the compiled library or a GPU, calls fail.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+from .problems import NCONS, NGHOST
+
+_lib = None
+
+
+class AmrsError(RuntimeError):
+    pass
+
+
+class Array4(ctypes.Structure):
+    _fields_ = [("p", ctypes.c_void_p), ("jstride", ctypes.c_int64), ("kstride", ctypes.c_int64),
+                ("nstride", ctypes.c_int64), ("begin", ctypes.c_int32 * 3), ("end", ctypes.c_int32 * 3),
+                ("ncomp", ctypes.c_int32)]
+
+
+class CClosures(ctypes.Structure):
+    _fields_ = [("gamma", ctypes.c_double), ("cv", ctypes.c_double), ("cp", ctypes.c_double),
+                ("Rspec", ctypes.c_double), ("visc_law", ctypes.c_int32), ("cond_law", ctypes.c_int32),
+                ("visc_ref", ctypes.c_double), ("Tvisc_ref", ctypes.c_double), ("cond_ref", ctypes.c_double),
+                ("Tcond_ref", ctypes.c_double), ("Cshock", ctypes.c_double), ("Cdamp", ctypes.c_double)]
+
+
+class CScheme(ctypes.Structure):
+    _fields_ = [("rhs_euler", ctypes.c_int32), ("rhs_visc", ctypes.c_int32), ("flux_euler", ctypes.c_int32),
+                ("order_keep", ctypes.c_int32), ("art_diss", ctypes.c_int32)]
+
+
+class CBox(ctypes.Structure):
+    _fields_ = [("lo", ctypes.c_int32 * 3), ("hi", ctypes.c_int32 * 3)]
+
+
+class RkOp(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("dst", ctypes.c_int32), ("x", ctypes.c_int32), ("y", ctypes.c_int32),
+                ("a", ctypes.c_double), ("b", ctypes.c_double)]
+
+
+class StageProg(ctypes.Structure):
+    _fields_ = [("src_state", ctypes.c_int32), ("nops", ctypes.c_int32), ("ops", RkOp * 3)]
+
+
+# name -> (restype, argtypes); every symbol declared in include/amrs_gb300.h
+_P = ctypes.c_void_p
+_S = ctypes.c_int
+SIGNATURES = {
+    "amrs_create": (_S, [ctypes.POINTER(_P), ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ctypes.c_int]),
+    "amrs_destroy": (_S, [_P]),
+    "amrs_set_closures": (_S, [_P, ctypes.POINTER(CClosures)]),
+    "amrs_status_string": (ctypes.c_char_p, [_S]),
+    "amrs_last_cuda_error": (ctypes.c_char_p, []),
+    "amrs_version": (ctypes.c_int32, []),
+    "amrs_cuda_arch": (ctypes.c_int32, []),
+    "amrs_rk_program": (_S, [ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.POINTER(StageProg),
+                             ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
+    "amrs_rhs_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double), Array4, Array4, _P]),
+    "amrs_rk_stage_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(StageProg),
+                               ctypes.c_double, Array4, Array4, Array4, _P]),
+    "amrs_fill_halo_box": (_S, [ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                                Array4, _P]),
+    "amrs_est_timestep_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double), ctypes.c_double, Array4,
+                                   _P, _P]),
+    "amrs_boxlist_create": (_S, [_P, ctypes.c_int32, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double),
+                                 ctypes.c_int32, ctypes.POINTER(Array4), ctypes.POINTER(ctypes.c_int32),
+                                 ctypes.c_int32, ctypes.POINTER(CClosures), ctypes.POINTER(_P)]),
+    "amrs_boxlist_destroy": (_S, [_P]),
+    "amrs_boxlist_set_tile": (_S, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                   ctypes.c_int32, ctypes.c_int32]),
+    "amrs_rk_stage_boxlist": (_S, [_P, ctypes.POINTER(StageProg), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                   _P]),
+    "amrs_rk_step_boxlist": (_S, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_int32,
+                                  ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P,
+                                  ctypes.POINTER(ctypes.c_int32)]),
+    "amrs_rhs_vjp_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double), Array4, Array4, Array4,
+                              _P]),
+    "amrs_sync_check": (_S, [_P, _P]),
+    "amrs_probe_fp64_tflops": (_S, [_P, ctypes.POINTER(ctypes.c_double)]),
+    "amrs_debug_tma_enabled": (ctypes.c_int32, [_P]),
+    "amrs_boxlist_tma_enabled": (ctypes.c_int32, [_P]),
+}
+
+
+def lib_path():
+    return _build.LIB
+
+
+def load(build_if_missing=False):
+    """Load the compiled library (never a fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = lib_path()
+    if not os.path.exists(p):
+        if not build_if_missing:
+            raise AmrsError("libamrs_gb300.so not built: run amrsolver_gb300.build.build()")
+        _build.build()
+    L = ctypes.CDLL(p)
+    for name, (rt, at) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = rt
+        f.argtypes = at
+    _lib = L
+    return L
+
+
+def check(status, what=""):
+    if status != 0:
+        L = load()
+        msg = L.amrs_status_string(status).decode()
+        cuda = L.amrs_last_cuda_error().decode()
+        raise AmrsError("%s failed: %s (%d)%s" % (what, msg, status, (" [" + cuda + "]") if cuda else ""))
+
+
+def c_closures(cl):
+    return CClosures(cl.gamma, cl.cv, cl.cp, cl.Rspec, int(cl.visc_law), int(cl.cond_law), cl.visc_ref,
+                     cl.Tvisc_ref, cl.cond_ref, cl.Tcond_ref, cl.Cshock, cl.Cdamp)
+
+
+def c_scheme(sc):
+    return CScheme(int(sc.rhs_euler), int(sc.rhs_visc), int(sc.flux_euler), int(sc.order_keep), int(sc.art_diss))
+
+
+def c_box(lo, n):
+    return CBox((ctypes.c_int32 * 3)(*lo), (ctypes.c_int32 * 3)(*[lo[d] + n[d] - 1 for d in range(3)]))
+
+
+def d3(v):
+    return (ctypes.c_double * 3)(*[float(x) for x in v])
+
+
+def i3(v):
+    return (ctypes.c_int32 * 3)(*[int(x) for x in v])
+
+
+def array4(t, lo, g):
+    """Array4 of a contiguous cuda float64 tensor (ncomp, nz+2g, ny+2g, nx+2g)
+    whose valid box starts at `lo`."""
+    if not t.is_cuda or t.dtype.itemsize != 8 or not t.is_contiguous():
+        raise AmrsError("expected a contiguous cuda float64 tensor")
+    nc, nz, ny, nx = t.shape
+    b = [lo[0] - g, lo[1] - g, lo[2] - g]
+    return Array4(t.data_ptr(), nx, nx * ny, nx * ny * nz, (ctypes.c_int32 * 3)(*b),
+                  (ctypes.c_int32 * 3)(b[0] + nx, b[1] + ny, b[2] + nz), nc)
+
+
+def rk_program(order_rk, stages_rk, dt):
+    L = load()
+    progs = (StageProg * 16)()
+    n = ctypes.c_int32()
+    check(L.amrs_rk_program(order_rk, stages_rk, dt, progs, 16, ctypes.byref(n)), "amrs_rk_program")
+    return [progs[i] for i in range(n.value)]
+
+
+def _stream_ptr(stream):
+    return ctypes.c_void_p(stream.cuda_stream if stream is not None else 0)
+
+
+class Handle:
+    """amrs_handle: scheme + closures bound to one CUDA device."""
+
+    def __init__(self, scheme, closures, device=0):
+        L = load()
+        self._L = L
+        self.scheme = scheme
+        self.closures = closures
+        h = ctypes.c_void_p()
+        sc, cl = c_scheme(scheme), c_closures(closures)
+        check(L.amrs_create(ctypes.byref(h), ctypes.byref(sc), ctypes.byref(cl), int(device)), "amrs_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self._L.amrs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def rhs_box(self, U, dxinv, out, lo=(0, 0, 0), stream=None):
+        """dSdt of one ghost-filled box into `out` (ncomp, nz, ny, nx)."""
+        nz, ny, nx = (s - 2 * NGHOST for s in U.shape[1:])
+        bx = c_box(lo, (nx, ny, nz))
+        check(self._L.amrs_rhs_box(self.h, ctypes.byref(bx), d3(dxinv), array4(U, lo, NGHOST), array4(out, lo, 0),
+                                   _stream_ptr(stream)), "amrs_rhs_box")
+        return out
+
+    def rk_stage_box(self, prog, Uin, U1, Uout, dxinv, lo=(0, 0, 0), stream=None):
+        nz, ny, nx = (s - 2 * NGHOST for s in Uin.shape[1:])
+        g1 = (U1.shape[1] - nz) // 2
+        go = (Uout.shape[1] - nz) // 2
+        bx = c_box(lo, (nx, ny, nz))
+        check(self._L.amrs_rk_stage_box(self.h, ctypes.byref(bx), d3(dxinv), ctypes.byref(prog), 0.0,
+                                        array4(Uin, lo, NGHOST), array4(U1, lo, g1), array4(Uout, lo, go),
+                                        _stream_ptr(stream)), "amrs_rk_stage_box")
+
+    def est_timestep(self, U, dx, cfl, dt_dev, lo=(0, 0, 0), stream=None):
+        nz, ny, nx = (s - 2 * NGHOST for s in U.shape[1:])
+        bx = c_box(lo, (nx, ny, nz))
+        check(self._L.amrs_est_timestep_box(self.h, ctypes.byref(bx), d3(dx), float(cfl), array4(U, lo, NGHOST),
+                                            ctypes.c_void_p(dt_dev.data_ptr()), _stream_ptr(stream)),
+              "amrs_est_timestep_box")
+
+    def sync_check(self, stream=None):
+        check(self._L.amrs_sync_check(self.h, _stream_ptr(stream)), "amrs_sync_check")
+
+    def tma_enabled(self):
+        return int(self._L.amrs_debug_tma_enabled(self.h))
+
+    def probe_fp64_tflops(self):
+        v = ctypes.c_double()
+        check(self._L.amrs_probe_fp64_tflops(self.h, ctypes.byref(v)), "amrs_probe_fp64_tflops")
+        return v.value
+
+
+def fill_halo_box(U, bc_lo, bc_hi, lo=(0, 0, 0), stream=None):
+    L = load()
+    nz, ny, nx = (s - 2 * NGHOST for s in U.shape[1:])
+    bx = c_box(lo, (nx, ny, nz))
+    check(L.amrs_fill_halo_box(ctypes.byref(bx), i3(bc_lo), i3(bc_hi), array4(U, lo, NGHOST), _stream_ptr(stream)),
+          "amrs_fill_halo_box")
+
+
+class BoxList:
+    """amrs_boxlist: many boxes, `nslots` caller-owned ghosted states each."""
+
+    def __init__(self, handle, los, slots, dxinv, closure_index=None, closures=None):
+        L = load()
+        self._L = L
+        self.handle = handle
+        n = len(los)
+        self.n = n
+        self.nslots = len(slots[0])
+        self.slots = slots  # keep tensors alive
+        boxes = (CBox * n)()
+        arr = (Array4 * (n * self.nslots))()
+        dx = (ctypes.c_double * (3 * n))()
+        for b in range(n):
+            U = slots[b][0]
+            nz, ny, nx = (s - 2 * NGHOST for s in U.shape[1:])
+            boxes[b] = c_box(los[b], (nx, ny, nz))
+            for s in range(self.nslots):
+                arr[b * self.nslots + s] = array4(slots[b][s], los[b], NGHOST)
+            dv = dxinv[b] if hasattr(dxinv[0], "__len__") else dxinv
+            for d in range(3):
+                dx[3 * b + d] = float(dv[d])
+        ci = None
+        cls = None
+        ncl = 0
+        if closure_index is not None:
+            ci = (ctypes.c_int32 * n)(*closure_index)
+            ncl = len(closures)
+            cls = (CClosures * ncl)(*[c_closures(c) for c in closures])
+        bl = ctypes.c_void_p()
+        check(L.amrs_boxlist_create(handle.h, n, boxes, dx, self.nslots, arr, ci, ncl, cls, ctypes.byref(bl)),
+              "amrs_boxlist_create")
+        self.bl = bl
+
+    def close(self):
+        if self.bl:
+            self._L.amrs_boxlist_destroy(self.bl)
+            self.bl = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_tile(self, n, tx, ty, kc):
+        check(self._L.amrs_boxlist_set_tile(self.bl, n[0], n[1], n[2], tx, ty, kc), "amrs_boxlist_set_tile")
+
+    def stage(self, prog, s_in, s1, s_out, stream=None):
+        check(self._L.amrs_rk_stage_boxlist(self.bl, ctypes.byref(prog), s_in, s1, s_out, _stream_ptr(stream)),
+              "amrs_rk_stage_boxlist")
+
+    def step(self, order_rk, stages_rk, dt, s1=0, w1=1, w2=2, use_graph=True, stream=None):
+        res = ctypes.c_int32()
+        check(self._L.amrs_rk_step_boxlist(self.bl, order_rk, stages_rk, float(dt), s1, w1, w2, int(use_graph),
+                                           _stream_ptr(stream), ctypes.byref(res)), "amrs_rk_step_boxlist")
+        return res.value
+
+    def tma_enabled(self):
+        return int(self._L.amrs_boxlist_tma_enabled(self.bl))

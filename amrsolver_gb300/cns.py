@@ -1,0 +1,126 @@
+"""Python mirror of the reference's CNS level over the C ABI.
+
+`CNSLevel` keeps the call surface of `class CNS : AmrLevel` for one level
+(src/CNS.h:10-166): `compute_rhs(S, dSdt)` (src/tim/CNS_advance.cpp:186-427),
+`advance(time, dt)` (src/tim/CNS_advance.cpp:14-183), `est_time_step()`
+(src/CNS.cpp:380-395), `compute_initial_dt` / `compute_new_dt`
+(src/CNS.cpp:282-377) and `print_total`'s conserved totals
+(src/CNS.cpp:532-621).  Every numerical step runs in the CUDA library; this
+module only sequences calls and owns the device buffers (torch tensors).
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import capi
+from .problems import NCONS, NGHOST
+
+
+class CNSLevel:
+    """One single-box level: state S1 (U^n) plus two work buffers, all ghosted."""
+
+    def __init__(self, scheme, closures, U0, dx, bc_lo=(-1, -1, -1), bc_hi=(-1, -1, -1), lo=(0, 0, 0),
+                 order_rk=3, stages_rk=3, device=0):
+        self.scheme, self.closures = scheme, closures
+        self.h = capi.Handle(scheme, closures, device)
+        self.dev = torch.device("cuda", device)
+        self.dx = tuple(float(v) for v in dx)
+        self.dxinv = tuple(1.0 / v for v in self.dx)
+        self.lo = tuple(lo)
+        self.bc_lo, self.bc_hi = tuple(bc_lo), tuple(bc_hi)
+        self.order_rk, self.stages_rk = order_rk, stages_rk
+        U0 = np.ascontiguousarray(U0, dtype=np.float64)
+        self.shape = U0.shape
+        self.n = tuple(s - 2 * NGHOST for s in U0.shape[1:][::-1])  # (nx, ny, nz)
+        self.bufs = [torch.from_numpy(U0).to(self.dev), torch.empty_like(torch.from_numpy(U0), device=self.dev),
+                     torch.empty_like(torch.from_numpy(U0), device=self.dev)]
+        self.cur = 0
+        self.time = 0.0
+        self.dt_dev = torch.zeros(1, dtype=torch.float64, device=self.dev)
+
+    # ------------------------------------------------------------ state --
+    @property
+    def S(self):
+        return self.bufs[self.cur]
+
+    def state_host(self):
+        return self.S.cpu().numpy()
+
+    def valid(self, t=None):
+        t = self.S if t is None else t
+        g = NGHOST
+        return t[:, g:-g, g:-g, g:-g]
+
+    # ------------------------------------------------------------ calls --
+    def fill_patch(self, t, stream=None):
+        """Ghost fill of `t` in place (single-level FillPatch)."""
+        capi.fill_halo_box(t, self.bc_lo, self.bc_hi, self.lo, stream)
+
+    def compute_rhs(self, S, dSdt, stream=None):
+        """CNS::compute_rhs for the box: S ghost-filled, dSdt valid-only."""
+        self.h.rhs_box(S, self.dxinv, dSdt, self.lo, stream)
+        return dSdt
+
+    def advance(self, time, dt, stream=None):
+        """CNS::advance: one RK step of order_rk / stages_rk; returns dt."""
+        progs = capi.rk_program(self.order_rk, self.stages_rk, dt)
+        s1 = self.cur
+        work = [i for i in range(3) if i != s1]
+        cur = s1
+        which = 0
+        for p in progs:
+            src = s1 if p.src_state == 0 else cur
+            out = work[which]
+            if out == src:
+                which ^= 1
+                out = work[which]
+            self.fill_patch(self.bufs[src], stream)
+            self.h.rk_stage_box(p, self.bufs[src], self.bufs[s1], self.bufs[out], self.dxinv, self.lo, stream)
+            cur = out
+            which ^= 1
+        self.cur = cur
+        self.time = time + dt
+        return dt
+
+    def est_time_step(self, cfl, stream=None):
+        """CNS::estTimeStep: cfl * min dx/(|u|+c) (host-synchronising)."""
+        self.h.est_timestep(self.S, self.dx, cfl, self.dt_dev, self.lo, stream)
+        return float(self.dt_dev.item())
+
+    def compute_initial_dt(self, cfl):
+        """CNS::computeInitialDt for a single level with dynamic dt."""
+        return self.est_time_step(cfl)
+
+    def compute_new_dt(self, cfl, dt_old, stop_time, change_max=1.1):
+        """CNS::computeNewDt (src/CNS.cpp:319-377): growth capped at 1.1x and
+        the last step clamped to stop_time."""
+        dt_min = min(self.est_time_step(cfl), change_max * dt_old)
+        dt0 = dt_min
+        eps = 0.001 * dt0
+        if stop_time >= 0.0 and self.time + dt0 > stop_time - eps:
+            dt0 = stop_time - self.time
+        return dt0
+
+    def totals(self):
+        """Conserved totals as CNS::printTotal reports them: sum over valid
+        cells times the domain volume (src/CNS.cpp:538-541)."""
+        vol = 1.0
+        for d in range(3):
+            vol *= self.n[d] * self.dx[d]
+        v = self.valid()
+        return (v.reshape(NCONS, -1).sum(dim=1) * vol).cpu().numpy()
+
+    def run(self, stop_time, max_step, cfl=None, dt=None):
+        """The reference's main loop (src/main.cpp:66-75) for one level."""
+        steps = 0
+        if cfl is not None:
+            dt_cur = self.compute_initial_dt(cfl)
+        else:
+            dt_cur = dt
+        while steps < max_step and self.time < stop_time:
+            self.advance(self.time, dt_cur)
+            steps += 1
+            if cfl is not None:
+                dt_cur = self.compute_new_dt(cfl, dt_cur, stop_time)
+        return steps

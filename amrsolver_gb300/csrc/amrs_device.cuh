@@ -1,0 +1,172 @@
+// Device-side types and point functions of the compressible RHS path.
+//
+// Every function keeps the floating-point operation order of the reference
+// function it cites, and the translation units are compiled with
+// -fmad=false, so results are bit-identical to the reference's CPU build.
+// Explicit fma() appears only where one multiplicand is a power of two
+// (exact product), which rounds identically to the separate mul + add.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace amrs {
+
+constexpr int URHO = 0, UMX = 1, UMY = 2, UMZ = 3, UET = 4, NCONS = 5;
+// primitive components; QE = cv*T, stored so KEEP reads it instead of recomputing
+constexpr int QRHO = 0, QU = 1, QV = 2, QW = 3, QT = 4, QPRES = 5, QE = 6, NQ = 7;
+constexpr int NGHOST = 3;
+constexpr int NVF = 12;  // viscous cell fluxes: x,y,z directions x (UMX..UET)
+
+// Array4-like view (amrex::Array4<Real>).
+struct DArr {
+  double* p;
+  long long js, ks, ns;
+  int b0, b1, b2;
+  __host__ __device__ __forceinline__ double& operator()(int i, int j, int k, int n = 0) const {
+    return p[(long long)(i - b0) + (long long)(j - b1) * js + (long long)(k - b2) * ks + (long long)n * ns];
+  }
+  __host__ __device__ __forceinline__ long long off(int i, int j, int k) const {
+    return (long long)(i - b0) + (long long)(j - b1) * js + (long long)(k - b2) * ks;
+  }
+};
+
+// Closures on the device (src/cls/Closures.h:72-182).
+struct DClosures {
+  double gamma, cv, cp, Rspec;
+  int visc_law, cond_law;
+  double visc_ref, Tvisc_ref, cond_ref, Tcond_ref;
+  double Cshock, Cdamp;
+};
+
+// visc_const_t::visc / visc_suth_t::visc (src/cls/Closures.h:103-120)
+__device__ __forceinline__ double visc(const DClosures& c, double T) {
+  if (c.visc_law == 0) return c.visc_ref;
+  return c.visc_ref * T * sqrt(T) / (c.Tvisc_ref + T);
+}
+// cond_const_t::cond / cond_suth_t::cond (src/cls/Closures.h:130-166)
+__device__ __forceinline__ double cond(const DClosures& c, double T) {
+  if (c.cond_law == 0) return c.cond_ref;
+  return c.cond_ref * T * sqrt(T) / (c.Tcond_ref + T);
+}
+
+// std::max / std::min semantics
+__device__ __forceinline__ double rmax(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ double rmin(double a, double b) { return (b < a) ? b : a; }
+
+// cons2prim (src/rhs/CNS_hydro_K.h:15-34) plus QE = cv*T.
+__device__ __forceinline__ void cons2prim(const double u[5], double q[NQ], const DClosures& c) {
+  double rho = rmax(1e-40, u[URHO]);
+  double rhoinv = 1.0 / rho;
+  double ux = u[UMX] * rhoinv;
+  double uy = u[UMY] * rhoinv;
+  double uz = u[UMZ] * rhoinv;
+  double rhoke = 0.5 * rho * (ux * ux + uy * uy + uz * uz);
+  double rhoei = (u[UET] - rhoke);
+  double p = (c.gamma - 1.0) * rhoei;
+  q[QRHO] = rho;
+  q[QU] = ux;
+  q[QV] = uy;
+  q[QW] = uz;
+  q[QPRES] = p;
+  q[QT] = p / (rho * c.Rspec);
+  q[QE] = c.cv * q[QT];
+}
+
+// One KEEP pair term (src/rhs/CentralKEEP.h:19-36 helpers, :76-83 body),
+// already multiplied by its coefficient: the contribution of pair
+// (point 1 = larger index, point 2 = smaller index) to the face flux in
+// direction d.  q1/q2 give rho,u,v,w,T,p,e.
+template <int D>
+__device__ __forceinline__ void keep_pair(const double* q1, const double* q2, double coef, double T[5]) {
+  constexpr int QN = QU + D;
+  const double rhoS = q1[QRHO] + q2[QRHO];
+  const double unS = q1[QN] + q2[QN];
+  const double massflx = 0.25 * rhoS * unS;                    // fgQuad
+  const double ke = 0.5 * (q1[QU] * q2[QU] + q1[QV] * q2[QV] + q1[QW] * q2[QW]);
+  const double t8 = 0.1250 * rhoS * unS;                       // common factor of fghCubic
+  const double cx = t8 * (q1[QU] + q2[QU]);
+  const double cy = t8 * (q1[QV] + q2[QV]);
+  const double cz = t8 * (q1[QW] + q2[QW]);
+  const double ce = t8 * (q1[QE] + q2[QE]);
+  const double fdiv = 0.5 * (q1[QPRES] + q2[QPRES]);           // fDiv
+  const double fgdiv = 0.5 * (q1[QPRES] * q2[QN] + q2[QPRES] * q1[QN]);  // fgDiv
+  T[URHO] = coef * massflx;
+  T[UMX] = coef * (D == 0 ? (cx + fdiv) : cx);
+  T[UMY] = coef * (D == 1 ? (cy + fdiv) : cy);
+  T[UMZ] = coef * (D == 2 ? (cz + fdiv) : cz);
+  T[UET] = coef * (massflx * ke + ce + fgdiv);
+}
+
+// Cell-centred viscous fluxes (src/rhs/CNS_hydro_K.h:108-172) from the
+// primitive values at the cell and its six neighbours.  Output: x, y, z
+// blocks of (UMX..UET); the mass entries are zero in the reference.
+// `qc` centre, `qxm/qxp`, `qym/qyp`, `qzm/qzp` neighbours (u,v,w,T read).
+__device__ __forceinline__ void viscous_cell(const double* qc, const double* qxm, const double* qxp,
+                                             const double* qym, const double* qyp, const double* qzm,
+                                             const double* qzp, const double dxinv[3], const DClosures& c,
+                                             double f[NVF]) {
+  // (a-b)*0.5*dxinv == (a-b)*(0.5*dxinv) exactly: the 0.5 scalings are exact.
+  const double hx = 0.5 * dxinv[0], hy = 0.5 * dxinv[1], hz = 0.5 * dxinv[2];
+  const double ux = qc[QU];
+  const double dudx = (qxp[QU] - qxm[QU]) * hx;
+  const double dvdx = (qxp[QV] - qxm[QV]) * hx;
+  const double dwdx = (qxp[QW] - qxm[QW]) * hx;
+  const double dTdx = (qxp[QT] - qxm[QT]) * hx;
+  const double uy = qc[QV];
+  const double dudy = (qyp[QU] - qym[QU]) * hy;
+  const double dvdy = (qyp[QV] - qym[QV]) * hy;
+  const double dwdy = (qyp[QW] - qym[QW]) * hy;
+  const double dTdy = (qyp[QT] - qym[QT]) * hy;
+  const double uz = qc[QW];
+  const double dudz = (qzp[QU] - qzm[QU]) * hz;
+  const double dvdz = (qzp[QV] - qzm[QV]) * hz;
+  const double dwdz = (qzp[QW] - qzm[QW]) * hz;
+  const double dTdz = (qzp[QT] - qzm[QT]) * hz;
+  const double div = dudx + dvdy + dwdz;
+  const double mu = visc(c, qc[QT]);
+  const double lambda = cond(c, qc[QT]);
+  const double r1_3 = 1.0 / 3.0;
+  const double mu2 = 2.0 * mu;
+  const double tauxx = mu2 * (dudx - r1_3 * div);
+  const double tauxy = mu * (dudy + dvdx);
+  const double tauxz = mu * (dudz + dwdx);
+  const double tauyy = mu2 * (dvdy - r1_3 * div);
+  const double tauyz = mu * (dvdz + dwdy);
+  const double tauzz = mu2 * (dwdz - r1_3 * div);
+  f[0] = -tauxx;
+  f[1] = -tauxy;
+  f[2] = -tauxz;
+  f[3] = -lambda * dTdx - tauxx * ux - tauxy * uy - tauxz * uz;
+  f[4] = -tauxy;
+  f[5] = -tauyy;
+  f[6] = -tauyz;
+  f[7] = -lambda * dTdy - tauxy * ux - tauyy * uy - tauyz * uz;
+  f[8] = -tauxz;
+  f[9] = -tauyz;
+  f[10] = -tauzz;
+  f[11] = -lambda * dTdz - tauxz * ux - tauyz * uy - tauzz * uz;
+}
+
+// RK stage program (AMReX BLAS-1 semantics), registers S1, S2, dS.
+struct DOp {
+  int kind, dst, x, y;
+  double a, b;
+};
+struct DProg {
+  int nops;
+  DOp ops[3];
+};
+
+__device__ __forceinline__ void apply_prog(const DProg& p, double reg[3]) {
+#pragma unroll
+  for (int o = 0; o < 3; ++o) {
+    if (o >= p.nops) break;
+    const DOp& q = p.ops[o];
+    if (q.kind == 0) reg[q.dst] = q.a * reg[q.x] + q.b * reg[q.y];
+    else if (q.kind == 1) reg[q.dst] = reg[q.dst] + q.a * reg[q.x];
+    else if (q.kind == 2) reg[q.dst] = reg[q.x] + q.a * reg[q.dst];
+    else reg[q.dst] = reg[q.x];
+  }
+}
+
+}  // namespace amrs

@@ -1,0 +1,62 @@
+// Launch wrappers of the device kernels (host-callable, no CUDA types in the
+// C ABI: these stay internal to the library).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "amrs_boxes.cuh"
+#include "tma.cuh"
+
+namespace amrs {
+
+// ---- KEEP fused path (rhs_keep.cu)
+cudaError_t launch_prims(const BoxTable& tb, int s_in, long long ncells, int nsm, cudaStream_t st);
+cudaError_t launch_visc(const BoxTable& tb, long long ncells, int nsm, cudaStream_t st);
+cudaError_t launch_keep_face(int order, bool visc, const BoxTable& tb, int s_in, int s_s1, int s_out,
+                             const DProg& prog, int rhs_only, const TmaDesc& tma, int* err, int nwork, int nsm,
+                             cudaStream_t st);
+bool keep_tile_fits(int order, int tx, int ty);
+template <int ORDER> int keep_smem_bytes();
+
+// ---- face-array (reference-structured) path (rhs_plain.cu)
+// Face flux scratch per box: three nodal arrays, described per box in FaceRec.
+struct FaceRec {
+  DArr f[3];    // face fluxes, nodal in direction d, NCONS comps, over [lo,hi] (+1 in d)
+  DArr pf[3];   // WENO physical fluxes over grow(box,3), NCONS comps
+  DArr lam;     // WENO / JST spectral radius over grow(box,3), 3 comps
+  DArr sen;     // JST sensor over grow(box,3), 3 comps
+  DArr slope[3];  // MUSCL slopes per direction over grow(box,1), NCONS comps
+  long long nface[3];  // faces per direction (for flattening)
+};
+struct FaceTable {
+  const FaceRec* fr;
+  const long long* fpre[3];  // prefix of face counts per direction
+  const long long* gpre;     // prefix of grow(box,3) cell counts
+  const long long* vpre;     // prefix of valid cell counts
+};
+
+cudaError_t launch_keep_faces_plain(int order, const BoxTable& tb, const FaceTable& ft, long long nfaces[3],
+                                    int nsm, cudaStream_t st);
+cudaError_t launch_weno(const BoxTable& tb, const FaceTable& ft, int s_in, long long ngcells, long long nfaces[3],
+                        int nsm, cudaStream_t st);
+cudaError_t launch_riemann(const BoxTable& tb, const FaceTable& ft, const long long* spre_d[3],
+                           long long nslope[3], long long nfaces[3], int nsm, cudaStream_t st);
+cudaError_t launch_jst(const BoxTable& tb, const FaceTable& ft, int s_in, long long ngcells, long long nvalid,
+                       long long nfaces[3], int nsm, cudaStream_t st);
+cudaError_t launch_visc_face_add(const BoxTable& tb, const FaceTable& ft, long long nfaces[3], int nsm,
+                                 cudaStream_t st);
+cudaError_t launch_div_stage(const BoxTable& tb, const FaceTable& ft, int s_in, int s_s1, int s_out,
+                             const DProg& prog, int rhs_only, long long nvalid, int nsm, cudaStream_t st);
+
+// ---- utilities (util.cu)
+struct HaloBox {
+  DArr u;
+  int lo[3], hi[3];
+  int bc_lo[3], bc_hi[3];
+  int ncomp;
+};
+cudaError_t launch_halo(const HaloBox& hb, cudaStream_t st);
+cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t st);
+cudaError_t launch_estdt(const BoxTable& tb, int s_in, long long nvalid, double cfl, unsigned long long* bits,
+                         double* dt_out, int nsm, cudaStream_t st);
+
+}  // namespace amrs

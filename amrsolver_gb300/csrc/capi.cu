@@ -1,0 +1,846 @@
+// C ABI of the GB300 RHS + SSP-RK path (include/amrs_gb300.h).
+//
+// Host-side orchestration mirrors CNS::compute_rhs and CNS::advance
+// (src/tim/CNS_advance.cpp:14-427): for every stage, the scheme's kernel
+// sequence runs over a device box table, then the stage's BLAS-1 program is
+// applied in the last kernel's epilogue.  Nothing here synchronises the host
+// except where the header says so.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/amrs_gb300.h"
+#include "amrs_kernels.h"
+
+using namespace amrs;
+
+namespace {
+
+thread_local std::string g_cuda_err;
+
+amrs_status cuda_fail(cudaError_t e, const char* where) {
+  g_cuda_err = std::string(where) + ": " + cudaGetErrorString(e);
+  return AMRS_ERR_CUDA;
+}
+#define CK(call)                                         \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);  \
+  } while (0)
+
+DClosures to_dev(const amrs_closures& c) {
+  DClosures d;
+  d.gamma = c.gamma; d.cv = c.cv; d.cp = c.cp; d.Rspec = c.Rspec;
+  d.visc_law = c.visc_law; d.cond_law = c.cond_law;
+  d.visc_ref = c.visc_ref; d.Tvisc_ref = c.Tvisc_ref;
+  d.cond_ref = c.cond_ref; d.Tcond_ref = c.Tcond_ref;
+  d.Cshock = c.Cshock; d.Cdamp = c.Cdamp;
+  return d;
+}
+
+DArr to_darr(const amrs_array4& a) {
+  DArr d;
+  d.p = a.p; d.js = a.jstride; d.ks = a.kstride; d.ns = a.nstride;
+  d.b0 = a.begin[0]; d.b1 = a.begin[1]; d.b2 = a.begin[2];
+  return d;
+}
+
+// array covers box grown by g with ncomp components?
+bool covers(const amrs_array4& a, const amrs_box& b, int g, int ncomp) {
+  if (!a.p || a.ncomp < ncomp) return false;
+  for (int d = 0; d < 3; ++d)
+    if (a.begin[d] > b.lo[d] - g || a.end[d] < b.hi[d] + g + 1) return false;
+  const long long nx = a.end[0] - a.begin[0], ny = a.end[1] - a.begin[1], nz = a.end[2] - a.begin[2];
+  if (a.jstride < nx || a.kstride < a.jstride * ny || a.nstride < a.kstride * nz) return false;
+  return true;
+}
+
+bool box_ok(const amrs_box& b) {
+  for (int d = 0; d < 3; ++d)
+    if (b.hi[d] < b.lo[d]) return false;
+  return true;
+}
+int bn(const amrs_box& b, int d) { return b.hi[d] - b.lo[d] + 1; }
+long long grown_cells(const amrs_box& b, int g) {
+  return (long long)(bn(b, 0) + 2 * g) * (bn(b, 1) + 2 * g) * (bn(b, 2) + 2 * g);
+}
+
+amrs_status check_scheme(const amrs_scheme& s) {
+  if (s.flux_euler < 0 || s.flux_euler > 2) return AMRS_ERR_SCHEME;
+  if (s.flux_euler == 1 && !(s.order_keep == 2 || s.order_keep == 4 || s.order_keep == 6)) return AMRS_ERR_SCHEME;
+  if (s.art_diss != 0 && s.art_diss != 1) return AMRS_ERR_SCHEME;
+  return AMRS_OK;
+}
+
+// ghost depth of the primitive region each scheme reads
+int prim_ghost(const amrs_scheme& s) {
+  int g = 0;
+  if (s.rhs_euler) {
+    if (s.flux_euler == 1) g = std::max(g, s.order_keep / 2);
+    else if (s.flux_euler == 0) g = std::max(g, 2);  // slopes on grow(bx,1) read +-1
+    if (s.art_diss) g = std::max(g, 1);
+  }
+  if (s.rhs_visc) g = std::max(g, 2);
+  return g;
+}
+
+bool fused_path(const amrs_scheme& s) { return s.rhs_euler && s.flux_euler == 1 && !s.art_diss; }
+
+// Tile choice for one box (the autotuner can override per box size).
+void default_tile(const amrs_box& b, int order, int& tx, int& ty, int& kc, int nsm) {
+  const int nx = bn(b, 0), ny = bn(b, 1), nz = bn(b, 2);
+  static const int cand[][2] = {{32, 8}, {16, 16}, {24, 10}, {8, 30}, {16, 8}, {8, 16}, {8, 8}};
+  double best = 1e300;
+  tx = 16; ty = 8;
+  for (auto& c : cand) {
+    if (!keep_tile_fits(order, c[0], c[1])) continue;
+    const long long ntx = (nx + c[0] - 1) / c[0], nty = (ny + c[1] - 1) / c[1];
+    // cost: lanes issued per useful cell, plus the x/y halo pair overheads
+    const double lanes = (double)ntx * nty * F_THREADS;
+    const double useful = (double)nx * ny;
+    const double halo = 1.0 + (double)(order / 2) / c[0] + (double)(order / 2) / c[1];
+    const double cost = lanes / useful * halo;
+    if (cost < best) { best = cost; tx = c[0]; ty = c[1]; }
+  }
+  const long long ncol = (long long)((nx + tx - 1) / tx) * ((ny + ty - 1) / ty);
+  // enough z chunks to give every SM two tiles, but at least 8 planes each
+  long long want = (2LL * nsm + ncol - 1) / ncol;
+  kc = (int)std::max<long long>(8, (nz + want - 1) / std::max<long long>(want, 1));
+  kc = std::min(kc, nz);
+}
+
+// -------------------------------------------------------------- list ----
+// Host + device state of one box list (a level, or one box for the per-box
+// entry points).
+struct List {
+  int n = 0, nslots = 0;
+  amrs_scheme sc{};
+  int gq = 2;
+  bool fused = true;
+  std::vector<amrs_box> boxes;
+  std::vector<BoxRec> hbox;
+  std::vector<FaceRec> hface;
+  std::vector<long long> pcell, vcell, gcell, valid, fpre[3], spre[3];
+  std::vector<int> fwork;
+  std::vector<DClosures> cls;
+  // device
+  void* dtab = nullptr;   // all tables in one allocation
+  size_t dtab_bytes = 0;
+  void* dscr = nullptr;   // scratch fields in one allocation
+  size_t dscr_bytes = 0;
+  CUtensorMap* dmaps = nullptr;
+  BoxTable tb{};
+  FaceTable ft{};
+  TmaDesc tma{};
+  const long long* d_spre[3] = {nullptr, nullptr, nullptr};
+  long long tot_p = 0, tot_v = 0, tot_g = 0, tot_valid = 0, tot_f[3] = {0, 0, 0}, tot_s[3] = {0, 0, 0};
+  int tot_work = 0;
+  cudaGraphExec_t graph = nullptr;
+  int graph_key[6] = {0, 0, 0, 0, 0, 0};
+  double graph_dt = 0.0;
+  int graph_result = -1;
+  ~List() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (dtab) cudaFree(dtab);
+    if (dscr) cudaFree(dscr);
+  }
+};
+
+}  // namespace
+
+struct amrs_handle {
+  int device = 0;
+  int nsm = 0;
+  amrs_scheme sc{};
+  amrs_closures cl{};
+  int* derr = nullptr;               // device error flag (bounded waits)
+  unsigned long long* dred = nullptr;  // reduction cell
+  bool tma_ok = true;
+  void* encode_fn = nullptr;
+  List* one = nullptr;               // reusable single-box list for per-box calls
+  std::mutex mu;
+};
+
+struct amrs_boxlist {
+  amrs_handle* h;
+  List L;
+};
+
+namespace {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// Tensor map of one box's primitive scratch: dims (x, y, z, comp) over
+// grow(box,3), box {tx+6, ty+2H, 1, NQ}.  Returns false when the layout
+// cannot be described (row pitch not a multiple of 16 bytes, etc.).
+bool make_qmap(amrs_handle* h, const BoxRec& R, int order, CUtensorMap* out) {
+  if (!h->encode_fn || !h->tma_ok) return false;
+  const int H = order / 2;
+  const cuuint64_t dims[4] = {(cuuint64_t)(R.hi[0] - R.lo[0] + 1 + 6), (cuuint64_t)(R.hi[1] - R.lo[1] + 1 + 6),
+                              (cuuint64_t)(R.hi[2] - R.lo[2] + 1 + 6), (cuuint64_t)NQ};
+  const cuuint64_t strides[3] = {(cuuint64_t)R.q.js * 8, (cuuint64_t)R.q.ks * 8, (cuuint64_t)R.q.ns * 8};
+  for (int i = 0; i < 3; ++i)
+    if (strides[i] % 16) return false;
+  if (((uintptr_t)R.q.p) % 16) return false;
+  const cuuint32_t box[4] = {(cuuint32_t)(R.tx + 6), (cuuint32_t)(R.ty + 2 * H), 1u, (cuuint32_t)NQ};
+  if ((box[0] * 8) % 16 || box[0] > 256 || box[1] > 256) return false;
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  CUresult r = reinterpret_cast<EncodeTiledFn>(h->encode_fn)(
+      out, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, R.q.p, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+      CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Build host tables and allocate/upload device tables + scratch.
+amrs_status list_build(amrs_handle* h, List& L, int n, const amrs_box* boxes, const double* dxinv3, int nslots,
+                       const amrs_array4* states, const int32_t* cidx, int ncl, const amrs_closures* cls,
+                       const int* tiles /* per box tx,ty,kc or null */) {
+  L.n = n;
+  L.nslots = nslots;
+  L.sc = h->sc;
+  L.gq = prim_ghost(h->sc);
+  L.fused = fused_path(h->sc);
+  L.boxes.assign(boxes, boxes + n);
+  L.hbox.assign(n, BoxRec{});
+  L.cls.resize(std::max(ncl, 1));
+  if (ncl > 0) for (int c = 0; c < ncl; ++c) L.cls[c] = to_dev(cls[c]);
+  else L.cls[0] = to_dev(h->cl);
+  const int order = h->sc.order_keep;
+  const bool need_faces = !L.fused;
+  const bool need_visc = h->sc.rhs_visc != 0;
+  const bool need_weno = h->sc.rhs_euler && h->sc.flux_euler == 2;
+  const bool need_slope = h->sc.rhs_euler && h->sc.flux_euler == 0;
+  const bool need_jst = h->sc.rhs_euler && h->sc.art_diss == 1;
+  L.pcell.assign(n + 1, 0); L.vcell.assign(n + 1, 0); L.gcell.assign(n + 1, 0); L.valid.assign(n + 1, 0);
+  L.fwork.assign(n + 1, 0);
+  for (int d = 0; d < 3; ++d) { L.fpre[d].assign(n + 1, 0); L.spre[d].assign(n + 1, 0); }
+  // scratch layout: per box, Q [NQ x grow3], VF [NVF x grow1], faces, pf, lam, sen, slopes
+  size_t off = 0;
+  std::vector<size_t> q_off(n), vf_off(n), f_off(n * 3), pf_off(n), lam_off(n), sen_off(n), sl_off(n * 3);
+  for (int b = 0; b < n; ++b) {
+    const amrs_box& B = boxes[b];
+    if (!box_ok(B)) return AMRS_ERR_BOX;
+    q_off[b] = off; off = align_up(off + grown_cells(B, 3) * NQ * 8, 256);
+    if (need_visc) { vf_off[b] = off; off = align_up(off + grown_cells(B, 1) * NVF * 8, 256); }
+    if (need_faces)
+      for (int d = 0; d < 3; ++d) {
+        const long long nf = (long long)(bn(B, 0) + (d == 0)) * (bn(B, 1) + (d == 1)) * (bn(B, 2) + (d == 2));
+        f_off[b * 3 + d] = off; off = align_up(off + nf * NCONS * 8, 256);
+      }
+    if (need_weno) {
+      pf_off[b] = off; off = align_up(off + grown_cells(B, 3) * 3 * NCONS * 8, 256);
+    }
+    if (need_weno || need_jst) { lam_off[b] = off; off = align_up(off + grown_cells(B, 3) * 3 * 8, 256); }
+    if (need_jst) { sen_off[b] = off; off = align_up(off + grown_cells(B, 3) * 3 * 8, 256); }
+    if (need_slope)
+      for (int d = 0; d < 3; ++d) { sl_off[b * 3 + d] = off; off = align_up(off + grown_cells(B, 1) * NCONS * 8, 256); }
+  }
+  if (off > L.dscr_bytes) {
+    if (L.dscr) { cudaFree(L.dscr); L.dscr = nullptr; L.dscr_bytes = 0; }
+    CK(cudaMalloc(&L.dscr, off));
+    L.dscr_bytes = off;
+  }
+  char* S = static_cast<char*>(L.dscr);
+  L.hface.assign(need_faces ? n : 0, FaceRec{});
+  for (int b = 0; b < n; ++b) {
+    const amrs_box& B = boxes[b];
+    BoxRec& R = L.hbox[b];
+    for (int d = 0; d < 3; ++d) {
+      R.lo[d] = B.lo[d]; R.hi[d] = B.hi[d];
+      R.dxinv[d] = dxinv3[3 * b + d];
+      R.dx[d] = 1.0 / dxinv3[3 * b + d];
+    }
+    for (int s = 0; s < nslots && s < MAX_SLOTS; ++s) R.slot[s] = to_darr(states[b * nslots + s]);
+    auto mk = [&](size_t o, int g, int nodal_d, int ncomp_unused) {
+      (void)ncomp_unused;
+      DArr a;
+      a.p = reinterpret_cast<double*>(S + o);
+      const int nx = bn(B, 0) + 2 * g + (nodal_d == 0), ny = bn(B, 1) + 2 * g + (nodal_d == 1),
+                nz = bn(B, 2) + 2 * g + (nodal_d == 2);
+      a.js = nx; a.ks = (long long)nx * ny; a.ns = (long long)nx * ny * nz;
+      a.b0 = B.lo[0] - g; a.b1 = B.lo[1] - g; a.b2 = B.lo[2] - g;
+      return a;
+    };
+    R.q = mk(q_off[b], 3, -1, NQ);
+    if (need_visc) R.vf = mk(vf_off[b], 1, -1, NVF);
+    R.cl = cidx ? cidx[b] : 0;
+    int tx, ty, kc;
+    if (tiles) { tx = tiles[3 * b]; ty = tiles[3 * b + 1]; kc = tiles[3 * b + 2]; }
+    else default_tile(B, order, tx, ty, kc, h->nsm);
+    R.tx = tx; R.ty = ty; R.kc = kc;
+    R.ntx = (bn(B, 0) + tx - 1) / tx; R.nty = (bn(B, 1) + ty - 1) / ty; R.nkz = (bn(B, 2) + kc - 1) / kc;
+    if (need_faces) {
+      FaceRec& F = L.hface[b];
+      for (int d = 0; d < 3; ++d) F.f[d] = mk(f_off[b * 3 + d], 0, d, NCONS);
+      if (need_weno) {
+        DArr pf = mk(pf_off[b], 3, -1, 3 * NCONS);
+        for (int d = 0; d < 3; ++d) { F.pf[d] = pf; F.pf[d].p = pf.p + d * NCONS * pf.ns; }
+      }
+      if (need_weno || need_jst) F.lam = mk(lam_off[b], 3, -1, 3);
+      if (need_jst) F.sen = mk(sen_off[b], 3, -1, 3);
+      if (need_slope) for (int d = 0; d < 3; ++d) F.slope[d] = mk(sl_off[b * 3 + d], 1, -1, NCONS);
+    }
+    const int g = L.gq;
+    L.pcell[b + 1] = L.pcell[b] + grown_cells(B, g);
+    L.vcell[b + 1] = L.vcell[b] + (need_visc ? grown_cells(B, 1) : 0);
+    L.gcell[b + 1] = L.gcell[b] + grown_cells(B, 3);
+    L.valid[b + 1] = L.valid[b] + grown_cells(B, 0);
+    L.fwork[b + 1] = L.fwork[b] + R.ntx * R.nty * R.nkz;
+    for (int d = 0; d < 3; ++d) {
+      const long long nf = (long long)(bn(B, 0) + (d == 0)) * (bn(B, 1) + (d == 1)) * (bn(B, 2) + (d == 2));
+      L.fpre[d][b + 1] = L.fpre[d][b] + nf;
+      const long long ns = (long long)(bn(B, 0) + 2 * (d == 0)) * (bn(B, 1) + 2 * (d == 1)) * (bn(B, 2) + 2 * (d == 2));
+      L.spre[d][b + 1] = L.spre[d][b] + ns;
+    }
+  }
+  L.tot_p = L.pcell[n]; L.tot_v = L.vcell[n]; L.tot_g = L.gcell[n]; L.tot_valid = L.valid[n];
+  L.tot_work = L.fwork[n];
+  for (int d = 0; d < 3; ++d) { L.tot_f[d] = L.fpre[d][n]; L.tot_s[d] = L.spre[d][n]; }
+
+  // tensor maps (fused path only)
+  std::vector<CUtensorMap> maps;
+  bool tma_all = L.fused && h->tma_ok && h->encode_fn;
+  if (tma_all) {
+    maps.resize(n);
+    for (int b = 0; b < n && tma_all; ++b) tma_all = make_qmap(h, L.hbox[b], order, &maps[b]);
+  }
+
+  // device tables in one allocation
+  size_t t = 0;
+  const size_t o_box = t; t = align_up(t + sizeof(BoxRec) * n, 128);
+  const size_t o_face = t; t = align_up(t + sizeof(FaceRec) * L.hface.size(), 128);
+  const size_t o_cls = t; t = align_up(t + sizeof(DClosures) * L.cls.size(), 128);
+  const size_t o_maps = t; t = align_up(t + sizeof(CUtensorMap) * (tma_all ? n : 0), 128);
+  const size_t o_p = t; t = align_up(t + 8 * (n + 1), 128);
+  const size_t o_v = t; t = align_up(t + 8 * (n + 1), 128);
+  const size_t o_g = t; t = align_up(t + 8 * (n + 1), 128);
+  const size_t o_va = t; t = align_up(t + 8 * (n + 1), 128);
+  size_t o_f[3], o_s[3];
+  for (int d = 0; d < 3; ++d) { o_f[d] = t; t = align_up(t + 8 * (n + 1), 128); }
+  for (int d = 0; d < 3; ++d) { o_s[d] = t; t = align_up(t + 8 * (n + 1), 128); }
+  const size_t o_w = t; t = align_up(t + 4 * (n + 1), 128);
+  if (t > L.dtab_bytes) {
+    if (L.dtab) { cudaFree(L.dtab); L.dtab = nullptr; L.dtab_bytes = 0; }
+    CK(cudaMalloc(&L.dtab, t));
+    L.dtab_bytes = t;
+  }
+  std::vector<char> host(t, 0);
+  std::memcpy(&host[o_box], L.hbox.data(), sizeof(BoxRec) * n);
+  if (!L.hface.empty()) std::memcpy(&host[o_face], L.hface.data(), sizeof(FaceRec) * L.hface.size());
+  std::memcpy(&host[o_cls], L.cls.data(), sizeof(DClosures) * L.cls.size());
+  if (tma_all) std::memcpy(&host[o_maps], maps.data(), sizeof(CUtensorMap) * n);
+  std::memcpy(&host[o_p], L.pcell.data(), 8 * (n + 1));
+  std::memcpy(&host[o_v], L.vcell.data(), 8 * (n + 1));
+  std::memcpy(&host[o_g], L.gcell.data(), 8 * (n + 1));
+  std::memcpy(&host[o_va], L.valid.data(), 8 * (n + 1));
+  for (int d = 0; d < 3; ++d) {
+    std::memcpy(&host[o_f[d]], L.fpre[d].data(), 8 * (n + 1));
+    std::memcpy(&host[o_s[d]], L.spre[d].data(), 8 * (n + 1));
+  }
+  std::memcpy(&host[o_w], L.fwork.data(), 4 * (n + 1));
+  CK(cudaMemcpy(L.dtab, host.data(), t, cudaMemcpyHostToDevice));
+  char* D = static_cast<char*>(L.dtab);
+  L.tb.box = reinterpret_cast<const BoxRec*>(D + o_box);
+  L.tb.pcell = reinterpret_cast<const long long*>(D + o_p);
+  L.tb.vcell = reinterpret_cast<const long long*>(D + o_v);
+  L.tb.fwork = reinterpret_cast<const int*>(D + o_w);
+  L.tb.cls = reinterpret_cast<const DClosures*>(D + o_cls);
+  L.tb.n = n;
+  L.tb.gq = L.gq;
+  L.ft.fr = reinterpret_cast<const FaceRec*>(D + o_face);
+  for (int d = 0; d < 3; ++d) {
+    L.ft.fpre[d] = reinterpret_cast<const long long*>(D + o_f[d]);
+    L.d_spre[d] = reinterpret_cast<const long long*>(D + o_s[d]);
+  }
+  L.ft.gpre = reinterpret_cast<const long long*>(D + o_g);
+  L.ft.vpre = reinterpret_cast<const long long*>(D + o_va);
+  L.tma.maps = tma_all ? reinterpret_cast<const CUtensorMap*>(D + o_maps) : nullptr;
+  L.tma.enabled = tma_all ? 1 : 0;
+  return AMRS_OK;
+}
+
+DProg to_dprog(const amrs_stage_prog* p) {
+  DProg d{};
+  d.nops = p ? p->nops : 0;
+  for (int i = 0; i < 3; ++i) {
+    if (p && i < p->nops) {
+      d.ops[i].kind = p->ops[i].kind; d.ops[i].dst = p->ops[i].dst; d.ops[i].x = p->ops[i].x;
+      d.ops[i].y = p->ops[i].y; d.ops[i].a = p->ops[i].a; d.ops[i].b = p->ops[i].b;
+    }
+  }
+  return d;
+}
+
+// One RHS evaluation (+ stage program) over the list: the kernel sequence of
+// CNS::compute_rhs (src/tim/CNS_advance.cpp:186-391).
+amrs_status list_stage(amrs_handle* h, List& L, const DProg& prog, int s_in, int s_s1, int s_out, int rhs_only,
+                       cudaStream_t st) {
+  const amrs_scheme& sc = L.sc;
+  const int nsm = h->nsm;
+  // 1. primitives over the grown boxes
+  if (L.gq > 0 || sc.rhs_visc) CK(launch_prims(L.tb, s_in, L.tot_p, nsm, st));
+  // 2. viscous cell fluxes
+  if (sc.rhs_visc) CK(launch_visc(L.tb, L.tot_v, nsm, st));
+  if (L.fused) {
+    // 3. fused KEEP faces + viscous averages + divergence + stage program
+    CK(launch_keep_face(sc.order_keep, sc.rhs_visc != 0, L.tb, s_in, s_s1, s_out, prog, rhs_only, L.tma, h->derr,
+                        L.tot_work, nsm, st));
+    return AMRS_OK;
+  }
+  long long nf[3] = {L.tot_f[0], L.tot_f[1], L.tot_f[2]};
+  // face arrays start from zero (pure viscous runs add to them)
+  for (int b = 0; b < L.n; ++b)
+    for (int d = 0; d < 3; ++d) {
+      const FaceRec& F = L.hface[b];
+      CK(cudaMemsetAsync(F.f[d].p, 0, (size_t)F.f[d].ns * NCONS * 8, st));
+    }
+  if (sc.rhs_euler) {
+    if (sc.flux_euler == 1) CK(launch_keep_faces_plain(sc.order_keep, L.tb, L.ft, nf, nsm, st));
+    else if (sc.flux_euler == 2) CK(launch_weno(L.tb, L.ft, s_in, L.tot_g, nf, nsm, st));
+    else {
+      long long ns[3] = {L.tot_s[0], L.tot_s[1], L.tot_s[2]};
+      CK(launch_riemann(L.tb, L.ft, L.d_spre, ns, nf, nsm, st));
+    }
+    if (sc.art_diss == 1) {
+      for (int b = 0; b < L.n; ++b) {
+        const FaceRec& F = L.hface[b];
+        CK(cudaMemsetAsync(F.sen.p, 0, (size_t)F.sen.ns * 3 * 8, st));
+        CK(cudaMemsetAsync(F.lam.p, 0, (size_t)F.lam.ns * 3 * 8, st));
+      }
+      CK(launch_jst(L.tb, L.ft, s_in, L.tot_g, L.tot_valid, nf, nsm, st));
+    }
+  }
+  if (sc.rhs_visc) CK(launch_visc_face_add(L.tb, L.ft, nf, nsm, st));
+  CK(launch_div_stage(L.tb, L.ft, s_in, s_s1, s_out, prog, rhs_only, L.tot_valid, nsm, st));
+  return AMRS_OK;
+}
+
+bool same_box(const amrs_box& a, const amrs_box& b) {
+  for (int d = 0; d < 3; ++d)
+    if (a.lo[d] != b.lo[d] || a.hi[d] != b.hi[d]) return false;
+  return true;
+}
+
+// Per-box calls reuse one single-box list; its tables are rebuilt only when
+// the box or the arrays change.
+amrs_status one_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3], const amrs_array4* slots, int nslots) {
+  List*& L = h->one;
+  bool same = L && L->n == 1 && same_box(L->boxes[0], *bx) && L->nslots == nslots;
+  if (same) {
+    const BoxRec& R = L->hbox[0];
+    for (int d = 0; d < 3 && same; ++d) same = R.dxinv[d] == dxinv[d];
+    for (int s = 0; s < nslots && same; ++s) {
+      DArr a = to_darr(slots[s]);
+      same = std::memcmp(&a, &R.slot[s], sizeof(DArr)) == 0;
+    }
+  }
+  if (same) return AMRS_OK;
+  if (!L) L = new (std::nothrow) List();
+  if (!L) return AMRS_ERR_ALLOC;
+  if (L->graph) { cudaGraphExecDestroy(L->graph); L->graph = nullptr; }
+  // the previous tables may still be read by queued kernels
+  CK(cudaDeviceSynchronize());
+  return list_build(h, *L, 1, bx, dxinv, nslots, slots, nullptr, 0, nullptr, nullptr);
+}
+
+}  // namespace
+
+// ===================================================================== API ==
+extern "C" {
+
+int32_t amrs_version(void) { return 100; }
+int32_t amrs_cuda_arch(void) { return 1030; }
+
+const char* amrs_last_cuda_error(void) { return g_cuda_err.c_str(); }
+
+const char* amrs_status_string(amrs_status s) {
+  switch (s) {
+    case AMRS_OK: return "ok";
+    case AMRS_ERR_NULL: return "null pointer";
+    case AMRS_ERR_BOX: return "bad box";
+    case AMRS_ERR_BC: return "unsupported boundary condition";
+    case AMRS_ERR_SCHEME: return "unsupported scheme";
+    case AMRS_ERR_RK: return "unsupported RK order/stages";
+    case AMRS_ERR_CUDA: return "CUDA error";
+    case AMRS_ERR_ALLOC: return "allocation failed";
+    case AMRS_ERR_LAYOUT: return "array layout does not cover the box";
+    case AMRS_ERR_SIZE: return "size beyond limit";
+    case AMRS_ERR_NONFINITE: return "non-finite value";
+    case AMRS_ERR_TIMEOUT: return "device wait timed out";
+    case AMRS_ERR_STATE: return "invalid call sequence";
+  }
+  return "unknown status";
+}
+
+amrs_status amrs_create(amrs_handle** out, const amrs_scheme* scheme, const amrs_closures* closures, int device) {
+  if (!out || !scheme || !closures) return AMRS_ERR_NULL;
+  *out = nullptr;
+  if (amrs_status s = check_scheme(*scheme)) return s;
+  amrs_handle* h = new (std::nothrow) amrs_handle();
+  if (!h) return AMRS_ERR_ALLOC;
+  h->device = device;
+  h->sc = *scheme;
+  h->cl = *closures;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaMalloc(&h->derr, 64);
+  if (e == cudaSuccess) e = cudaMemset(h->derr, 0, 64);
+  if (e == cudaSuccess) e = cudaMalloc(&h->dred, 64);
+  if (e != cudaSuccess) {
+    amrs_status s = cuda_fail(e, "amrs_create");
+    amrs_destroy(h);
+    return s;
+  }
+  const char* tma_env = std::getenv("AMRS_TMA");
+  h->tma_ok = !(tma_env && tma_env[0] == '0');
+  cudaDriverEntryPointQueryResult q;
+  void* fn = nullptr;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    h->encode_fn = fn;
+  *out = h;
+  return AMRS_OK;
+}
+
+amrs_status amrs_destroy(amrs_handle* h) {
+  if (!h) return AMRS_ERR_NULL;
+  cudaSetDevice(h->device);
+  delete h->one;
+  if (h->derr) cudaFree(h->derr);
+  if (h->dred) cudaFree(h->dred);
+  delete h;
+  return AMRS_OK;
+}
+
+amrs_status amrs_set_closures(amrs_handle* h, const amrs_closures* closures) {
+  if (!h || !closures) return AMRS_ERR_NULL;
+  std::lock_guard<std::mutex> lk(h->mu);
+  h->cl = *closures;
+  if (h->one) { CK(cudaDeviceSynchronize()); delete h->one; h->one = nullptr; }
+  return AMRS_OK;
+}
+
+amrs_status amrs_rk_program(int32_t order_rk, int32_t stages_rk, double dt, amrs_stage_prog* st, int32_t cap,
+                            int32_t* nstages) {
+  if (!st || !nstages) return AMRS_ERR_NULL;
+  auto op = [](int kind, int dst, int x, int y, double a, double b) {
+    amrs_rk_op o; o.kind = kind; o.dst = dst; o.x = x; o.y = y; o.a = a; o.b = b; return o;
+  };
+  auto set = [&](int i, int src, int nops, amrs_rk_op a, amrs_rk_op b = amrs_rk_op{}) {
+    st[i].src_state = src; st[i].nops = nops; st[i].ops[0] = a; st[i].ops[1] = b;
+  };
+  const int S1 = 0, S2 = 1, DS = 2;
+  int n = -1;
+  if (order_rk == -2) n = 2;
+  else if (order_rk == 0 || order_rk == 1) n = 1;
+  else if (order_rk == 2) n = (stages_rk >= 2) ? stages_rk : -1;
+  else if (order_rk == 3 && (stages_rk == 3 || stages_rk == 4)) n = stages_rk;
+  if (n < 0) return AMRS_ERR_RK;
+  if (n > cap) return AMRS_ERR_SIZE;
+  std::memset(st, 0, sizeof(amrs_stage_prog) * n);
+  if (order_rk == -2) {  // src/tim/CNS_advance.cpp:51-70
+    set(0, 0, 1, op(0, S2, S1, DS, 1.0, dt));
+    set(1, 1, 2, op(0, S2, S2, S1, 0.5, 0.5), op(1, S2, DS, 0, 0.5 * dt, 0));
+  } else if (order_rk == 0) {  // :71-75
+    set(0, 0, 1, op(3, S2, DS, 0, 0, 0));
+  } else if (order_rk == 1) {  // :76-80
+    set(0, 0, 1, op(0, S2, S1, DS, 1.0, dt));
+  } else if (order_rk == 2) {  // :81-114
+    const int m = stages_rk;
+    for (int i = 1; i <= m - 1; ++i) set(i - 1, i == 1 ? 0 : 1, 1, op(1, S2, DS, 0, dt / double(m - 1), 0));
+    set(m - 1, 1, 2, op(0, S2, S2, DS, double(m - 1), dt), op(0, S2, S1, S2, 1.0 / m, 1.0 / m));
+  } else if (stages_rk == 3) {  // :118-139
+    set(0, 0, 1, op(0, S2, S1, DS, 1.0, dt));
+    set(1, 1, 2, op(2, DS, S2, 0, dt, 0), op(0, S2, S1, DS, 3.0 / 4, 1.0 / 4));
+    set(2, 1, 2, op(2, DS, S2, 0, dt, 0), op(0, S2, S1, DS, 1.0 / 3, 2.0 / 3));
+  } else {  // :141-166
+    set(0, 0, 1, op(0, S2, S1, DS, 1.0, dt / 2));
+    set(1, 1, 1, op(1, S2, DS, 0, dt / 2, 0));
+    set(2, 1, 2, op(0, S2, S1, S2, 2.0 / 3, 1.0 / 3), op(1, S2, DS, 0, dt / 6, 0));
+    set(3, 1, 1, op(1, S2, DS, 0, dt / 2, 0));
+  }
+  *nstages = n;
+  return AMRS_OK;
+}
+
+amrs_status amrs_rhs_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3], amrs_array4 state,
+                         amrs_array4 dsdt, void* stream) {
+  if (!h || !bx || !dxinv) return AMRS_ERR_NULL;
+  if (!box_ok(*bx)) return AMRS_ERR_BOX;
+  if (!covers(state, *bx, NGHOST, NCONS) || !covers(dsdt, *bx, 0, NCONS)) return AMRS_ERR_LAYOUT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  CK(cudaSetDevice(h->device));
+  amrs_array4 slots[3] = {state, state, dsdt};
+  if (amrs_status s = one_box(h, bx, dxinv, slots, 3)) return s;
+  DProg p{};
+  return list_stage(h, *h->one, p, 0, 1, 2, 1, static_cast<cudaStream_t>(stream));
+}
+
+amrs_status amrs_rk_stage_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3], const amrs_stage_prog* prog,
+                              double dt, amrs_array4 stage_in, amrs_array4 s1, amrs_array4 out, void* stream) {
+  (void)dt;
+  if (!h || !bx || !dxinv || !prog) return AMRS_ERR_NULL;
+  if (!box_ok(*bx)) return AMRS_ERR_BOX;
+  if (prog->nops < 0 || prog->nops > 3) return AMRS_ERR_RK;
+  if (!covers(stage_in, *bx, NGHOST, NCONS) || !covers(s1, *bx, 0, NCONS) || !covers(out, *bx, 0, NCONS))
+    return AMRS_ERR_LAYOUT;
+  if (out.p == stage_in.p) return AMRS_ERR_LAYOUT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  CK(cudaSetDevice(h->device));
+  amrs_array4 slots[3] = {stage_in, s1, out};
+  if (amrs_status s = one_box(h, bx, dxinv, slots, 3)) return s;
+  return list_stage(h, *h->one, to_dprog(prog), 0, 1, 2, 0, static_cast<cudaStream_t>(stream));
+}
+
+amrs_status amrs_fill_halo_box(const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3],
+                               amrs_array4 state, void* stream) {
+  if (!domain || !bc_lo || !bc_hi) return AMRS_ERR_NULL;
+  if (!box_ok(*domain)) return AMRS_ERR_BOX;
+  if (!covers(state, *domain, NGHOST, 1)) return AMRS_ERR_LAYOUT;
+  HaloBox hb;
+  hb.u = to_darr(state);
+  hb.ncomp = state.ncomp;
+  for (int d = 0; d < 3; ++d) {
+    if ((bc_lo[d] == -1) != (bc_hi[d] == -1)) return AMRS_ERR_BC;
+    for (int s = 0; s < 2; ++s) {
+      const int p = s ? bc_hi[d] : bc_lo[d];
+      if (p == 1 || p == 6 || p < -1 || p > 6) return AMRS_ERR_BC;
+    }
+    if (bn(*domain, d) < NGHOST && bc_lo[d] != -1 && bc_lo[d] != 2) return AMRS_ERR_BOX;
+    hb.lo[d] = domain->lo[d]; hb.hi[d] = domain->hi[d]; hb.bc_lo[d] = bc_lo[d]; hb.bc_hi[d] = bc_hi[d];
+  }
+  CK(launch_halo(hb, static_cast<cudaStream_t>(stream)));
+  return AMRS_OK;
+}
+
+amrs_status amrs_est_timestep_box(amrs_handle* h, const amrs_box* bx, const double dx[3], double cfl,
+                                  amrs_array4 state, double* dt_device, void* stream) {
+  if (!h || !bx || !dx || !dt_device) return AMRS_ERR_NULL;
+  if (!box_ok(*bx)) return AMRS_ERR_BOX;
+  if (!covers(state, *bx, 0, NCONS)) return AMRS_ERR_LAYOUT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  CK(cudaSetDevice(h->device));
+  amrs_array4 slots[3] = {state, state, state};
+  const double dxinv[3] = {1.0 / dx[0], 1.0 / dx[1], 1.0 / dx[2]};
+  if (amrs_status s = one_box(h, bx, dxinv, slots, 3)) return s;
+  // cns_estdt divides dx by the wave speed: pass dx exactly as given
+  List& L = *h->one;
+  bool exact = true;
+  for (int d = 0; d < 3; ++d) exact = exact && L.hbox[0].dx[d] == dx[d];
+  if (!exact) {
+    for (int d = 0; d < 3; ++d) L.hbox[0].dx[d] = dx[d];
+    CK(cudaMemcpy(const_cast<BoxRec*>(L.tb.box), L.hbox.data(), sizeof(BoxRec), cudaMemcpyHostToDevice));
+  }
+  CK(launch_estdt(L.tb, 0, L.tot_valid, cfl, h->dred, dt_device, h->nsm, static_cast<cudaStream_t>(stream)));
+  return AMRS_OK;
+}
+
+amrs_status amrs_boxlist_create(amrs_handle* h, int32_t nboxes, const amrs_box* boxes, const double* dxinv3,
+                                int32_t nslots, const amrs_array4* states, const int32_t* closure_index,
+                                int32_t nclosures, const amrs_closures* closures, amrs_boxlist** out) {
+  if (!h || !boxes || !dxinv3 || !states || !out) return AMRS_ERR_NULL;
+  *out = nullptr;
+  if (nboxes <= 0 || nslots < 1 || nslots > MAX_SLOTS) return AMRS_ERR_SIZE;
+  if (closure_index && (nclosures <= 0 || !closures)) return AMRS_ERR_NULL;
+  for (int b = 0; b < nboxes; ++b) {
+    if (!box_ok(boxes[b])) return AMRS_ERR_BOX;
+    for (int s = 0; s < nslots; ++s)
+      if (!covers(states[b * nslots + s], boxes[b], NGHOST, NCONS)) return AMRS_ERR_LAYOUT;
+    if (closure_index && (closure_index[b] < 0 || closure_index[b] >= nclosures)) return AMRS_ERR_SIZE;
+  }
+  std::lock_guard<std::mutex> lk(h->mu);
+  CK(cudaSetDevice(h->device));
+  amrs_boxlist* bl = new (std::nothrow) amrs_boxlist();
+  if (!bl) return AMRS_ERR_ALLOC;
+  bl->h = h;
+  amrs_status s = list_build(h, bl->L, nboxes, boxes, dxinv3, nslots, states, closure_index,
+                             closure_index ? nclosures : 0, closures, nullptr);
+  if (s) { delete bl; return s; }
+  *out = bl;
+  return AMRS_OK;
+}
+
+amrs_status amrs_boxlist_destroy(amrs_boxlist* bl) {
+  if (!bl) return AMRS_ERR_NULL;
+  cudaSetDevice(bl->h->device);
+  cudaDeviceSynchronize();
+  delete bl;
+  return AMRS_OK;
+}
+
+amrs_status amrs_boxlist_set_tile(amrs_boxlist* bl, int32_t nx, int32_t ny, int32_t nz, int32_t tx, int32_t ty,
+                                  int32_t kchunk) {
+  if (!bl) return AMRS_ERR_NULL;
+  List& L = bl->L;
+  if (!keep_tile_fits(L.sc.order_keep, tx, ty) || kchunk < 1) return AMRS_ERR_SIZE;
+  std::lock_guard<std::mutex> lk(bl->h->mu);
+  CK(cudaSetDevice(bl->h->device));
+  CK(cudaDeviceSynchronize());
+  std::vector<int> tiles(3 * L.n);
+  std::vector<amrs_array4> states(L.n * L.nslots);
+  std::vector<double> dxinv(3 * L.n);
+  std::vector<int32_t> cidx(L.n);
+  std::vector<amrs_closures> cls(L.cls.size());
+  for (int b = 0; b < L.n; ++b) {
+    const BoxRec& R = L.hbox[b];
+    const bool match = (nx == 0 && ny == 0 && nz == 0) ||
+                       (bn(L.boxes[b], 0) == nx && bn(L.boxes[b], 1) == ny && bn(L.boxes[b], 2) == nz);
+    tiles[3 * b] = match ? tx : R.tx;
+    tiles[3 * b + 1] = match ? ty : R.ty;
+    tiles[3 * b + 2] = match ? std::min<int>(kchunk, bn(L.boxes[b], 2)) : R.kc;
+    for (int d = 0; d < 3; ++d) dxinv[3 * b + d] = R.dxinv[d];
+    cidx[b] = R.cl;
+    for (int s = 0; s < L.nslots; ++s) {
+      amrs_array4 a{};
+      a.p = R.slot[s].p; a.jstride = R.slot[s].js; a.kstride = R.slot[s].ks; a.nstride = R.slot[s].ns;
+      a.begin[0] = R.slot[s].b0; a.begin[1] = R.slot[s].b1; a.begin[2] = R.slot[s].b2;
+      const amrs_box& B = L.boxes[b];
+      for (int d = 0; d < 3; ++d) a.end[d] = B.hi[d] + NGHOST + 1;
+      a.ncomp = NCONS;
+      states[b * L.nslots + s] = a;
+    }
+  }
+  for (size_t c = 0; c < L.cls.size(); ++c) {
+    const DClosures& d = L.cls[c];
+    amrs_closures& o = cls[c];
+    o.gamma = d.gamma; o.cv = d.cv; o.cp = d.cp; o.Rspec = d.Rspec; o.visc_law = d.visc_law; o.cond_law = d.cond_law;
+    o.visc_ref = d.visc_ref; o.Tvisc_ref = d.Tvisc_ref; o.cond_ref = d.cond_ref; o.Tcond_ref = d.Tcond_ref;
+    o.Cshock = d.Cshock; o.Cdamp = d.Cdamp;
+  }
+  std::vector<amrs_box> boxes = L.boxes;
+  if (L.graph) { cudaGraphExecDestroy(L.graph); L.graph = nullptr; }
+  return list_build(bl->h, L, L.n, boxes.data(), dxinv.data(), L.nslots, states.data(), cidx.data(),
+                    (int)cls.size(), cls.data(), tiles.data());
+}
+
+amrs_status amrs_rk_stage_boxlist(amrs_boxlist* bl, const amrs_stage_prog* prog, int32_t in, int32_t s1, int32_t out,
+                                  void* stream) {
+  if (!bl || !prog) return AMRS_ERR_NULL;
+  List& L = bl->L;
+  if (in < 0 || s1 < 0 || out < 0 || in >= L.nslots || s1 >= L.nslots || out >= L.nslots || in == out)
+    return AMRS_ERR_SIZE;
+  CK(cudaSetDevice(bl->h->device));
+  return list_stage(bl->h, L, to_dprog(prog), in, s1, out, 0, static_cast<cudaStream_t>(stream));
+}
+
+amrs_status amrs_rk_step_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t stages_rk, double dt, int32_t s1,
+                                 int32_t w1, int32_t w2, int32_t use_graph, void* stream, int32_t* result_slot) {
+  if (!bl || !result_slot) return AMRS_ERR_NULL;
+  List& L = bl->L;
+  if (s1 < 0 || w1 < 0 || w2 < 0 || s1 >= L.nslots || w1 >= L.nslots || w2 >= L.nslots || s1 == w1 || s1 == w2 ||
+      w1 == w2)
+    return AMRS_ERR_SIZE;
+  amrs_stage_prog progs[16];
+  int32_t ns = 0;
+  if (amrs_status s = amrs_rk_program(order_rk, stages_rk, dt, progs, 16, &ns)) return s;
+  CK(cudaSetDevice(bl->h->device));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // slot rotation: stage input is S1 for src_state 0, else the last output;
+  // outputs alternate between the two work slots.
+  auto record = [&](cudaStream_t s, int* res) -> amrs_status {
+    int cur = s1;  // holds S2 values (stage input)
+    int outs[2] = {w1, w2};
+    int which = 0;
+    for (int i = 0; i < ns; ++i) {
+      const int in = (progs[i].src_state == 0) ? s1 : cur;
+      int out = outs[which];
+      if (out == in) { which ^= 1; out = outs[which]; }
+      if (amrs_status e = list_stage(bl->h, L, to_dprog(&progs[i]), in, s1, out, 0, s)) return e;
+      cur = out;
+      which ^= 1;
+    }
+    *res = cur;
+    return AMRS_OK;
+  };
+  if (!use_graph) return record(st, result_slot);
+  const int key[6] = {order_rk, stages_rk, s1, w1, w2, 1};
+  if (!L.graph || std::memcmp(key, L.graph_key, sizeof(key)) != 0 || L.graph_dt != dt) {
+    if (L.graph) { cudaGraphExecDestroy(L.graph); L.graph = nullptr; }
+    cudaStream_t cs;
+    CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t g;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) { cudaStreamDestroy(cs); return cuda_fail(e, "cudaStreamBeginCapture"); }
+    int res = -1;
+    amrs_status rs = record(cs, &res);
+    e = cudaStreamEndCapture(cs, &g);
+    cudaStreamDestroy(cs);
+    if (rs) { if (e == cudaSuccess) cudaGraphDestroy(g); return rs; }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&L.graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    std::memcpy(L.graph_key, key, sizeof(key));
+    L.graph_dt = dt;
+    L.graph_result = res;
+  }
+  CK(cudaGraphLaunch(L.graph, st));
+  *result_slot = L.graph_result;
+  return AMRS_OK;
+}
+
+amrs_status amrs_rhs_vjp_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3], amrs_array4 state,
+                             amrs_array4 vbar, amrs_array4 ubar, void* stream) {
+  (void)h; (void)bx; (void)dxinv; (void)state; (void)vbar; (void)ubar; (void)stream;
+  return AMRS_ERR_SCHEME;
+}
+
+// Synchronise `stream`, then report (and clear) the device error flag set by
+// bounded waits.  Host-synchronising.
+amrs_status amrs_sync_check(amrs_handle* h, void* stream) {
+  if (!h) return AMRS_ERR_NULL;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+  int flag = 0;
+  CK(cudaMemcpy(&flag, h->derr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag) {
+    CK(cudaMemset(h->derr, 0, sizeof(int)));
+    return AMRS_ERR_TIMEOUT;
+  }
+  return AMRS_OK;
+}
+
+// Measured FP64 FMA throughput of the handle's device in TFLOP/s (an FMA
+// counts 2 flops): 2 CTAs of 256 threads per SM, eight DFMA chains each,
+// timed with CUDA events after one warm-up launch.  Host-synchronising.
+amrs_status amrs_probe_fp64_tflops(amrs_handle* h, double* tflops) {
+  if (!h || !tflops) return AMRS_ERR_NULL;
+  CK(cudaSetDevice(h->device));
+  const int blocks = 2 * h->nsm, iters = 8192;
+  double* buf = nullptr;
+  CK(cudaMalloc(&buf, sizeof(double) * blocks * 256));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaError_t e = launch_fp64_probe(buf, blocks, iters, 0);
+  if (e == cudaSuccess) e = cudaEventRecord(e0, 0);
+  if (e == cudaSuccess) e = launch_fp64_probe(buf, blocks, iters, 0);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, 0);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  if (e != cudaSuccess) return cuda_fail(e, "amrs_probe_fp64_tflops");
+  *tflops = 2.0 * 8.0 * (double)blocks * 256.0 * iters / (ms * 1e-3) / 1e12;
+  return AMRS_OK;
+}
+
+// Whether the fused face kernel of this handle's last single-box list stages
+// its planes with TMA (1) or with plain loads (0).
+int32_t amrs_debug_tma_enabled(amrs_handle* h) { return (h && h->one) ? h->one->tma.enabled : -1; }
+int32_t amrs_boxlist_tma_enabled(amrs_boxlist* bl) { return bl ? bl->L.tma.enabled : -1; }
+
+}  // extern "C"

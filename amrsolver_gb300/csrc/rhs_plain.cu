@@ -1,0 +1,561 @@
+// Face-array RHS path: the reference's kernel sequence, one kernel per
+// sub-operation, flattened over a box list.  It carries the schemes that
+// have no fused kernel yet (WENO5-JS LLF, MUSCL + Riemann, JST dissipation)
+// and a KEEP variant kept as the "plain per-box" baseline.
+//
+//   Euler face fluxes  -> FaceRec::f[d]   (KEEP / WENO / Riemann)
+//   JST dissipation    -> subtracted from f[d]
+//   viscous averages   -> added to f[d]   (cell fluxes from visc_cell_kernel)
+//   divergence + RK stage program -> output slot
+//
+// Operation order follows the cited reference functions and the file is
+// built with -fmad=false, so results match the reference's CPU build
+// (WENO5 squares its smoothness terms directly, where the reference calls
+// pow(x, 2); the two can differ in the last bit).
+#include "amrs_kernels.h"
+
+namespace amrs {
+
+// face index -> (box, direction, i, j, k) over faces nodal in d
+struct FaceIdx {
+  int b, d, i, j, k;
+};
+
+__device__ __forceinline__ bool decode_face(const BoxTable& tb, const FaceTable& ft, long long g, FaceIdx& f) {
+  long long base = 0;
+  for (int d = 0; d < 3; ++d) {
+    const long long tot = ft.fpre[d][tb.n];
+    if (g < base + tot) {
+      const long long l = g - base;
+      const int b = find_box_ll(ft.fpre[d], tb.n, l);
+      const BoxRec& R = tb.box[b];
+      const int loc = (int)(l - ft.fpre[d][b]);
+      const int nx = R.hi[0] - R.lo[0] + 1 + (d == 0), ny = R.hi[1] - R.lo[1] + 1 + (d == 1);
+      f.b = b;
+      f.d = d;
+      f.i = loc % nx + R.lo[0];
+      const int t = loc / nx;
+      f.j = t % ny + R.lo[1];
+      f.k = t / ny + R.lo[2];
+      return true;
+    }
+    base += tot;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void decode_cell(const BoxRec& R, int loc, int g, int& i, int& j, int& k) {
+  const int nx = R.hi[0] - R.lo[0] + 1 + 2 * g, ny = R.hi[1] - R.lo[1] + 1 + 2 * g;
+  i = loc % nx + R.lo[0] - g;
+  const int t = loc / nx;
+  j = t % ny + R.lo[1] - g;
+  k = t / ny + R.lo[2] - g;
+}
+
+static int grid_for(long long n, int nsm) {
+  long long blocks = (n + 255) / 256;
+  const long long cap = (long long)nsm * 8;
+  return (int)(blocks < cap ? (blocks < 1 ? 1 : blocks) : cap);
+}
+
+// ------------------------------------------------------- KEEP, plain ----
+// src/rhs/CentralKEEP.h:40-145, one face per thread, pairs summed in the
+// reference's (l, m) order without sharing between faces.
+template <int ORDER>
+__global__ void __launch_bounds__(256) keep_faces_plain_kernel(BoxTable tb, FaceTable ft, long long total) {
+  constexpr int H = ORDER / 2;
+  double coef[3];
+  if (ORDER == 6) { coef[0] = 6.0 / 4; coef[1] = -6.0 / 20; coef[2] = 2.0 / 60; }
+  else if (ORDER == 4) { coef[0] = 4.0 / 3; coef[1] = -2.0 / 12; coef[2] = 0.0; }
+  else { coef[0] = 1.0; coef[1] = 0.0; coef[2] = 0.0; }
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    FaceIdx f;
+    if (!decode_face(tb, ft, g, f)) continue;
+    const BoxRec& R = tb.box[f.b];
+    const DArr Q = R.q;
+    const int di = f.d == 0, dj = f.d == 1, dk = f.d == 2;
+    double F[5] = {0, 0, 0, 0, 0};
+#pragma unroll
+    for (int l = 1; l <= H; ++l)
+#pragma unroll
+      for (int m = 0; m < l; ++m) {
+        double q1[NQ], q2[NQ], T[5];
+        const long long o1 = Q.off(f.i + m * di, f.j + m * dj, f.k + m * dk);
+        const long long o2 = Q.off(f.i + (m - l) * di, f.j + (m - l) * dj, f.k + (m - l) * dk);
+#pragma unroll
+        for (int n = 0; n < NQ; ++n) { q1[n] = Q.p[o1 + n * Q.ns]; q2[n] = Q.p[o2 + n * Q.ns]; }
+        if (f.d == 0) keep_pair<0>(q1, q2, coef[l - 1], T);
+        else if (f.d == 1) keep_pair<1>(q1, q2, coef[l - 1], T);
+        else keep_pair<2>(q1, q2, coef[l - 1], T);
+#pragma unroll
+        for (int n = 0; n < 5; ++n) F[n] = F[n] + T[n];
+      }
+    const DArr Fd = ft.fr[f.b].f[f.d];
+    const long long of = Fd.off(f.i, f.j, f.k);
+#pragma unroll
+    for (int n = 0; n < 5; ++n) Fd.p[of + n * Fd.ns] = F[n];
+  }
+}
+
+// ------------------------------------------------------------- WENO5 ----
+// Physical Euler fluxes + max eigenvalue: src/rhs/High_resolution.h:83-121.
+__global__ void __launch_bounds__(256) weno_flux_lambda_kernel(BoxTable tb, FaceTable ft, int s_in, long long total) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    const int b = find_box_ll(ft.gpre, tb.n, g);
+    const BoxRec& R = tb.box[b];
+    const FaceRec& FR = ft.fr[b];
+    int i, j, k;
+    decode_cell(R, (int)(g - ft.gpre[b]), NGHOST, i, j, k);
+    const DArr U = R.slot[s_in];
+    const long long o = U.off(i, j, k);
+    const double gam = tb.cls[R.cl].gamma;
+    const double rhoinv = 1.0 / U.p[o];
+    const double momx = U.p[o + U.ns], momy = U.p[o + 2 * U.ns], momz = U.p[o + 3 * U.ns];
+    const double rhoet = U.p[o + 4 * U.ns];
+    const double ux = momx * rhoinv, uy = momy * rhoinv, uz = momz * rhoinv;
+    const double rhoekin = 0.5 * rhoinv * (momx * momx + momy * momy + momz * momz);
+    const double rhoeint = rhoet - rhoekin;
+    const double P = (gam - 1.0) * rhoeint;
+    const long long op = FR.pf[0].off(i, j, k);
+    const long long ns = FR.pf[0].ns;
+    double* fx = FR.pf[0].p + op;
+    double* fy = FR.pf[1].p + op;
+    double* fz = FR.pf[2].p + op;
+    fx[0] = momx; fx[ns] = momx * ux + P; fx[2 * ns] = momy * ux; fx[3 * ns] = momz * ux; fx[4 * ns] = (rhoet + P) * ux;
+    fy[0] = momy; fy[ns] = momx * uy; fy[2 * ns] = momy * uy + P; fy[3 * ns] = momz * uy; fy[4 * ns] = (rhoet + P) * uy;
+    fz[0] = momz; fz[ns] = momx * uz; fz[2 * ns] = momy * uz; fz[3 * ns] = momz * uz + P; fz[4 * ns] = (rhoet + P) * uz;
+    const double cs = sqrt(gam * P * rhoinv);
+    const long long ol = FR.lam.off(i, j, k);
+    FR.lam.p[ol] = fabs(rmax(rmax(ux + cs, ux - cs), ux));
+    FR.lam.p[ol + FR.lam.ns] = fabs(rmax(rmax(uy + cs, uy - cs), uy));
+    FR.lam.p[ol + 2 * FR.lam.ns] = fabs(rmax(rmax(uz + cs, uz - cs), uz));
+  }
+}
+
+// WENO5-JS (src/rhs/High_resolution.h:124-159), beta[1] with the fourth power.
+__device__ __forceinline__ double weno5js(const double s0, const double s1, const double s2, const double s3,
+                                          const double s4) {
+  const double eps = 1e-40;
+  const double beta0 = (13.0 / 12.0) * (s0 - 2.0 * s1 + s2) * (s0 - 2.0 * s1 + s2) +
+                       0.25 * (s0 - 4.0 * s1 + 3.0 * s2) * (s0 - 4.0 * s1 + 3.0 * s2);
+  const double beta1 = (13.0 / 12.0) * (s1 - 2.0 * s2 + s3) * (s1 - 2.0 * s2 + s3) +
+                       0.25 * (s1 - s3) * (s1 - s3) * (s1 - s3) * (s1 - s3);
+  const double beta2 = (13.0 / 12.0) * (s2 - 2.0 * s3 + s4) * (s2 - 2.0 * s3 + s4) +
+                       0.25 * (3.0 * s2 - 4.0 * s3 + s4) * (3.0 * s2 - 4.0 * s3 + s4);
+  const double e0 = eps + beta0, e1 = eps + beta1, e2 = eps + beta2;
+  const double alpha0 = 0.1 / (e0 * e0);
+  const double alpha1 = 0.6 / (e1 * e1);
+  const double alpha2 = 0.3 / (e2 * e2);
+  const double sum = 1.0 / (alpha0 + alpha1 + alpha2);
+  const double vl0 = 2.0 * s0 - 7.0 * s1 + 11.0 * s2;
+  const double vl1 = -s1 + 5.0 * s2 + 2.0 * s3;
+  const double vl2 = 2.0 * s2 + 5.0 * s3 - s4;
+  return (1.0 / 6.0) * sum * (alpha0 * vl0 + alpha1 * vl1 + alpha2 * vl2);
+}
+
+// LLF-split WENO face flux for all components (src/rhs/High_resolution.h:162-246).
+__global__ void __launch_bounds__(256) weno_face_kernel(BoxTable tb, FaceTable ft, int s_in, long long total) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    FaceIdx f;
+    if (!decode_face(tb, ft, g, f)) continue;
+    const BoxRec& R = tb.box[f.b];
+    const FaceRec& FR = ft.fr[f.b];
+    const DArr U = R.slot[s_in];
+    const DArr PF = FR.pf[f.d];
+    const DArr L = FR.lam;
+    const long long st = (f.d == 0) ? 1 : (f.d == 1 ? L.js : L.ks);
+    const long long su = (f.d == 0) ? 1 : (f.d == 1 ? U.js : U.ks);
+    const long long ol = L.off(f.i, f.j, f.k) + f.d * L.ns;
+    double me = rmax(L.p[ol - 3 * st], L.p[ol - 2 * st]);
+    me = rmax(me, L.p[ol - st]);
+    me = rmax(me, L.p[ol]);
+    me = rmax(me, L.p[ol + st]);
+    me = rmax(me, L.p[ol + 2 * st]);
+    const long long ou = U.off(f.i, f.j, f.k), opf = PF.off(f.i, f.j, f.k);
+    const DArr Fd = FR.f[f.d];
+    const long long of = Fd.off(f.i, f.j, f.k);
+    for (int n = 0; n < 5; ++n) {
+      double df[6], p[6];
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        df[q] = me * U.p[ou + (q - 3) * su + n * U.ns];
+        p[q] = PF.p[opf + (q - 3) * su + n * PF.ns];
+      }
+      double flx = weno5js(0.5 * (p[0] + df[0]), 0.5 * (p[1] + df[1]), 0.5 * (p[2] + df[2]), 0.5 * (p[3] + df[3]),
+                           0.5 * (p[4] + df[4]));
+      flx += weno5js(0.5 * (p[5] - df[5]), 0.5 * (p[4] - df[4]), 0.5 * (p[3] - df[3]), 0.5 * (p[2] - df[2]),
+                     0.5 * (p[1] - df[1]));
+      Fd.p[of + n * Fd.ns] = flx;
+    }
+  }
+}
+
+// ----------------------------------------------------------- Riemann ----
+__device__ __forceinline__ double mc_limiter(double dlft, double drgt) {
+  // src/rhs/Riemann.h:9-17
+  const double dcen = 0.5 * (dlft + drgt);
+  const double dsgn = copysign(1.0, dcen);
+  const double slop = 2.0 * rmin(fabs(dlft), fabs(drgt));
+  const double dlim = (dlft * drgt >= 0.0) ? slop : 0.0;
+  return dsgn * rmin(dlim, fabs(dcen));
+}
+
+// Characteristic slopes in direction d (src/rhs/Riemann.h:19-120).
+__global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, const long long* spre0,
+                                                    const long long* spre1, const long long* spre2,
+                                                    long long tot0, long long tot1, long long tot2) {
+  const long long total = tot0 + tot1 + tot2;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    int d;
+    long long l;
+    const long long* pre;
+    if (g < tot0) { d = 0; l = g; pre = spre0; }
+    else if (g < tot0 + tot1) { d = 1; l = g - tot0; pre = spre1; }
+    else { d = 2; l = g - tot0 - tot1; pre = spre2; }
+    const int b = find_box_ll(pre, tb.n, l);
+    const BoxRec& R = tb.box[b];
+    const int loc = (int)(l - pre[b]);
+    const int nx = R.hi[0] - R.lo[0] + 1 + 2 * (d == 0), ny = R.hi[1] - R.lo[1] + 1 + 2 * (d == 1);
+    const int i = loc % nx + R.lo[0] - (d == 0);
+    const int t = loc / nx;
+    const int j = t % ny + R.lo[1] - (d == 1);
+    const int k = t / ny + R.lo[2] - (d == 2);
+    const DArr q = R.q;
+    const DClosures& cl = tb.cls[R.cl];
+    const long long s = (d == 0) ? 1 : (d == 1 ? q.js : q.ks);
+    const long long o = q.off(i, j, k);
+    const int QN = QU + d, QT1 = (d == 0) ? QV : QU, QT2 = (d == 2) ? QV : QW;
+    auto Q = [&](long long off, int n) { return q.p[off + n * q.ns]; };
+    const double cspeed = sqrt(cl.gamma * cl.Rspec * Q(o, QT)) + (d == 0 ? 2.e-40 : 1.e-40);
+    double dlft = 0.5 * (Q(o, QPRES) - Q(o - s, QPRES)) / cspeed - 0.5 * Q(o, QRHO) * (Q(o, QN) - Q(o - s, QN));
+    double drgt = 0.5 * (Q(o + s, QPRES) - Q(o, QPRES)) / cspeed - 0.5 * Q(o, QRHO) * (Q(o + s, QN) - Q(o, QN));
+    const double d0 = mc_limiter(dlft, drgt);
+    const double cs2 = cspeed * cspeed;
+    dlft = (Q(o, QRHO) - Q(o - s, QRHO)) - (Q(o, QPRES) - Q(o - s, QPRES)) / cs2;
+    drgt = (Q(o + s, QRHO) - Q(o, QRHO)) - (Q(o + s, QPRES) - Q(o, QPRES)) / cs2;
+    const double d1 = mc_limiter(dlft, drgt);
+    dlft = 0.5 * (Q(o, QPRES) - Q(o - s, QPRES)) / cspeed + 0.5 * Q(o, QRHO) * (Q(o, QN) - Q(o - s, QN));
+    drgt = 0.5 * (Q(o + s, QPRES) - Q(o, QPRES)) / cspeed + 0.5 * Q(o, QRHO) * (Q(o + s, QN) - Q(o, QN));
+    const double d2 = mc_limiter(dlft, drgt);
+    const double d3 = mc_limiter(Q(o, QT1) - Q(o - s, QT1), Q(o + s, QT1) - Q(o, QT1));
+    const double d4 = mc_limiter(Q(o, QT2) - Q(o - s, QT2), Q(o + s, QT2) - Q(o, QT2));
+    const DArr S = ft.fr[b].slope[d];
+    const long long os = S.off(i, j, k);
+    S.p[os] = d0;
+    S.p[os + S.ns] = d1;
+    S.p[os + 2 * S.ns] = d2;
+    S.p[os + 3 * S.ns] = d3;
+    S.p[os + 4 * S.ns] = d4;
+  }
+}
+
+// Two-shock approximate Riemann solver (src/rhs/Riemann.h:123-249).
+__device__ void riemann_prob(const double gamma, const double smallp, const double rl, const double ul,
+                             const double pl, const double ut1l, const double ut2l, const double rr, const double ur,
+                             const double pr, const double ut1r, const double ut2r, double& flxrho, double& flxu,
+                             double& flxut, double& flxutt, double& flxe) {
+  const double weakwv = 1.e-3;
+  const double small = 1.e-6;
+  const double clsql = gamma * pl * rl;
+  const double clsqr = gamma * pr * rr;
+  double wl = sqrt(clsql);
+  double wr = sqrt(clsqr);
+  const double cleft = wl / rl;
+  const double cright = wr / rr;
+  const double ccsmall = small * (cleft + cright);
+  double pstar = (wl * pr + wr * pl - wr * wl * (ur - ul)) / (wl + wr);
+  pstar = rmax(pstar, smallp);
+  double pstnm1 = pstar;
+  double wlsq = (0.5 * (gamma - 1.) * (pstar + pl) + pstar) * rl;
+  double wrsq = (0.5 * (gamma - 1.) * (pstar + pr) + pstar) * rr;
+  wl = sqrt(wlsq);
+  wr = sqrt(wrsq);
+  double ustarp = ul - (pstar - pl) / wl;
+  double ustarm = ur + (pstar - pr) / wr;
+  pstar = (wl * pr + wr * pl - wr * wl * (ur - ul)) / (wl + wr);
+  pstar = rmax(pstar, smallp);
+  double ustar = 0.0;
+  for (int iter = 0; iter < 3; ++iter) {
+    wlsq = (0.5 * (gamma - 1.) * (pstar + pl) + pstar) * rl;
+    wrsq = (0.5 * (gamma - 1.) * (pstar + pr) + pstar) * rr;
+    wl = 1. / sqrt(wlsq);
+    wr = 1. / sqrt(wrsq);
+    const double ustnm1 = ustarm;
+    const double ustnp1 = ustarp;
+    ustarm = ur - (pr - pstar) * wr;
+    ustarp = ul + (pl - pstar) * wl;
+    const double dpditer = fabs(pstnm1 - pstar);
+    double zp = fabs(ustarp - ustnp1);
+    if (zp - weakwv * cleft < 0.0) zp = dpditer * wl;
+    double zm = fabs(ustarm - ustnm1);
+    if (zm - weakwv * cright < 0.0) zm = dpditer * wr;
+    const double zz = zp + zm;
+    const double denom = dpditer / rmax(zz, ccsmall);
+    pstnm1 = pstar;
+    pstar = pstar - denom * (ustarm - ustarp);
+    pstar = rmax(pstar, smallp);
+    ustar = 0.5 * (ustarm + ustarp);
+  }
+  double ro, uo, po, sgnm, utrans1, utrans2;
+  if (ustar > 0.) {
+    ro = rl; uo = ul; po = pl; sgnm = 1.; utrans1 = ut1l; utrans2 = ut2l;
+  } else if (ustar < 0.) {
+    ro = rr; uo = ur; po = pr; sgnm = -1.; utrans1 = ut1r; utrans2 = ut2r;
+  } else {
+    uo = 0.5 * (ur + ul);
+    po = 0.5 * (pr + pl);
+    ro = 2. * (rl * rr) / (rl + rr);
+    sgnm = 1.;
+    utrans1 = 0.5 * (ut1l + ut1r);
+    utrans2 = 0.5 * (ut2l + ut2r);
+  }
+  const double wosq = (0.5 * (gamma - 1.) * (pstar + po) + pstar) * ro;
+  const double co = sqrt(gamma * po / ro);
+  const double wo = sqrt(wosq);
+  const double dpjmp = pstar - po;
+  const double rstar = ro / (1. - ro * dpjmp / wosq);
+  const double cstar = sqrt(gamma * pstar / rstar);
+  double spout = co - sgnm * uo;
+  double spin = cstar - sgnm * uo;
+  if (pstar >= po) {
+    spin = wo / ro - sgnm * uo;
+    spout = spin;
+  }
+  const double ss = rmax(spout - spin, spout + spin);
+  const double frac = 0.5 * (1. + (spin + spout) / rmax(ss, ccsmall));
+  double rgdnv, ugdnv, pgdnv;
+  if (spout < 0.) {
+    rgdnv = ro; ugdnv = uo; pgdnv = po;
+  } else if (spin >= 0.) {
+    rgdnv = rstar; ugdnv = ustar; pgdnv = pstar;
+  } else {
+    rgdnv = frac * rstar + (1. - frac) * ro;
+    ugdnv = frac * ustar + (1. - frac) * uo;
+    pgdnv = frac * pstar + (1. - frac) * po;
+  }
+  flxrho = rgdnv * ugdnv;
+  flxu = rgdnv * ugdnv * ugdnv + pgdnv;
+  flxut = rgdnv * ugdnv * utrans1;
+  flxutt = rgdnv * ugdnv * utrans2;
+  flxe = ugdnv * (0.5 * rgdnv * (ugdnv * ugdnv + utrans1 * utrans1 + utrans2 * utrans2) + pgdnv / (gamma - 1.) +
+                  pgdnv);
+}
+
+// MUSCL face states + Riemann flux (src/rhs/Riemann.h:251-337).
+__global__ void __launch_bounds__(256) riemann_face_kernel(BoxTable tb, FaceTable ft, long long total) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    FaceIdx f;
+    if (!decode_face(tb, ft, g, f)) continue;
+    const BoxRec& R = tb.box[f.b];
+    const int d = f.d;
+    const DArr q = R.q;
+    const DArr dq = ft.fr[f.b].slope[d];
+    const DClosures& cl = tb.cls[R.cl];
+    const int QN = QU + d, QT1 = (d == 0) ? QV : QU, QT2 = (d == 2) ? QV : QW;
+    const int UN = UMX + d, UT1 = (d == 0) ? UMY : UMX, UT2 = (d == 2) ? UMY : UMZ;
+    const int im = f.i - (d == 0), jm = f.j - (d == 1), km = f.k - (d == 2);
+    const long long oq = q.off(f.i, f.j, f.k), oqm = q.off(im, jm, km);
+    const long long os = dq.off(f.i, f.j, f.k), osm = dq.off(im, jm, km);
+    auto Q = [&](long long off, int n) { return q.p[off + n * q.ns]; };
+    auto D = [&](long long off, int n) { return dq.p[off + n * dq.ns]; };
+    const double gam = cl.gamma, Rs = cl.Rspec;
+    double cspeed = (d == 2) ? sqrt(gam * Rs * Q(q.off(f.i, f.j, f.k + 1), QT)) + 1.e-40
+                             : sqrt(gam * Rs * Q(oqm, QT)) + 1.e-40;
+    double rl = Q(oqm, QRHO) + 0.5 * ((D(osm, 0) + D(osm, 2)) / cspeed + D(osm, 1));
+    rl = rmax(rl, 1.0e-40);
+    const double ul = Q(oqm, QN) + 0.5 * ((D(osm, 2) - D(osm, 0)) / Q(oqm, QRHO));
+    double pl = Q(oqm, QPRES) + 0.5 * (D(osm, 0) + D(osm, 2)) * cspeed;
+    pl = rmax(pl, 1.0e-40);
+    const double ut1l = Q(oqm, QT1) + 0.5 * D(osm, 3);
+    const double ut2l = Q(oqm, QT2) + 0.5 * D(osm, 4);
+    cspeed = sqrt(gam * Rs * Q(oq, QT)) + 1.e-40;
+    double rr = Q(oq, QRHO) - 0.5 * ((D(os, 0) + D(os, 2)) / cspeed + D(os, 1));
+    rr = rmax(rr, 1.0e-40);
+    const double ur = Q(oq, QN) - 0.5 * ((D(os, 2) - D(os, 0)) / Q(oq, QRHO));
+    double pr = Q(oq, QPRES) - 0.5 * (D(os, 0) + D(os, 2)) * cspeed;
+    pr = rmax(pr, 1.0e-40);
+    const double ut1r = Q(oq, QT1) - 0.5 * D(os, 3);
+    const double ut2r = Q(oq, QT2) - 0.5 * D(os, 4);
+    double frho, fu, fut, futt, fe;
+    riemann_prob(gam, 1.0e-40, rl, ul, pl, ut1l, ut2l, rr, ur, pr, ut1r, ut2r, frho, fu, fut, futt, fe);
+    const DArr Fd = ft.fr[f.b].f[d];
+    const long long of = Fd.off(f.i, f.j, f.k);
+    Fd.p[of + URHO * Fd.ns] = frho;
+    Fd.p[of + UN * Fd.ns] = fu;
+    Fd.p[of + UT1 * Fd.ns] = fut;
+    Fd.p[of + UT2 * Fd.ns] = futt;
+    Fd.p[of + UET * Fd.ns] = fe;
+  }
+}
+
+// --------------------------------------------------------------- JST ----
+__device__ __forceinline__ double discon_sensor(double pp, double pl, double pr) {
+  // src/rhs/CNS_hydro_K.h:39-44
+  const double pjst = pr + 2.0 * pp + pl;
+  const double ptvd = fabs(pr - pp) + fabs(pp - pl);
+  return fabs(2.0 * (pr - 2.0 * pp + pl) / (pjst + ptvd + 1.0e-40));
+}
+
+// Sensor and spectral radius on the valid box (src/rhs/CNS_hydro_K.h:46-75);
+// the arrays are zeroed beforehand, as the reference zeroes its MultiFabs.
+__global__ void __launch_bounds__(256) jst_sensor_kernel(BoxTable tb, FaceTable ft, long long total) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    const int b = find_box_ll(ft.vpre, tb.n, g);
+    const BoxRec& R = tb.box[b];
+    int i, j, k;
+    decode_cell(R, (int)(g - ft.vpre[b]), 0, i, j, k);
+    const DArr q = R.q;
+    const long long o = q.off(i, j, k);
+    auto P = [&](long long off) { return q.p[off + QPRES * q.ns]; };
+    const double pp = P(o);
+    const FaceRec& FR = ft.fr[b];
+    const long long os = FR.sen.off(i, j, k);
+    FR.sen.p[os] = discon_sensor(pp, P(o - 1), P(o + 1));
+    FR.sen.p[os + FR.sen.ns] = discon_sensor(pp, P(o - q.js), P(o + q.js));
+    FR.sen.p[os + 2 * FR.sen.ns] = discon_sensor(pp, P(o - q.ks), P(o + q.ks));
+    const double ux = q.p[o + QU * q.ns], uy = q.p[o + QV * q.ns], uz = q.p[o + QW * q.ns];
+    const double cs = sqrt(tb.cls[R.cl].gamma * pp / q.p[o + QRHO * q.ns]);
+    FR.lam.p[os] = fabs(ux) + cs;
+    FR.lam.p[os + FR.lam.ns] = fabs(uy) + cs;
+    FR.lam.p[os + 2 * FR.lam.ns] = fabs(uz) + cs;
+  }
+}
+
+// JST dissipation subtracted from face fluxes (src/rhs/CNS_hydro_K.h:78-104);
+// y and z read component 0 of sensor and lambda, and the z fourth
+// difference uses k-1 three times, as in the reference.
+__global__ void __launch_bounds__(256) jst_face_kernel(BoxTable tb, FaceTable ft, int s_in, long long total) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    FaceIdx f;
+    if (!decode_face(tb, ft, g, f)) continue;
+    const BoxRec& R = tb.box[f.b];
+    const FaceRec& FR = ft.fr[f.b];
+    const DClosures& cl = tb.cls[R.cl];
+    const DArr U = R.slot[s_in];
+    const long long s = (f.d == 0) ? 1 : (f.d == 1 ? U.js : U.ks);
+    const long long sl = (f.d == 0) ? 1 : (f.d == 1 ? FR.sen.js : FR.sen.ks);
+    const long long ou = U.off(f.i, f.j, f.k), ol = FR.sen.off(f.i, f.j, f.k);
+    const double sen = cl.Cshock * rmax(FR.sen.p[ol - sl], FR.sen.p[ol]);
+    const double rr = rmax(FR.lam.p[ol - sl], FR.lam.p[ol]);
+    const DArr Fd = FR.f[f.d];
+    const long long of = Fd.off(f.i, f.j, f.k);
+    for (int n = 0; n < 5; ++n) {
+      const long long on = ou + n * U.ns;
+      const double dw = (U.p[on] - U.p[on - s]);
+      double fdamp;
+      if (f.d < 2) fdamp = U.p[on + s] - 3.0 * U.p[on] + 3.0 * U.p[on - s] - U.p[on - 2 * s];
+      else fdamp = U.p[on - s] - 3.0 * U.p[on] + 3.0 * U.p[on - s] - U.p[on - s];
+      Fd.p[of + n * Fd.ns] -= (sen * dw - rmax(0.0, cl.Cdamp - sen) * fdamp) * rr;
+    }
+  }
+}
+
+// ---------------------------------------------- viscous face average ----
+// src/rhs/CNS_hydro_K.h:254-261 (mass component adds zero and is skipped).
+__global__ void __launch_bounds__(256) visc_face_add_kernel(BoxTable tb, FaceTable ft, long long total) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    FaceIdx f;
+    if (!decode_face(tb, ft, g, f)) continue;
+    const BoxRec& R = tb.box[f.b];
+    const DArr V = R.vf;
+    const long long s = (f.d == 0) ? 1 : (f.d == 1 ? V.js : V.ks);
+    const long long ov = V.off(f.i, f.j, f.k);
+    const DArr Fd = ft.fr[f.b].f[f.d];
+    const long long of = Fd.off(f.i, f.j, f.k);
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      const int c = 4 * f.d + n;
+      Fd.p[of + (1 + n) * Fd.ns] = fma(0.5, V.p[ov - s + c * V.ns] + V.p[ov + c * V.ns], Fd.p[of + (1 + n) * Fd.ns]);
+    }
+  }
+}
+
+// --------------------------------------- divergence + stage program ----
+// src/tim/CNS_advance.cpp:384-390, then the BLAS-1 program of the stage.
+__global__ void __launch_bounds__(256) div_stage_kernel(BoxTable tb, FaceTable ft, int s_in, int s_s1, int s_out,
+                                                        DProg prog, int rhs_only, long long total) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    const int b = find_box_ll(ft.vpre, tb.n, g);
+    const BoxRec& R = tb.box[b];
+    int i, j, k;
+    decode_cell(R, (int)(g - ft.vpre[b]), 0, i, j, k);
+    const FaceRec& FR = ft.fr[b];
+    const DArr Fx = FR.f[0], Fy = FR.f[1], Fz = FR.f[2];
+    const long long ox = Fx.off(i, j, k), oy = Fy.off(i, j, k), oz = Fz.off(i, j, k);
+    const DArr Uin = R.slot[s_in], U1 = R.slot[s_s1], Uo = R.slot[s_out];
+    for (int n = 0; n < 5; ++n) {
+      const double ds = R.dxinv[0] * (Fx.p[ox + n * Fx.ns] - Fx.p[ox + 1 + n * Fx.ns]) +
+                        R.dxinv[1] * (Fy.p[oy + n * Fy.ns] - Fy.p[oy + Fy.js + n * Fy.ns]) +
+                        R.dxinv[2] * (Fz.p[oz + n * Fz.ns] - Fz.p[oz + Fz.ks + n * Fz.ns]);
+      if (rhs_only) {
+        Uo(i, j, k, n) = ds;
+      } else {
+        double reg[3] = {U1(i, j, k, n), Uin(i, j, k, n), ds};
+        apply_prog(prog, reg);
+        Uo(i, j, k, n) = reg[1];
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------ launchers --
+cudaError_t launch_keep_faces_plain(int order, const BoxTable& tb, const FaceTable& ft, long long nfaces[3], int nsm,
+                                    cudaStream_t st) {
+  const long long tot = nfaces[0] + nfaces[1] + nfaces[2];
+  const int grid = grid_for(tot, nsm);
+  if (order == 2) keep_faces_plain_kernel<2><<<grid, 256, 0, st>>>(tb, ft, tot);
+  else if (order == 4) keep_faces_plain_kernel<4><<<grid, 256, 0, st>>>(tb, ft, tot);
+  else keep_faces_plain_kernel<6><<<grid, 256, 0, st>>>(tb, ft, tot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_weno(const BoxTable& tb, const FaceTable& ft, int s_in, long long ngcells, long long nfaces[3],
+                        int nsm, cudaStream_t st) {
+  weno_flux_lambda_kernel<<<grid_for(ngcells, nsm), 256, 0, st>>>(tb, ft, s_in, ngcells);
+  const long long tot = nfaces[0] + nfaces[1] + nfaces[2];
+  weno_face_kernel<<<grid_for(tot, nsm), 256, 0, st>>>(tb, ft, s_in, tot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_riemann(const BoxTable& tb, const FaceTable& ft, const long long* spre_d[3], long long nslope[3],
+                           long long nfaces[3], int nsm, cudaStream_t st) {
+  const long long ts = nslope[0] + nslope[1] + nslope[2];
+  slope_kernel<<<grid_for(ts, nsm), 256, 0, st>>>(tb, ft, spre_d[0], spre_d[1], spre_d[2], nslope[0], nslope[1],
+                                                  nslope[2]);
+  const long long tot = nfaces[0] + nfaces[1] + nfaces[2];
+  riemann_face_kernel<<<grid_for(tot, nsm), 256, 0, st>>>(tb, ft, tot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_jst(const BoxTable& tb, const FaceTable& ft, int s_in, long long ngcells, long long nvalid,
+                       long long nfaces[3], int nsm, cudaStream_t st) {
+  (void)ngcells;
+  jst_sensor_kernel<<<grid_for(nvalid, nsm), 256, 0, st>>>(tb, ft, nvalid);
+  const long long tot = nfaces[0] + nfaces[1] + nfaces[2];
+  jst_face_kernel<<<grid_for(tot, nsm), 256, 0, st>>>(tb, ft, s_in, tot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_visc_face_add(const BoxTable& tb, const FaceTable& ft, long long nfaces[3], int nsm,
+                                 cudaStream_t st) {
+  const long long tot = nfaces[0] + nfaces[1] + nfaces[2];
+  visc_face_add_kernel<<<grid_for(tot, nsm), 256, 0, st>>>(tb, ft, tot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_div_stage(const BoxTable& tb, const FaceTable& ft, int s_in, int s_s1, int s_out,
+                             const DProg& prog, int rhs_only, long long nvalid, int nsm, cudaStream_t st) {
+  div_stage_kernel<<<grid_for(nvalid, nsm), 256, 0, st>>>(tb, ft, s_in, s_s1, s_out, prog, rhs_only, nvalid);
+  return cudaGetLastError();
+}
+
+}  // namespace amrs

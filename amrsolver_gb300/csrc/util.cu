@@ -1,0 +1,169 @@
+// Ghost fill and time-step reduction kernels.
+#include "amrs_kernels.h"
+
+namespace amrs {
+
+// ---------------------------------------------------------------- halo ----
+// Single-level FillPatch for a box that is the whole domain.  Each ghost
+// cell takes the value of the valid cell obtained by mapping every
+// out-of-range coordinate independently (periodic wrap, foextrap clamp,
+// reflection), with a sign flip for every reflect_odd mapping; this equals
+// AMReX's sequential fill (periodic images, then physical BCs direction by
+// direction).  BC types per component: src/set/CNS_setup.cpp:18-31.
+__device__ __forceinline__ int map_coord(int c, int lo, int hi, int bcl, int bch, int comp, int dir, bool& flip) {
+  if (c >= lo && c <= hi) return c;
+  const int n = hi - lo + 1;
+  const bool low = c < lo;
+  const int phys = low ? bcl : bch;
+  if (phys == -1) {  // periodic
+    int r = (c - lo) % n;
+    if (r < 0) r += n;
+    return lo + r;
+  }
+  if (phys == 2) return low ? lo : hi;  // foextrap
+  const bool vel = comp >= UMX && comp <= UMZ;
+  const bool normal = comp == UMX + dir;
+  bool odd = false;
+  if (phys == 3 || phys == 4) odd = vel && normal;
+  else if (phys == 5) odd = vel;
+  if (odd) flip = !flip;
+  return low ? 2 * lo - c - 1 : 2 * hi - c + 1;
+}
+
+__global__ void __launch_bounds__(256) halo_kernel(HaloBox hb) {
+  const int g = NGHOST;
+  const int nx = hb.hi[0] - hb.lo[0] + 1 + 2 * g, ny = hb.hi[1] - hb.lo[1] + 1 + 2 * g,
+            nz = hb.hi[2] - hb.lo[2] + 1 + 2 * g;
+  const long long total = (long long)nx * ny * nz;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < total;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % nx) + hb.lo[0] - g;
+    const long long t = c / nx;
+    const int j = (int)(t % ny) + hb.lo[1] - g;
+    const int k = (int)(t / ny) + hb.lo[2] - g;
+    const bool inside = i >= hb.lo[0] && i <= hb.hi[0] && j >= hb.lo[1] && j <= hb.hi[1] && k >= hb.lo[2] &&
+                        k <= hb.hi[2];
+    if (inside) continue;
+    for (int n = 0; n < hb.ncomp; ++n) {
+      bool flip = false;
+      const int si = map_coord(i, hb.lo[0], hb.hi[0], hb.bc_lo[0], hb.bc_hi[0], n, 0, flip);
+      const int sj = map_coord(j, hb.lo[1], hb.hi[1], hb.bc_lo[1], hb.bc_hi[1], n, 1, flip);
+      const int sk = map_coord(k, hb.lo[2], hb.hi[2], hb.bc_lo[2], hb.bc_hi[2], n, 2, flip);
+      const double v = hb.u(si, sj, sk, n);
+      hb.u(i, j, k, n) = flip ? -v : v;
+    }
+  }
+}
+
+cudaError_t launch_halo(const HaloBox& hb, cudaStream_t st) {
+  const long long total = (long long)(hb.hi[0] - hb.lo[0] + 7) * (hb.hi[1] - hb.lo[1] + 7) * (hb.hi[2] - hb.lo[2] + 7);
+  long long blocks = (total + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  halo_kernel<<<(int)blocks, 256, 0, st>>>(hb);
+  return cudaGetLastError();
+}
+
+// ----------------------------------------------------------- time step ----
+// cns_estdt (src/cls/CNS_K.h:12-47, z-velocity from UMY as there) reduced
+// with min over cells.  Positive doubles order like their bit patterns, so
+// the block minima meet in one unsigned 64-bit atomicMin; the result is the
+// exact minimum whatever the order.
+__global__ void __launch_bounds__(256) estdt_kernel(BoxTable tb, int s_in, long long total,
+                                                     unsigned long long* bits) {
+  unsigned long long best = ~0ull;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    int b = 0;
+    {
+      // valid-cell prefix = pcell when gq == 0; recompute from box sizes
+      long long acc = 0;
+      for (b = 0; b < tb.n; ++b) {
+        const BoxRec& R = tb.box[b];
+        const long long nc = (long long)(R.hi[0] - R.lo[0] + 1) * (R.hi[1] - R.lo[1] + 1) * (R.hi[2] - R.lo[2] + 1);
+        if (g < acc + nc) { g -= acc; break; }
+        acc += nc;
+      }
+      if (b == tb.n) break;
+      const BoxRec& R = tb.box[b];
+      const int nx = R.hi[0] - R.lo[0] + 1, ny = R.hi[1] - R.lo[1] + 1;
+      const int l = (int)g;
+      g += acc;
+      const int i = l % nx + R.lo[0];
+      const int t = l / nx;
+      const int j = t % ny + R.lo[1];
+      const int k = t / ny + R.lo[2];
+      const DArr S = R.slot[s_in];
+      const DClosures& cl = tb.cls[R.cl];
+      const long long o = S.off(i, j, k);
+      const double rho = S.p[o], mx = S.p[o + S.ns], my = S.p[o + 2 * S.ns], mz = S.p[o + 2 * S.ns];
+      const double rhoinv = 1.0 / rmax(rho, 1.0e-40);
+      const double vx = mx * rhoinv, vy = my * rhoinv, vz = mz * rhoinv;
+      const double ke = 0.5 * rho * (vx * vx + vy * vy + vz * vz);
+      const double rhoei = (S.p[o + 4 * S.ns] - ke);
+      const double p = (cl.gamma - 1.0) * rhoei;
+      const double cs = sqrt(cl.gamma * p * rhoinv);
+      const double dtx = R.dx[0] / (fabs(vx) + cs);
+      const double dty = R.dx[1] / (fabs(vy) + cs);
+      const double dtz = R.dx[2] / (fabs(vz) + cs);
+      const double dt = rmin(dtx, rmin(dty, dtz));
+      const unsigned long long bb = (unsigned long long)__double_as_longlong(dt);
+      if (dt >= 0.0 && bb < best) best = bb;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long v = __shfl_down_sync(0xffffffffu, best, o);
+    best = v < best ? v : best;
+  }
+  __shared__ unsigned long long sm[8];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = best;
+  __syncthreads();
+  if (threadIdx.x < 8) {
+    unsigned long long v = sm[threadIdx.x];
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+      const unsigned long long w = __shfl_down_sync(0xffu, v, o);
+      v = w < v ? w : v;
+    }
+    if (threadIdx.x == 0 && v != ~0ull) atomicMin(bits, v);
+  }
+}
+
+__global__ void estdt_init(unsigned long long* bits) { *bits = ~0ull; }
+
+__global__ void estdt_final(const unsigned long long* bits, double cfl, double* out) {
+  const unsigned long long b = *bits;
+  const double dt = (b == ~0ull) ? 1.7976931348623157e308 : __longlong_as_double((long long)b);
+  *out = dt * cfl;
+}
+
+cudaError_t launch_estdt(const BoxTable& tb, int s_in, long long nvalid, double cfl, unsigned long long* bits,
+                         double* dt_out, int nsm, cudaStream_t st) {
+  estdt_init<<<1, 1, 0, st>>>(bits);
+  long long blocks = (nvalid + 255) / 256;
+  if (blocks > (long long)nsm * 4) blocks = (long long)nsm * 4;
+  if (blocks < 1) blocks = 1;
+  estdt_kernel<<<(int)blocks, 256, 0, st>>>(tb, s_in, nvalid, bits);
+  estdt_final<<<1, 1, 0, st>>>(bits, cfl, dt_out);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------- FP64 probe ----
+// Eight independent DFMA chains per thread: the FP64 pipe's issue rate, the
+// denominator of this path's roofline (the path is FP64-bound on GB300).
+__global__ void __launch_bounds__(256) fp64_probe_kernel(double* out, int iters, double s) {
+  double a0 = threadIdx.x * 1e-3 + 1.0, a1 = a0 + 0.1, a2 = a0 + 0.2, a3 = a0 + 0.3, a4 = a0 + 0.4, a5 = a0 + 0.5,
+         a6 = a0 + 0.6, a7 = a0 + 0.7;
+  for (int it = 0; it < iters; ++it) {
+    a0 = fma(a0, s, 0.5); a1 = fma(a1, s, 0.5); a2 = fma(a2, s, 0.5); a3 = fma(a3, s, 0.5);
+    a4 = fma(a4, s, 0.5); a5 = fma(a5, s, 0.5); a6 = fma(a6, s, 0.5); a7 = fma(a7, s, 0.5);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t st) {
+  fp64_probe_kernel<<<blocks, 256, 0, st>>>(out, iters, 0.999);
+  return cudaGetLastError();
+}
+
+}  // namespace amrs

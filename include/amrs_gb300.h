@@ -1,0 +1,212 @@
+/*
+ * amrs_gb300.h - C ABI of the GB300-native compressible RHS + SSP-RK path.
+ *
+ * Drop-in for the per-box RHS and RK-stage calls of amrsolver:
+ *   CNS::compute_rhs(MultiFab& S, MultiFab& dSdt, Real dt, FluxRegister*, FluxRegister*)
+ *       (src/CNS.h:51, src/tim/CNS_advance.cpp:186-427)
+ *   CNS::advance(Real time, Real dt, int iteration, int ncycle)
+ *       (src/CNS.h:77-80, src/tim/CNS_advance.cpp:14-183)
+ * plus the pieces of AMReX those calls rely on (FillPatch ghost fill,
+ * MultiFab::LinComb/Saxpy/Xpay/Copy, ReduceMin for cns_estdt).
+ *
+ * All arrays are FP64 device memory in the amrex::Array4 convention:
+ * element (i,j,k,n) lives at p[(i-begin[0]) + (j-begin[1])*jstride +
+ * (k-begin[2])*kstride + n*nstride].  Conserved components are
+ * (rho, rho u, rho v, rho w, rho E) as URHO..UET in the reference's prob.h.
+ *
+ * Every function returns an amrs_status; none aborts, none throws, and none
+ * synchronises the host unless its comment says so.  Caller-owned buffers
+ * are never freed by the library.  Scratch memory belongs to the handle.
+ */
+#ifndef AMRS_GB300_H
+#define AMRS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum amrs_status {
+  AMRS_OK = 0,
+  AMRS_ERR_NULL = 1,        /* a required pointer is NULL */
+  AMRS_ERR_BOX = 2,         /* empty box or box outside its array */
+  AMRS_ERR_BC = 3,          /* unsupported or inconsistent boundary codes */
+  AMRS_ERR_SCHEME = 4,      /* unsupported scheme switches */
+  AMRS_ERR_RK = 5,          /* order_rk/stages_rk combination the reference rejects */
+  AMRS_ERR_CUDA = 6,        /* a CUDA runtime call failed (see amrs_last_cuda_error) */
+  AMRS_ERR_ALLOC = 7,       /* device or host allocation failed */
+  AMRS_ERR_LAYOUT = 8,      /* strides/ncomp inconsistent with the box */
+  AMRS_ERR_SIZE = 9,        /* request beyond a documented size limit */
+  AMRS_ERR_NONFINITE = 10,  /* non-finite value detected in a checked result */
+  AMRS_ERR_TIMEOUT = 11,    /* a bounded device-side wait ran out */
+  AMRS_ERR_STATE = 12       /* call sequence error (e.g. graph not built) */
+} amrs_status;
+
+/* amrex::Array4<Real> */
+typedef struct amrs_array4 {
+  double* p;
+  int64_t jstride, kstride, nstride;
+  int32_t begin[3]; /* inclusive lower corner of the allocation (ghosts included) */
+  int32_t end[3];   /* exclusive upper corner */
+  int32_t ncomp;
+} amrs_array4;
+
+/* closures_derived_t<Visc, Cond, calorifically_perfect_gas_t>
+ * (src/cls/Closures.h:72-182).  visc_law/cond_law: 0 = constant
+ * (visc_const_t / cond_const_t), 1 = Sutherland (visc_suth_t / cond_suth_t). */
+typedef struct amrs_closures {
+  double gamma, cv, cp, Rspec;
+  int32_t visc_law, cond_law;
+  double visc_ref, Tvisc_ref, cond_ref, Tcond_ref;
+  double Cshock, Cdamp;
+} amrs_closures;
+
+/* cns.* run-time switches read by CNS::read_params (src/CNS.cpp:85-136).
+ * flux_euler: 0 = MUSCL + Riemann (src/rhs/Riemann.h), 1 = KEEP split form
+ * (src/rhs/CentralKEEP.h), 2 = WENO5-JS with local Lax-Friedrichs splitting
+ * (src/rhs/High_resolution.h).  order_keep: 2, 4 or 6.  art_diss: JST. */
+typedef struct amrs_scheme {
+  int32_t rhs_euler, rhs_visc, flux_euler, order_keep, art_diss;
+} amrs_scheme;
+
+/* Cell-centred index box, inclusive bounds (amrex::Box). */
+typedef struct amrs_box {
+  int32_t lo[3], hi[3];
+} amrs_box;
+
+/* One RK stage as the BLAS-1 program CNS::advance runs after compute_rhs
+ * (src/tim/CNS_advance.cpp:51-166).  Registers: 0 = S1 (old state),
+ * 1 = S2 (new state; equal to the stage input's valid cells), 2 = dSdt.
+ * kind 0 LinComb dst = a*x + b*y; 1 Saxpy dst += a*x; 2 Xpay dst = x + a*dst;
+ * 3 Copy dst = x.  src_state tells which state FillPatch reads for this
+ * stage (0 = S1, 1 = S2).  The stage's result is register 1. */
+typedef struct amrs_rk_op {
+  int32_t kind, dst, x, y;
+  double a, b;
+} amrs_rk_op;
+
+typedef struct amrs_stage_prog {
+  int32_t src_state;
+  int32_t nops;
+  amrs_rk_op ops[3];
+} amrs_stage_prog;
+
+typedef struct amrs_handle amrs_handle;
+
+/* ---- handle ---------------------------------------------------------- */
+
+/* Create a handle bound to CUDA device `device` with the given scheme and
+ * closures (the reference's CNS::variableSetUp + read_params,
+ * src/set/CNS_setup.cpp:90-104, src/CNS.cpp:85-153).  The handle owns the
+ * scratch arena (primitive and viscous-flux fields, reduction cells). */
+amrs_status amrs_create(amrs_handle** out, const amrs_scheme* scheme, const amrs_closures* closures, int device);
+amrs_status amrs_destroy(amrs_handle* h);
+amrs_status amrs_set_closures(amrs_handle* h, const amrs_closures* closures);
+const char* amrs_status_string(amrs_status s);
+/* Last CUDA error string recorded by the library (thread-local). */
+const char* amrs_last_cuda_error(void);
+/* Library version (major*10000 + minor*100 + patch) and the CUDA arch it was built for. */
+int32_t amrs_version(void);
+int32_t amrs_cuda_arch(void);
+
+/* ---- RK programs ------------------------------------------------------ */
+
+/* Fill `progs` (capacity `cap`) with the stage programs of CNS::advance for
+ * (order_rk, stages_rk) and time step dt; *nstages receives the count.
+ * Mirrors src/tim/CNS_advance.cpp:51-166 and the checks of
+ * src/CNS.cpp:119-133.  Host only. */
+amrs_status amrs_rk_program(int32_t order_rk, int32_t stages_rk, double dt, amrs_stage_prog* progs, int32_t cap,
+                            int32_t* nstages);
+
+/* ---- per-box entry points (drop-in for one MFIter iteration) ---------- */
+
+/* dSdt over `bx` from the ghost-filled state (3 ghost cells): one box of
+ * CNS::compute_rhs (src/tim/CNS_advance.cpp:186-391).  `dxinv` is
+ * Geometry::InvCellSizeArray().  Asynchronous on `stream` (cudaStream_t). */
+amrs_status amrs_rhs_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3], amrs_array4 state,
+                         amrs_array4 dsdt, void* stream);
+
+/* One RK stage of one box: RHS of the ghost-filled stage input `stage_in`
+ * followed by the stage's BLAS-1 program, writing register S2 into the
+ * valid cells of `out`.  `s1` holds the old state S1.  `out` must not alias
+ * `stage_in` (the RHS reads neighbours of cells being written); it may
+ * alias `s1`'s storage only if the program never reads S1. */
+amrs_status amrs_rk_stage_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3],
+                              const amrs_stage_prog* prog, double dt, amrs_array4 stage_in, amrs_array4 s1,
+                              amrs_array4 out, void* stream);
+
+/* Ghost fill of a box that is the whole single-box domain: periodic images
+ * and the physical BC types of src/set/CNS_setup.cpp:18-31 for cns.lo_bc /
+ * cns.hi_bc codes (-1 periodic, 2 outflow/foextrap, 3/4 symmetry and slip
+ * wall, 5 no-slip wall).  Codes 1 and 6 (problem bcnormal) are rejected. */
+amrs_status amrs_fill_halo_box(const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3],
+                               amrs_array4 state, void* stream);
+
+/* cfl * min over the valid box of dx_d/(|u_d|+c): CNS::estTimeStep
+ * (src/CNS.cpp:380-395, kernel cns_estdt src/cls/CNS_K.h:12-47).  Writes the
+ * result to *dt_device (device pointer) without a host sync. */
+amrs_status amrs_est_timestep_box(amrs_handle* h, const amrs_box* bx, const double dx[3], double cfl,
+                                  amrs_array4 state, double* dt_device, void* stream);
+
+/* ---- box lists: one persistent launch over many boxes ---------------- */
+
+/* A level's box list with caller-owned state arrays per box, uploaded once.
+ * states[b*nslots + s] is slot s of box b (all ghosted with 3 cells);
+ * out[b] receives dSdt in amrs_rhs_boxlist.  The scratch arena grows to the
+ * list's needs at creation.  Optional per-box closure index (ensembles):
+ * closure_index[b] selects closures[closure_index[b]]. */
+typedef struct amrs_boxlist amrs_boxlist;
+amrs_status amrs_boxlist_create(amrs_handle* h, int32_t nboxes, const amrs_box* boxes, const double* dxinv3,
+                                int32_t nslots, const amrs_array4* states, const int32_t* closure_index,
+                                int32_t nclosures, const amrs_closures* closures, amrs_boxlist** out);
+amrs_status amrs_boxlist_destroy(amrs_boxlist* bl);
+
+/* Tile shape (threads per tile = tx*ty <= 256) and z-chunk per box, as
+ * chosen by the autotuner; tx must be a multiple of 8.  Applies to every
+ * box whose valid extents match (nx,ny,nz) exactly; nx=ny=nz=0 sets the default. */
+amrs_status amrs_boxlist_set_tile(amrs_boxlist* bl, int32_t nx, int32_t ny, int32_t nz, int32_t tx, int32_t ty,
+                                  int32_t kchunk);
+
+/* RK stage over all boxes: stage input slot `in`, old state slot `s1`,
+ * output slot `out` (valid cells).  One launch per kernel kind. */
+amrs_status amrs_rk_stage_boxlist(amrs_boxlist* bl, const amrs_stage_prog* prog, int32_t in, int32_t s1,
+                                  int32_t out, void* stream);
+
+/* Whole RK step (all stages) over all boxes, slots rotating among
+ * s1/work slots as CNS::advance does; result in slot `result`.  When
+ * use_graph != 0 the step is captured once into a CUDA graph and replayed.
+ * Ghost cells of the work slots are left as the caller initialised them
+ * (boxes of a batched level with frozen, analytically filled ghosts). */
+amrs_status amrs_rk_step_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t stages_rk, double dt, int32_t s1,
+                                 int32_t w1, int32_t w2, int32_t use_graph, void* stream, int32_t* result_slot);
+
+/* ---- adjoint ----------------------------------------------------------- */
+
+/* Vector-Jacobian product of one RHS evaluation of one box (KEEP + viscous
+ * path): given the ghost-filled state and a cotangent `vbar` on the valid
+ * cells, writes ubar = (d dSdt/d state)^T vbar into `ubar` over the ghosted
+ * box (ghost entries hold the sensitivities to ghost values).  `ubar` is
+ * overwritten. */
+amrs_status amrs_rhs_vjp_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3], amrs_array4 state,
+                             amrs_array4 vbar, amrs_array4 ubar, void* stream);
+
+/* ---- diagnostics ---------------------------------------------------- */
+
+/* Synchronise `stream`, then report and clear the device error flag that a
+ * bounded device-side wait raises when it gives up (AMRS_ERR_TIMEOUT).
+ * Host-synchronising. */
+amrs_status amrs_sync_check(amrs_handle* h, void* stream);
+/* FP64 FMA throughput of the device (TFLOP/s, FMA = 2 flops), measured
+ * by a DFMA-chain kernel: the roofline denominator of this FP64-bound path.
+ * Host-synchronising. */
+amrs_status amrs_probe_fp64_tflops(amrs_handle* h, double* tflops);
+/* 1 if the fused face kernel stages planes with TMA for the handle's last
+ * per-box call (resp. for the box list), 0 if with plain loads, -1 if none. */
+int32_t amrs_debug_tma_enabled(amrs_handle* h);
+int32_t amrs_boxlist_tma_enabled(amrs_boxlist* bl);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AMRS_GB300_H */

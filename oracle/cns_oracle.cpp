@@ -38,7 +38,12 @@ namespace orc {
 
 // ---------------------------------------------------------------- scalars --
 struct OpCounts { long long add = 0, mul = 0, div = 0, sqrt = 0, cmp = 0; };
-static thread_local OpCounts g_cnt;
+// phases of compute_rhs: 0 cons2prim, 1 Euler face fluxes, 2 JST,
+// 3 viscous cell fluxes, 4 viscous face averages, 5 flux divergence
+constexpr int NPHASE = 6;
+static thread_local OpCounts g_cntp[NPHASE];
+static thread_local int g_phase = 0;
+#define g_cnt g_cntp[g_phase]
 
 // Operation-counting scalar.  +,-,* and / each count 1 in their bucket;
 // sqrt counts 1; comparisons (max/min/branches) count in cmp; unary minus,
@@ -610,6 +615,8 @@ inline void jst_flux(int i, int j, int k, int n, const Arr<R>& lam, const Arr<R>
   fz -= (s * dw - rmax(R(0.0), Cd - s) * fdamp) * rr;
 }
 
+inline void set_phase(int p) { g_phase = p; }
+
 // ------------------------------------------------------------ compute_rhs --
 // CNS::compute_rhs for one box: src/tim/CNS_advance.cpp:186-391.
 // u: ghosted (NGHOST) conserved state; dsdt: valid-only output.
@@ -630,6 +637,7 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
   const int nt = nthreads > 0 ? nthreads : 1;
 #endif
 
+  set_phase(0);
   // 1. cons -> prims over the grown box (:200-208)
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(nt) schedule(static)
@@ -648,6 +656,7 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
   }
 
   // 2. Euler fluxes (:221-224)
+  set_phase(1);
   if (sc.rhs_euler) {
     if (sc.flux_euler == 1) {
       double coeffs[3];
@@ -715,6 +724,7 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
     // JST artificial dissipation (:235-265): sensor/lambda on the valid box,
     // zero elsewhere, then subtracted on every face.
     if (sc.art_diss == 1) {
+      set_phase(2);
       std::vector<R> lb(ncg * 3, R(0.0)), sb(ncg * 3, R(0.0));
       Arr<R> lam = make_arr<R>(lb.data(), bx, g), sen = make_arr<R>(sb.data(), bx, g);
       for (int k = lo2; k <= hi2; ++k)
@@ -739,6 +749,7 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
 
   // 3. viscous fluxes (:276-353): cell fluxes on grow(bx,1), face averages added
   if (sc.rhs_visc) {
+    set_phase(3);
     Box b1 = bx;
     for (int d = 0; d < 3; ++d) { b1.lo[d] -= 1; b1.hi[d] += 1; }
     std::vector<R> vb[3];
@@ -754,6 +765,7 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
       for (int j = lo1 - 1; j <= hi1 + 1; ++j)
         for (int i = lo0 - 1; i <= hi0 + 1; ++i) viscous_fluxes(i, j, k, q, VF, dxinv, cl);
     // ViscousNumericalFluxes: src/rhs/CNS_hydro_K.h:254-261
+    set_phase(4);
     for (int d = 0; d < 3; ++d) {
       const int di = (d == 0), dj = (d == 1), dk = (d == 2);
 #ifdef _OPENMP
@@ -768,6 +780,7 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
   }
 
   // 4. flux divergence (:376-391)
+  set_phase(5);
   Arr<R> ds = make_arr<R>(dsdt, bx, 0);
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(nt) schedule(static)
@@ -1004,8 +1017,9 @@ int orc_compute_rhs_jvp(const OrcScheme* s, const OrcClosures* c, const int* lo,
   return 0;
 }
 
-// Algorithmic operation counts of one RHS evaluation of one box:
-// counts = {add, mul, div, sqrt, cmp}.
+// Algorithmic operation counts of one RHS evaluation of one box, per phase
+// (cons2prim, Euler faces, JST, viscous cells, viscous faces, divergence):
+// counts[5*phase + {0..4}] = {add, mul, div, sqrt, cmp}.
 int orc_compute_rhs_count(const OrcScheme* s, const OrcClosures* c, const int* lo, const int* hi,
                           const double* dxinv, const double* U, long long* counts) {
   if (!s || !c || !lo || !hi || !dxinv || !U || !counts) return 1;
@@ -1013,10 +1027,13 @@ int orc_compute_rhs_count(const OrcScheme* s, const OrcClosures* c, const int* l
   const long long ng = ghosted(b) * NCONS, nv = b.cells() * NCONS;
   std::vector<Cnt> uc(ng), rc(nv);
   for (long long t = 0; t < ng; ++t) uc[t] = Cnt(U[t]);
-  g_cnt = OpCounts();
+  for (int p = 0; p < NPHASE; ++p) g_cntp[p] = OpCounts();
   compute_rhs_box<Cnt>(to_sc(s), to_cl(c), b, dxinv, uc.data(), rc.data(), 1);
-  counts[0] = g_cnt.add; counts[1] = g_cnt.mul; counts[2] = g_cnt.div;
-  counts[3] = g_cnt.sqrt; counts[4] = g_cnt.cmp;
+  g_phase = 0;
+  for (int p = 0; p < NPHASE; ++p) {
+    counts[5 * p + 0] = g_cntp[p].add; counts[5 * p + 1] = g_cntp[p].mul; counts[5 * p + 2] = g_cntp[p].div;
+    counts[5 * p + 3] = g_cntp[p].sqrt; counts[5 * p + 4] = g_cntp[p].cmp;
+  }
   return 0;
 }
 

@@ -111,18 +111,25 @@ class Oracle:
             raise RuntimeError("orc_compute_rhs_jvp failed: %d" % rc)
         return R, JW
 
-    def rhs_counts(self, scheme, closures, U, dxinv, lo=(0, 0, 0)):
-        """{add, mul, div, sqrt, cmp} operation counts of one RHS of this box."""
+    PHASES = ("prims", "euler_faces", "jst", "visc_cells", "visc_faces", "divergence")
+
+    def rhs_counts(self, scheme, closures, U, dxinv, lo=(0, 0, 0), per_phase=False):
+        """{add, mul, div, sqrt, cmp} operation counts of one RHS of this box
+        (summed, or per phase of compute_rhs when per_phase)."""
         U = np.ascontiguousarray(U, dtype=np.float64)
         nz, ny, nx = (s - 2 * NG for s in U.shape[1:])
         hi = (lo[0] + nx - 1, lo[1] + ny - 1, lo[2] + nz - 1)
-        cnt = (ctypes.c_longlong * 5)()
+        cnt = (ctypes.c_longlong * 30)()
         sc, cl = c_scheme(scheme), c_closures(closures)
         rc = self.lib.orc_compute_rhs_count(ctypes.byref(sc), ctypes.byref(cl), _i3(lo), _i3(hi),
                                             _d3(dxinv), _ptr(U), cnt)
         if rc:
             raise RuntimeError("orc_compute_rhs_count failed: %d" % rc)
-        return dict(zip(("add", "mul", "div", "sqrt", "cmp"), list(cnt)))
+        keys = ("add", "mul", "div", "sqrt", "cmp")
+        per = {ph: dict(zip(keys, list(cnt)[5 * p:5 * p + 5])) for p, ph in enumerate(self.PHASES)}
+        if per_phase:
+            return per
+        return {k: sum(per[ph][k] for ph in self.PHASES) for k in keys}
 
     def fill_halo(self, U, bc_lo, bc_hi, lo=(0, 0, 0)):
         """In-place ghost fill of a single-box domain."""

@@ -86,6 +86,9 @@ SIGNATURES = {
                               _P]),
     "amrs_sync_check": (_S, [_P, _P]),
     "amrs_probe_fp64_tflops": (_S, [_P, ctypes.POINTER(ctypes.c_double)]),
+    "amrs_profile_stage_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(StageProg), Array4, Array4, Array4, ctypes.c_int32, _P,
+                                    ctypes.POINTER(ctypes.c_double)]),
     "amrs_debug_tma_enabled": (ctypes.c_int32, [_P]),
     "amrs_boxlist_tma_enabled": (ctypes.c_int32, [_P]),
 }
@@ -219,6 +222,18 @@ class Handle:
 
     def tma_enabled(self):
         return int(self._L.amrs_debug_tma_enabled(self.h))
+
+    def profile_stage_box(self, prog, Uin, U1, Uout, dxinv, lo=(0, 0, 0), reps=5, stream=None):
+        """Per-kernel ms of one fused stage: (prims, viscous cells, face kernel, total)."""
+        nz, ny, nx = (s - 2 * NGHOST for s in Uin.shape[1:])
+        g1 = (U1.shape[1] - nz) // 2
+        go = (Uout.shape[1] - nz) // 2
+        bx = c_box(lo, (nx, ny, nz))
+        ms = (ctypes.c_double * 4)()
+        check(self._L.amrs_profile_stage_box(self.h, ctypes.byref(bx), d3(dxinv), ctypes.byref(prog),
+                                             array4(Uin, lo, NGHOST), array4(U1, lo, g1), array4(Uout, lo, go),
+                                             int(reps), _stream_ptr(stream), ms), "amrs_profile_stage_box")
+        return tuple(ms)
 
     def probe_fp64_tflops(self):
         v = ctypes.c_double()

@@ -838,6 +838,54 @@ amrs_status amrs_probe_fp64_tflops(amrs_handle* h, double* tflops) {
   return AMRS_OK;
 }
 
+// Per-kernel timing of one RK stage of one box (KEEP fused path): the
+// primitive, viscous-cell and fused face kernels each bracketed by CUDA
+// events on `stream`, averaged over `reps` stages.  ms[0..3] = prims, viscous
+// cells, face kernel, whole stage.  Host-synchronising.
+amrs_status amrs_profile_stage_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3],
+                                   const amrs_stage_prog* prog, amrs_array4 stage_in, amrs_array4 s1, amrs_array4 out,
+                                   int32_t reps, void* stream, double* ms) {
+  if (!h || !bx || !dxinv || !prog || !ms) return AMRS_ERR_NULL;
+  if (reps < 1) return AMRS_ERR_SIZE;
+  if (!covers(stage_in, *bx, NGHOST, NCONS) || !covers(s1, *bx, 0, NCONS) || !covers(out, *bx, 0, NCONS))
+    return AMRS_ERR_LAYOUT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  CK(cudaSetDevice(h->device));
+  amrs_array4 slots[3] = {stage_in, s1, out};
+  if (amrs_status s = one_box(h, bx, dxinv, slots, 3)) return s;
+  List& L = *h->one;
+  if (!L.fused) return AMRS_ERR_SCHEME;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const DProg p = to_dprog(prog);
+  cudaEvent_t ev[4];
+  for (int i = 0; i < 4; ++i) CK(cudaEventCreate(&ev[i]));
+  double acc[3] = {0, 0, 0};
+  amrs_status rs = AMRS_OK;
+  for (int r = 0; r < reps && rs == AMRS_OK; ++r) {
+    cudaError_t e = cudaEventRecord(ev[0], st);
+    if (e == cudaSuccess) e = launch_prims(L.tb, 0, L.tot_p, h->nsm, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
+    if (e == cudaSuccess && L.sc.rhs_visc) e = launch_visc(L.tb, L.tot_v, h->nsm, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[2], st);
+    if (e == cudaSuccess)
+      e = launch_keep_face(L.sc.order_keep, L.sc.rhs_visc != 0, L.tb, 0, 1, 2, p, 0, L.tma, h->derr, L.tot_work,
+                           h->nsm, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[3], st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[3]);
+    for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
+      float t = 0.f;
+      e = cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
+      acc[i] += t;
+    }
+    if (e != cudaSuccess) rs = cuda_fail(e, "amrs_profile_stage_box");
+  }
+  for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
+  if (rs) return rs;
+  for (int i = 0; i < 3; ++i) ms[i] = acc[i] / reps;
+  ms[3] = ms[0] + ms[1] + ms[2];
+  return AMRS_OK;
+}
+
 // Whether the fused face kernel of this handle's last single-box list stages
 // its planes with TMA (1) or with plain loads (0).
 int32_t amrs_debug_tma_enabled(amrs_handle* h) { return (h && h->one) ? h->one->tma.enabled : -1; }

@@ -235,7 +235,7 @@ def run_gpu(args, rank, world, local):
     from amrsolver_gb300 import problems as P
     torch.cuda.set_device(local)
     capi.load(build_if_missing=True)
-    n = 128
+    n = args.n
     U, dx = P.tgv(n)
     cl = P.Closures.nondimensional(1.0 / 1600.0)
     sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1)
@@ -298,13 +298,17 @@ def run_gpu(args, rank, world, local):
         out = torch.empty_like(S0)
         s1 = lev.bufs[(lev.cur + 1) % 3]
         lev.fill_patch(S0)
-        # isolate the face kernel: prims + viscous once, then the face kernel K times
-        tf = time_face_kernel(torch, lev, progs[1], S0, s1, out, args.steps)
+        # the face kernel alone, CUDA events on the launching stream
+        lev.h.profile_stage_box(progs[1], S0, s1, out, lev.dxinv, lev.lo, reps=2, stream=stream)
+        kms = lev.h.profile_stage_box(progs[1], S0, s1, out, lev.dxinv, lev.lo, reps=max(args.steps, 5),
+                                      stream=stream)
+        tf = kms[2]
         achieved = face_flops / (tf * 1e-3) / 1e12
         roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                     "traffic": None, "kernel": "keep_face_kernel<4,true>",
                     "peak_source": "measured: DFMA-chain probe kernel (amrs_probe_fp64_tflops), FMA = 2 flops",
                     "algorithmic_flops_per_launch": face_flops, "ms_per_launch": tf,
+                    "stage_kernel_ms": {"prims": kms[0], "visc_cells": kms[1], "faces": kms[2]},
                     "hbm_peak_gbs_measured": None}
         try:
             mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -313,8 +317,10 @@ def run_gpu(args, rank, world, local):
             pass
         algo_bytes_face = n ** 3 * (3 * 40)  # reads U_s, U^n, writes U_{s+1}: 120 B/cell
         roofline["hbm_achieved_gbs_algorithmic"] = algo_bytes_face / (tf * 1e-3) / 1e9
-        prof = os.path.join(ROOT, "profiles", "keep_face_kernel_tgv128.md")
-        roofline["traffic"] = read_traffic(prof)
+        prof = os.path.join(ROOT, "profiles", "keep_face_kernel_tgv96.md")
+        t96 = read_traffic(prof)
+        # traffic grows with the cells processed: scale the 96^3 capture to this box
+        roofline["traffic"] = None if t96 is None else t96 * (n ** 3) / 96 ** 3
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_all, "higher_is_better": True, "scaling": "weak",
@@ -335,43 +341,6 @@ def run_gpu(args, rank, world, local):
     return result
 
 
-def time_face_kernel(torch, lev, prog, S0, s1, out, k):
-    """Average duration of the fused face kernel alone (CUDA events)."""
-    from amrsolver_gb300 import capi
-    # one stage call runs prims + viscous + face; time the whole stage and the
-    # prims + viscous part (rhs-only face replaced by a stage without Euler)
-    st = torch.cuda.current_stream()
-    for _ in range(3):
-        lev.h.rk_stage_box(prog, S0, s1, out, lev.dxinv, lev.lo)
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(st)
-    for _ in range(k):
-        lev.h.rk_stage_box(prog, S0, s1, out, lev.dxinv, lev.lo)
-    e1.record(st)
-    torch.cuda.synchronize()
-    stage_ms = e0.elapsed_time(e1) / k
-    # prims + viscous cell fluxes alone: a viscous-only handle runs the same
-    # two producer kernels followed by the face-array path; subtract the
-    # producers measured through the library's probe of the face share
-    share = face_share_from_profile()
-    return stage_ms * share
-
-
-def face_share_from_profile():
-    """Share of the stage time spent in the face kernel, from the committed
-    ncu launch-list summary (1.0 if absent)."""
-    p = os.path.join(ROOT, "profiles", "launches_tgv128.md")
-    try:
-        for line in open(p):
-            if line.startswith("face_share:"):
-                return float(line.split(":")[1])
-    except Exception:
-        pass
-    return 1.0
-
-
 def read_traffic(path):
     try:
         for line in open(path):
@@ -390,6 +359,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--n", type=int, default=128, help="TGV box edge (128 for the headline; smaller for profiling)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1:

@@ -201,6 +201,13 @@ amrs_status amrs_sync_check(amrs_handle* h, void* stream);
  * by a DFMA-chain kernel: the roofline denominator of this FP64-bound path.
  * Host-synchronising. */
 amrs_status amrs_probe_fp64_tflops(amrs_handle* h, double* tflops);
+/* Per-kernel timing of one RK stage of one box on the fused KEEP path:
+ * CUDA events around the primitive, viscous-cell and face kernels on
+ * `stream`, averaged over `reps`; ms[0..3] = prims, viscous cells, face
+ * kernel, whole stage.  Host-synchronising. */
+amrs_status amrs_profile_stage_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3],
+                                   const amrs_stage_prog* prog, amrs_array4 stage_in, amrs_array4 s1,
+                                   amrs_array4 out, int32_t reps, void* stream, double* ms);
 /* 1 if the fused face kernel stages planes with TMA for the handle's last
  * per-box call (resp. for the box list), 0 if with plain loads, -1 if none. */
 int32_t amrs_debug_tma_enabled(amrs_handle* h);

@@ -617,6 +617,14 @@ inline void jst_flux(int i, int j, int k, int n, const Arr<R>& lam, const Arr<R>
 
 inline void set_phase(int p) { g_phase = p; }
 
+// Grow-only per-thread scratch fields, reused across calls the way the
+// reference allocates its level scratch MultiFabs once (src/CNS.cpp:432-467).
+template <class R> R* pool(int slot, size_t n) {
+  static thread_local std::vector<R> p[16];
+  if (p[slot].size() < n) p[slot].resize(n);
+  return p[slot].data();
+}
+
 // ------------------------------------------------------------ compute_rhs --
 // CNS::compute_rhs for one box: src/tim/CNS_advance.cpp:186-391.
 // u: ghosted (NGHOST) conserved state; dsdt: valid-only output.
@@ -627,9 +635,8 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
                      const R* uptr, R* dsdt, int nthreads) {
   const int g = NGHOST;
   const long long ncg = (long long)(bx.n(0) + 2 * g) * (bx.n(1) + 2 * g) * (bx.n(2) + 2 * g);
-  std::vector<R> qbuf(ncg * NPRIM);
   Arr<R> u = make_arr<R>(const_cast<R*>(uptr), bx, g);
-  Arr<R> q = make_arr<R>(qbuf.data(), bx, g);
+  Arr<R> q = make_arr<R>(pool<R>(0, ncg * NPRIM), bx, g);
   const int lo0 = bx.lo[0], lo1 = bx.lo[1], lo2 = bx.lo[2];
   const int hi0 = bx.hi[0], hi1 = bx.hi[1], hi2 = bx.hi[2];
   (void)nthreads;
@@ -647,12 +654,17 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
       for (int i = lo0 - g; i <= hi0 + g; ++i) cons2prim(i, j, k, u, q, cl);
 
   // face fluxes, one array per direction, nodal in that direction
-  std::vector<R> fbuf[3];
   Arr<R> F[3];
   for (int d = 0; d < 3; ++d) {
     const long long nf = (long long)(bx.n(0) + (d == 0)) * (bx.n(1) + (d == 1)) * (bx.n(2) + (d == 2));
-    fbuf[d].assign(nf * NCONS, R(0.0));
-    F[d] = make_face_arr<R>(fbuf[d].data(), bx, d);
+    R* fp = pool<R>(1 + d, nf * NCONS);
+    F[d] = make_face_arr<R>(fp, bx, d);
+    if (!sc.rhs_euler) {  // every face is written by the Euler fluxes otherwise
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nt) schedule(static)
+#endif
+      for (long long t = 0; t < nf * NCONS; ++t) fp[t] = R(0.0);
+    }
   }
 
   // 2. Euler fluxes (:221-224)
@@ -675,14 +687,9 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
             }
       }
     } else if (sc.flux_euler == 2) {
-      std::vector<R> pbuf[3];
       Arr<R> PF[3];
-      for (int d = 0; d < 3; ++d) {
-        pbuf[d].assign(ncg * NCONS, R(0.0));
-        PF[d] = make_arr<R>(pbuf[d].data(), bx, g);
-      }
-      std::vector<R> lbuf(ncg * 3);
-      Arr<R> lam = make_arr<R>(lbuf.data(), bx, g);
+      for (int d = 0; d < 3; ++d) PF[d] = make_arr<R>(pool<R>(4 + d, ncg * NCONS), bx, g);
+      Arr<R> lam = make_arr<R>(pool<R>(7, ncg * 3), bx, g);
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(nt) schedule(static)
 #endif
@@ -702,8 +709,7 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
       // MUSCL + Riemann (src/rhs/Riemann.h:339-408); slope temp on grow(bx,1)
       Box b1 = bx;
       for (int d = 0; d < 3; ++d) { b1.lo[d] -= 1; b1.hi[d] += 1; }
-      std::vector<R> sbuf(b1.cells() * NCONS, R(0.0));
-      Arr<R> dq = make_arr<R>(sbuf.data(), b1, 0);
+      Arr<R> dq = make_arr<R>(pool<R>(8, b1.cells() * NCONS), b1, 0);
       for (int d = 0; d < 3; ++d) {
         const int di = (d == 0), dj = (d == 1), dk = (d == 2);
 #ifdef _OPENMP
@@ -725,8 +731,10 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
     // zero elsewhere, then subtracted on every face.
     if (sc.art_diss == 1) {
       set_phase(2);
-      std::vector<R> lb(ncg * 3, R(0.0)), sb(ncg * 3, R(0.0));
-      Arr<R> lam = make_arr<R>(lb.data(), bx, g), sen = make_arr<R>(sb.data(), bx, g);
+      R* lb = pool<R>(9, ncg * 3);
+      R* sb = pool<R>(10, ncg * 3);
+      for (long long t = 0; t < ncg * 3; ++t) { lb[t] = R(0.0); sb[t] = R(0.0); }
+      Arr<R> lam = make_arr<R>(lb, bx, g), sen = make_arr<R>(sb, bx, g);
       for (int k = lo2; k <= hi2; ++k)
         for (int j = lo1; j <= hi1; ++j)
           for (int i = lo0; i <= hi0; ++i) sensor_lambda(i, j, k, q, lam, sen, cl);
@@ -752,12 +760,8 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
     set_phase(3);
     Box b1 = bx;
     for (int d = 0; d < 3; ++d) { b1.lo[d] -= 1; b1.hi[d] += 1; }
-    std::vector<R> vb[3];
     Arr<R> VF[3];
-    for (int d = 0; d < 3; ++d) {
-      vb[d].assign(b1.cells() * NCONS, R(0.0));
-      VF[d] = make_arr<R>(vb[d].data(), b1, 0);
-    }
+    for (int d = 0; d < 3; ++d) VF[d] = make_arr<R>(pool<R>(11 + d, b1.cells() * NCONS), b1, 0);
 #ifdef _OPENMP
 #pragma omp parallel for num_threads(nt) schedule(static)
 #endif
@@ -830,6 +834,9 @@ void fill_halo_box(const Box& dom, const int bc_lo[3], const int bc_hi[3], R* up
   for (int d = 0; d < 3; ++d) {
     if (!(bc_lo[d] == -1 && bc_hi[d] == -1)) continue;
     const int n = dom.n(d);
+#ifdef _OPENMP
+    #pragma omp parallel for schedule(static) if (u.ns > 100000)
+#endif
     for (int k = glo[2]; k <= ghi[2]; ++k)
       for (int j = glo[1]; j <= ghi[1]; ++j)
         for (int i = glo[0]; i <= ghi[0]; ++i) {
@@ -844,6 +851,9 @@ void fill_halo_box(const Box& dom, const int bc_lo[3], const int bc_hi[3], R* up
     for (int side = 0; side < 2; ++side) {
       const int phys = side ? bc_hi[d] : bc_lo[d];
       if (phys == -1 || phys == 0) continue;
+#ifdef _OPENMP
+      #pragma omp parallel for schedule(static) if (u.ns > 100000)
+#endif
       for (int k = glo[2]; k <= ghi[2]; ++k)
         for (int j = glo[1]; j <= ghi[1]; ++j)
           for (int i = glo[0]; i <= ghi[0]; ++i) {
@@ -1076,7 +1086,9 @@ int orc_advance(const OrcScheme* s, const OrcClosures* c, const int* lo, const i
   if (ns < 0) return 5;
   Box b = to_box(lo, hi);
   const long long ng = ghosted(b), nv = b.cells();
-  std::vector<double> sborder(ng * NCONS), ds(nv * NCONS);
+  double* sborder_p = pool<double>(14, ng * NCONS);
+  double* ds_p = pool<double>(15, nv * NCONS);
+  struct { double* p; double* data() const { return p; } } sborder{sborder_p}, ds{ds_p};
   Arr<double> a1 = make_arr<double>(S1, b, NGHOST), a2 = make_arr<double>(S2, b, NGHOST);
   Arr<double> ab = make_arr<double>(sborder.data(), b, NGHOST), ad = make_arr<double>(ds.data(), b, 0);
   const Scheme sc = to_sc(s);
@@ -1090,6 +1102,9 @@ int orc_advance(const OrcScheme* s, const OrcClosures* c, const int* lo, const i
   for (int is = 0; is < ns; ++is) {
     // FillPatch: copy the source state's valid cells, then fill ghosts
     Arr<double>& src = st[is].src ? a2 : a1;
+#ifdef _OPENMP
+#pragma omp parallel for collapse(2) num_threads(nthreads > 0 ? nthreads : 1) schedule(static)
+#endif
     for (int n = 0; n < NCONS; ++n)
       for (int k = b.lo[2]; k <= b.hi[2]; ++k)
         for (int j = b.lo[1]; j <= b.hi[1]; ++j)
@@ -1097,6 +1112,9 @@ int orc_advance(const OrcScheme* s, const OrcClosures* c, const int* lo, const i
     int rc = orc_fill_halo(lo, hi, bc_lo, bc_hi, sborder.data(), NCONS);
     if (rc) return rc;
     compute_rhs_box<double>(sc, cl, b, dxinv, sborder.data(), ds.data(), nthreads);
+#ifdef _OPENMP
+#pragma omp parallel for collapse(2) num_threads(nthreads > 0 ? nthreads : 1) schedule(static)
+#endif
     for (int n = 0; n < NCONS; ++n)
       for (int k = b.lo[2]; k <= b.hi[2]; ++k)
         for (int j = b.lo[1]; j <= b.hi[1]; ++j)

@@ -77,13 +77,20 @@ SIGNATURES = {
     "amrs_boxlist_destroy": (_S, [_P]),
     "amrs_boxlist_set_tile": (_S, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                    ctypes.c_int32, ctypes.c_int32]),
+    "amrs_boxlist_set_bc": (_S, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
+    "amrs_boxlist_fill_halo": (_S, [_P, ctypes.c_int32, _P]),
     "amrs_rk_stage_boxlist": (_S, [_P, ctypes.POINTER(StageProg), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                    _P]),
     "amrs_rk_step_boxlist": (_S, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_int32,
                                   ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P,
                                   ctypes.POINTER(ctypes.c_int32)]),
     "amrs_rhs_vjp_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double), Array4, Array4, Array4,
-                              _P]),
+                              _P, _P]),
+    "amrs_fill_halo_box_adjoint": (_S, [ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_int32),
+                                        ctypes.POINTER(ctypes.c_int32), Array4, _P]),
+    "amrs_rk_stage_vjp_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double),
+                                   ctypes.POINTER(StageProg), ctypes.POINTER(ctypes.c_int32),
+                                   ctypes.POINTER(ctypes.c_int32), Array4, Array4, Array4, Array4, _P, _P]),
     "amrs_sync_check": (_S, [_P, _P]),
     "amrs_probe_fp64_tflops": (_S, [_P, ctypes.POINTER(ctypes.c_double)]),
     "amrs_profile_stage_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double),
@@ -223,6 +230,27 @@ class Handle:
     def tma_enabled(self):
         return int(self._L.amrs_debug_tma_enabled(self.h))
 
+    def rhs_vjp_box(self, U, vbar, ubar, dxinv, lo=(0, 0, 0), param_bar=None, stream=None):
+        """ubar (ghosted) = (d dSdt/dU)^T vbar; param_bar (cuda, 2 doubles) += d/d(visc_ref, cond_ref)."""
+        nz, ny, nx = (s - 2 * NGHOST for s in U.shape[1:])
+        bx = c_box(lo, (nx, ny, nz))
+        pb = ctypes.c_void_p(param_bar.data_ptr()) if param_bar is not None else None
+        check(self._L.amrs_rhs_vjp_box(self.h, ctypes.byref(bx), d3(dxinv), array4(U, lo, NGHOST),
+                                       array4(vbar, lo, 0), array4(ubar, lo, NGHOST), pb, _stream_ptr(stream)),
+              "amrs_rhs_vjp_box")
+
+    def rk_stage_vjp_box(self, prog, bc_lo, bc_hi, Uin, wbar, s1bar, inbar, dxinv, lo=(0, 0, 0), param_bar=None,
+                         stream=None):
+        """Adds the S1 and stage-input cotangents of one RK stage (valid cells)."""
+        nz, ny, nx = (s - 2 * NGHOST for s in Uin.shape[1:])
+        bx = c_box(lo, (nx, ny, nz))
+        g = lambda t: (t.shape[1] - nz) // 2
+        pb = ctypes.c_void_p(param_bar.data_ptr()) if param_bar is not None else None
+        check(self._L.amrs_rk_stage_vjp_box(self.h, ctypes.byref(bx), d3(dxinv), ctypes.byref(prog), i3(bc_lo),
+                                            i3(bc_hi), array4(Uin, lo, NGHOST), array4(wbar, lo, g(wbar)),
+                                            array4(s1bar, lo, g(s1bar)), array4(inbar, lo, g(inbar)), pb,
+                                            _stream_ptr(stream)), "amrs_rk_stage_vjp_box")
+
     def profile_stage_box(self, prog, Uin, U1, Uout, dxinv, lo=(0, 0, 0), reps=5, stream=None):
         """Per-kernel ms of one fused stage: (prims, viscous cells, face kernel, total)."""
         nz, ny, nx = (s - 2 * NGHOST for s in Uin.shape[1:])
@@ -297,6 +325,15 @@ class BoxList:
 
     def set_tile(self, n, tx, ty, kc):
         check(self._L.amrs_boxlist_set_tile(self.bl, n[0], n[1], n[2], tx, ty, kc), "amrs_boxlist_set_tile")
+
+    def set_bc(self, bc_lo, bc_hi):
+        if bc_lo is None:
+            check(self._L.amrs_boxlist_set_bc(self.bl, None, None), "amrs_boxlist_set_bc")
+        else:
+            check(self._L.amrs_boxlist_set_bc(self.bl, i3(bc_lo), i3(bc_hi)), "amrs_boxlist_set_bc")
+
+    def fill_halo(self, slot, stream=None):
+        check(self._L.amrs_boxlist_fill_halo(self.bl, slot, _stream_ptr(stream)), "amrs_boxlist_fill_halo")
 
     def stage(self, prog, s_in, s1, s_out, stream=None):
         check(self._L.amrs_rk_stage_boxlist(self.bl, ctypes.byref(prog), s_in, s1, s_out, _stream_ptr(stream)),

@@ -25,7 +25,9 @@ struct BoxTable {
   const BoxRec* box;
   const long long* pcell;  // prefix of primitive-region cells, size n+1
   const long long* vcell;  // prefix of viscous-region cells, size n+1
-  const int* fwork;        // prefix of face-kernel work items, size n+1
+  const int* fwork;        // prefix of face-kernel work items, size n+1 (unused by the balanced schedule)
+  const int4* seg;         // face-kernel segments: (box, tile index, k0, k1)
+  const int* cta_seg;      // segments of CTA c: [cta_seg[c], cta_seg[c+1])
   const DClosures* cls;
   int n;
   int gq;                  // ghost depth of the primitive region

@@ -12,9 +12,10 @@ namespace amrs {
 cudaError_t launch_prims(const BoxTable& tb, int s_in, long long ncells, int nsm, cudaStream_t st);
 cudaError_t launch_visc(const BoxTable& tb, long long ncells, int nsm, cudaStream_t st);
 cudaError_t launch_keep_face(int order, bool visc, const BoxTable& tb, int s_in, int s_s1, int s_out,
-                             const DProg& prog, int rhs_only, const TmaDesc& tma, int* err, int nwork, int nsm,
+                             const DProg& prog, int rhs_only, const TmaDesc& tma, int* err, int grid, int nsm,
                              cudaStream_t st);
 bool keep_tile_fits(int order, int tx, int ty);
+int keep_ctas_per_sm(int order);
 template <int ORDER> int keep_smem_bytes();
 
 // ---- face-array (reference-structured) path (rhs_plain.cu)
@@ -55,6 +56,22 @@ struct HaloBox {
   int ncomp;
 };
 cudaError_t launch_halo(const HaloBox& hb, cudaStream_t st);
+
+// ---- adjoint (adjoint.cu), single box (tb.box[0], Q already computed)
+struct AdjRecHost {
+  DArr vbar, ubar;
+  DArr pair[3][3];  // [direction][separation-1], 12 comps over grow(box,3)
+  DArr vg;          // 16 comps over grow(box,1)
+  int n[3];
+  int visc;
+};
+cudaError_t launch_rhs_vjp(int order, const BoxTable& tb, const AdjRecHost& ah, double* pbar, int nsm,
+                           cudaStream_t st);
+cudaError_t launch_adj_prog(const BoxRec& R, const DProg& prog, const DArr& wbar, const DArr& s1bar, const DArr& inbar,
+                            const DArr& vbar, int accumulate, int nsm, cudaStream_t st);
+cudaError_t launch_adj_halo(const HaloBox& hb, int nsm, cudaStream_t st);
+cudaError_t launch_halo_list(const BoxTable& tb, const long long* gpre, long long total, int slot, const int bc_lo[3],
+                             const int bc_hi[3], int nsm, cudaStream_t st);
 cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t st);
 cudaError_t launch_estdt(const BoxTable& tb, int s_in, long long nvalid, double cfl, unsigned long long* bits,
                          double* dt_out, int nsm, cudaStream_t st);

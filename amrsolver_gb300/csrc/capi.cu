@@ -142,10 +142,13 @@ struct List {
   const long long* d_spre[3] = {nullptr, nullptr, nullptr};
   long long tot_p = 0, tot_v = 0, tot_g = 0, tot_valid = 0, tot_f[3] = {0, 0, 0}, tot_s[3] = {0, 0, 0};
   int tot_work = 0;
+  int face_grid = 0;  // CTAs of the balanced face-kernel schedule
   cudaGraphExec_t graph = nullptr;
   int graph_key[6] = {0, 0, 0, 0, 0, 0};
   double graph_dt = 0.0;
   int graph_result = -1;
+  int has_bc = 0;  // fill each stage input's ghosts, every box its own domain
+  int bc_lo[3] = {-1, -1, -1}, bc_hi[3] = {-1, -1, -1};
   ~List() {
     if (graph) cudaGraphExecDestroy(graph);
     if (dtab) cudaFree(dtab);
@@ -165,6 +168,13 @@ struct amrs_handle {
   bool tma_ok = true;
   void* encode_fn = nullptr;
   List* one = nullptr;               // reusable single-box list for per-box calls
+  void* adj = nullptr;               // adjoint scratch (pair and viscous cotangents), grow-only
+  size_t adj_bytes = 0;
+  BoxRec* dring = nullptr;           // per-call box records of per-box calls (device ring)
+  BoxRec* hring = nullptr;           // pinned staging of the ring
+  cudaEvent_t ring_ev[64];
+  int ring_used[64] = {0};
+  int ring_pos = 0, ring_cur = -1;
   std::mutex mu;
 };
 
@@ -308,6 +318,59 @@ amrs_status list_build(amrs_handle* h, List& L, int n, const amrs_box* boxes, co
   L.tot_work = L.fwork[n];
   for (int d = 0; d < 3; ++d) { L.tot_f[d] = L.fpre[d][n]; L.tot_s[d] = L.spre[d][n]; }
 
+  // Balanced static schedule of the fused face kernel: the (tile column x
+  // plane) work of all boxes, weighted by the column's cells, is cut into
+  // G equal shares (G = resident CTAs); a share is a run of segments
+  // (box, column, k0, k1), each segment costing one z-prologue.
+  std::vector<int4> segs;
+  std::vector<int> cta_seg;
+  L.face_grid = 0;
+  if (L.fused) {
+    double total = 0.0;
+    long long colplanes = 0;
+    for (int b = 0; b < n; ++b) {
+      const BoxRec& R = L.hbox[b];
+      for (int c = 0; c < R.ntx * R.nty; ++c) {
+        const int txi = c % R.ntx, tyi = c / R.ntx;
+        const int txw = std::min(R.tx, R.hi[0] + 1 - (R.lo[0] + txi * R.tx));
+        const int tyw = std::min(R.ty, R.hi[1] + 1 - (R.lo[1] + tyi * R.ty));
+        total += (double)txw * tyw * bn(boxes[b], 2);
+        colplanes += bn(boxes[b], 2);
+      }
+    }
+    const long long G = std::min<long long>((long long)keep_ctas_per_sm(order) * h->nsm, colplanes);
+    const double per = total / (double)G;
+    int cta = 0;
+    double acc = 0.0;
+    cta_seg.push_back(0);
+    for (int b = 0; b < n; ++b) {
+      const BoxRec& R = L.hbox[b];
+      for (int c = 0; c < R.ntx * R.nty; ++c) {
+        const int txi = c % R.ntx, tyi = c / R.ntx;
+        const int txw = std::min(R.tx, R.hi[0] + 1 - (R.lo[0] + txi * R.tx));
+        const int tyw = std::min(R.ty, R.hi[1] + 1 - (R.lo[1] + tyi * R.ty));
+        const double w = (double)txw * tyw;
+        int k = R.lo[2];
+        while (k <= R.hi[2]) {
+          const double boundary = (cta + 1) * per;
+          long long fit = (long long)((boundary - acc) / w + 0.5);
+          if (fit < 1) fit = 1;
+          const int kend = (int)std::min<long long>(R.hi[2] + 1, k + fit);
+          segs.push_back(make_int4(b, c, k, kend));
+          acc += (kend - k) * w;
+          k = kend;
+          if (acc >= boundary - 0.5 * w && cta < G - 1) {
+            ++cta;
+            cta_seg.push_back((int)segs.size());
+          }
+        }
+      }
+    }
+    while ((long long)cta_seg.size() < G + 1) cta_seg.push_back((int)segs.size());
+    cta_seg[G] = (int)segs.size();
+    L.face_grid = (int)G;
+  }
+
   // tensor maps (fused path only)
   std::vector<CUtensorMap> maps;
   bool tma_all = L.fused && h->tma_ok && h->encode_fn;
@@ -330,6 +393,8 @@ amrs_status list_build(amrs_handle* h, List& L, int n, const amrs_box* boxes, co
   for (int d = 0; d < 3; ++d) { o_f[d] = t; t = align_up(t + 8 * (n + 1), 128); }
   for (int d = 0; d < 3; ++d) { o_s[d] = t; t = align_up(t + 8 * (n + 1), 128); }
   const size_t o_w = t; t = align_up(t + 4 * (n + 1), 128);
+  const size_t o_seg = t; t = align_up(t + sizeof(int4) * segs.size(), 128);
+  const size_t o_cs = t; t = align_up(t + 4 * cta_seg.size(), 128);
   if (t > L.dtab_bytes) {
     if (L.dtab) { cudaFree(L.dtab); L.dtab = nullptr; L.dtab_bytes = 0; }
     CK(cudaMalloc(&L.dtab, t));
@@ -349,12 +414,16 @@ amrs_status list_build(amrs_handle* h, List& L, int n, const amrs_box* boxes, co
     std::memcpy(&host[o_s[d]], L.spre[d].data(), 8 * (n + 1));
   }
   std::memcpy(&host[o_w], L.fwork.data(), 4 * (n + 1));
+  if (!segs.empty()) std::memcpy(&host[o_seg], segs.data(), sizeof(int4) * segs.size());
+  if (!cta_seg.empty()) std::memcpy(&host[o_cs], cta_seg.data(), 4 * cta_seg.size());
   CK(cudaMemcpy(L.dtab, host.data(), t, cudaMemcpyHostToDevice));
   char* D = static_cast<char*>(L.dtab);
   L.tb.box = reinterpret_cast<const BoxRec*>(D + o_box);
   L.tb.pcell = reinterpret_cast<const long long*>(D + o_p);
   L.tb.vcell = reinterpret_cast<const long long*>(D + o_v);
   L.tb.fwork = reinterpret_cast<const int*>(D + o_w);
+  L.tb.seg = reinterpret_cast<const int4*>(D + o_seg);
+  L.tb.cta_seg = reinterpret_cast<const int*>(D + o_cs);
   L.tb.cls = reinterpret_cast<const DClosures*>(D + o_cls);
   L.tb.n = n;
   L.tb.gq = L.gq;
@@ -395,7 +464,7 @@ amrs_status list_stage(amrs_handle* h, List& L, const DProg& prog, int s_in, int
   if (L.fused) {
     // 3. fused KEEP faces + viscous averages + divergence + stage program
     CK(launch_keep_face(sc.order_keep, sc.rhs_visc != 0, L.tb, s_in, s_s1, s_out, prog, rhs_only, L.tma, h->derr,
-                        L.tot_work, nsm, st));
+                        L.face_grid, nsm, st));
     return AMRS_OK;
   }
   long long nf[3] = {L.tot_f[0], L.tot_f[1], L.tot_f[2]};
@@ -434,24 +503,56 @@ bool same_box(const amrs_box& a, const amrs_box& b) {
 
 // Per-box calls reuse one single-box list; its tables are rebuilt only when
 // the box or the arrays change.
-amrs_status one_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3], const amrs_array4* slots, int nslots) {
+// Per-box calls: the geometry tables (prefixes, schedule, scratch, tensor
+// maps) of the single-box list are rebuilt only when the box or its cell
+// size changes; the per-call box record (state pointers) goes through a ring
+// of device records filled from pinned staging by an async copy on the
+// call's stream.  A ring entry is reused only after the event recorded
+// behind the kernels of its previous call has completed.
+constexpr int RING = 64;
+
+amrs_status one_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3], const amrs_array4* slots, int nslots,
+                    cudaStream_t st, const double* dx_override = nullptr) {
   List*& L = h->one;
   bool same = L && L->n == 1 && same_box(L->boxes[0], *bx) && L->nslots == nslots;
   if (same) {
     const BoxRec& R = L->hbox[0];
     for (int d = 0; d < 3 && same; ++d) same = R.dxinv[d] == dxinv[d];
-    for (int s = 0; s < nslots && same; ++s) {
-      DArr a = to_darr(slots[s]);
-      same = std::memcmp(&a, &R.slot[s], sizeof(DArr)) == 0;
+  }
+  if (!same) {
+    if (!L) L = new (std::nothrow) List();
+    if (!L) return AMRS_ERR_ALLOC;
+    if (L->graph) { cudaGraphExecDestroy(L->graph); L->graph = nullptr; }
+    // the previous tables may still be read by queued kernels
+    CK(cudaDeviceSynchronize());
+    if (amrs_status s = list_build(h, *L, 1, bx, dxinv, nslots, slots, nullptr, 0, nullptr, nullptr)) return s;
+  }
+  if (!h->dring) {
+    CK(cudaMalloc(&h->dring, sizeof(BoxRec) * RING));
+    CK(cudaMallocHost(&h->hring, sizeof(BoxRec) * RING));
+    for (int i = 0; i < RING; ++i) {
+      CK(cudaEventCreateWithFlags(&h->ring_ev[i], cudaEventDisableTiming));
+      h->ring_used[i] = 0;
     }
   }
-  if (same) return AMRS_OK;
-  if (!L) L = new (std::nothrow) List();
-  if (!L) return AMRS_ERR_ALLOC;
-  if (L->graph) { cudaGraphExecDestroy(L->graph); L->graph = nullptr; }
-  // the previous tables may still be read by queued kernels
-  CK(cudaDeviceSynchronize());
-  return list_build(h, *L, 1, bx, dxinv, nslots, slots, nullptr, 0, nullptr, nullptr);
+  const int i = h->ring_pos;
+  h->ring_pos = (i + 1) % RING;
+  if (h->ring_used[i]) CK(cudaEventSynchronize(h->ring_ev[i]));
+  BoxRec R = L->hbox[0];
+  for (int s = 0; s < nslots; ++s) R.slot[s] = to_darr(slots[s]);
+  if (dx_override)
+    for (int d = 0; d < 3; ++d) R.dx[d] = dx_override[d];
+  h->hring[i] = R;
+  CK(cudaMemcpyAsync(&h->dring[i], &h->hring[i], sizeof(BoxRec), cudaMemcpyHostToDevice, st));
+  L->tb.box = &h->dring[i];
+  h->ring_cur = i;
+  return AMRS_OK;
+}
+
+// Mark the current ring entry as in use by the work queued on `st`.
+void ring_release(amrs_handle* h, cudaStream_t st) {
+  const int i = h->ring_cur;
+  if (i >= 0 && cudaEventRecord(h->ring_ev[i], st) == cudaSuccess) h->ring_used[i] = 1;
 }
 
 }  // namespace
@@ -517,6 +618,12 @@ amrs_status amrs_destroy(amrs_handle* h) {
   if (!h) return AMRS_ERR_NULL;
   cudaSetDevice(h->device);
   delete h->one;
+  if (h->adj) cudaFree(h->adj);
+  if (h->dring) {
+    cudaFree(h->dring);
+    cudaFreeHost(h->hring);
+    for (int i = 0; i < 64; ++i) cudaEventDestroy(h->ring_ev[i]);
+  }
   if (h->derr) cudaFree(h->derr);
   if (h->dred) cudaFree(h->dred);
   delete h;
@@ -582,9 +689,12 @@ amrs_status amrs_rhs_box(amrs_handle* h, const amrs_box* bx, const double dxinv[
   std::lock_guard<std::mutex> lk(h->mu);
   CK(cudaSetDevice(h->device));
   amrs_array4 slots[3] = {state, state, dsdt};
-  if (amrs_status s = one_box(h, bx, dxinv, slots, 3)) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (amrs_status s = one_box(h, bx, dxinv, slots, 3, st)) return s;
   DProg p{};
-  return list_stage(h, *h->one, p, 0, 1, 2, 1, static_cast<cudaStream_t>(stream));
+  amrs_status rs = list_stage(h, *h->one, p, 0, 1, 2, 1, st);
+  ring_release(h, st);
+  return rs;
 }
 
 amrs_status amrs_rk_stage_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3], const amrs_stage_prog* prog,
@@ -599,8 +709,11 @@ amrs_status amrs_rk_stage_box(amrs_handle* h, const amrs_box* bx, const double d
   std::lock_guard<std::mutex> lk(h->mu);
   CK(cudaSetDevice(h->device));
   amrs_array4 slots[3] = {stage_in, s1, out};
-  if (amrs_status s = one_box(h, bx, dxinv, slots, 3)) return s;
-  return list_stage(h, *h->one, to_dprog(prog), 0, 1, 2, 0, static_cast<cudaStream_t>(stream));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (amrs_status s = one_box(h, bx, dxinv, slots, 3, st)) return s;
+  amrs_status rs = list_stage(h, *h->one, to_dprog(prog), 0, 1, 2, 0, st);
+  ring_release(h, st);
+  return rs;
 }
 
 amrs_status amrs_fill_halo_box(const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3],
@@ -633,16 +746,13 @@ amrs_status amrs_est_timestep_box(amrs_handle* h, const amrs_box* bx, const doub
   CK(cudaSetDevice(h->device));
   amrs_array4 slots[3] = {state, state, state};
   const double dxinv[3] = {1.0 / dx[0], 1.0 / dx[1], 1.0 / dx[2]};
-  if (amrs_status s = one_box(h, bx, dxinv, slots, 3)) return s;
-  // cns_estdt divides dx by the wave speed: pass dx exactly as given
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // cns_estdt divides dx by the wave speed: the record carries dx exactly as given
+  if (amrs_status s = one_box(h, bx, dxinv, slots, 3, st, dx)) return s;
   List& L = *h->one;
-  bool exact = true;
-  for (int d = 0; d < 3; ++d) exact = exact && L.hbox[0].dx[d] == dx[d];
-  if (!exact) {
-    for (int d = 0; d < 3; ++d) L.hbox[0].dx[d] = dx[d];
-    CK(cudaMemcpy(const_cast<BoxRec*>(L.tb.box), L.hbox.data(), sizeof(BoxRec), cudaMemcpyHostToDevice));
-  }
-  CK(launch_estdt(L.tb, 0, L.tot_valid, cfl, h->dred, dt_device, h->nsm, static_cast<cudaStream_t>(stream)));
+  cudaError_t e = launch_estdt(L.tb, 0, L.tot_valid, cfl, h->dred, dt_device, h->nsm, st);
+  ring_release(h, st);
+  if (e != cudaSuccess) return cuda_fail(e, "launch_estdt");
   return AMRS_OK;
 }
 
@@ -724,6 +834,40 @@ amrs_status amrs_boxlist_set_tile(amrs_boxlist* bl, int32_t nx, int32_t ny, int3
                     (int)cls.size(), cls.data(), tiles.data());
 }
 
+amrs_status amrs_boxlist_set_bc(amrs_boxlist* bl, const int32_t bc_lo[3], const int32_t bc_hi[3]) {
+  if (!bl) return AMRS_ERR_NULL;
+  List& L = bl->L;
+  if (!bc_lo || !bc_hi) {
+    L.has_bc = 0;
+  } else {
+    for (int d = 0; d < 3; ++d) {
+      if ((bc_lo[d] == -1) != (bc_hi[d] == -1)) return AMRS_ERR_BC;
+      for (int s = 0; s < 2; ++s) {
+        const int p = s ? bc_hi[d] : bc_lo[d];
+        if (p == 1 || p == 6 || p < -1 || p > 6) return AMRS_ERR_BC;
+      }
+      for (int b = 0; b < L.n; ++b)
+        if (bn(L.boxes[b], d) < NGHOST && bc_lo[d] != -1 && bc_lo[d] != 2) return AMRS_ERR_BOX;
+      L.bc_lo[d] = bc_lo[d];
+      L.bc_hi[d] = bc_hi[d];
+    }
+    L.has_bc = 1;
+  }
+  if (L.graph) { cudaGraphExecDestroy(L.graph); L.graph = nullptr; }
+  return AMRS_OK;
+}
+
+amrs_status amrs_boxlist_fill_halo(amrs_boxlist* bl, int32_t slot, void* stream) {
+  if (!bl) return AMRS_ERR_NULL;
+  List& L = bl->L;
+  if (!L.has_bc) return AMRS_ERR_STATE;
+  if (slot < 0 || slot >= L.nslots) return AMRS_ERR_SIZE;
+  CK(cudaSetDevice(bl->h->device));
+  CK(launch_halo_list(L.tb, L.ft.gpre, L.tot_g, slot, L.bc_lo, L.bc_hi, bl->h->nsm,
+                      static_cast<cudaStream_t>(stream)));
+  return AMRS_OK;
+}
+
 amrs_status amrs_rk_stage_boxlist(amrs_boxlist* bl, const amrs_stage_prog* prog, int32_t in, int32_t s1, int32_t out,
                                   void* stream) {
   if (!bl || !prog) return AMRS_ERR_NULL;
@@ -756,6 +900,7 @@ amrs_status amrs_rk_step_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t sta
       const int in = (progs[i].src_state == 0) ? s1 : cur;
       int out = outs[which];
       if (out == in) { which ^= 1; out = outs[which]; }
+      if (L.has_bc) CK(launch_halo_list(L.tb, L.ft.gpre, L.tot_g, in, L.bc_lo, L.bc_hi, bl->h->nsm, s));
       if (amrs_status e = list_stage(bl->h, L, to_dprog(&progs[i]), in, s1, out, 0, s)) return e;
       cur = out;
       which ^= 1;
@@ -790,10 +935,149 @@ amrs_status amrs_rk_step_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t sta
   return AMRS_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Adjoint scratch of one box: per (direction, separation) pair cotangents
+// (12 comps over grow(box,3)), viscous cotangents (16 comps over
+// grow(box,1)), a valid-cell dSdt cotangent and a ghosted state cotangent.
+struct AdjScratch {
+  AdjRecHost ah;
+  DArr vbar_tmp, ubar_tmp;
+};
+
+amrs_status adj_prepare(amrs_handle* h, const amrs_box& B, AdjScratch& S, cudaStream_t st) {
+  const int H = h->sc.order_keep / 2;
+  auto cells = [&](int g) { return (size_t)grown_cells(B, g); };
+  size_t off = 0;
+  const size_t o_pair = off; off = align_up(off + cells(3) * 12 * 8 * 3 * H, 256);
+  const size_t o_vg = off; off = align_up(off + cells(1) * 16 * 8, 256);
+  const size_t o_v = off; off = align_up(off + cells(0) * 5 * 8, 256);
+  const size_t o_u = off; off = align_up(off + cells(3) * 5 * 8, 256);
+  if (off > h->adj_bytes) {
+    if (h->adj) { CK(cudaStreamSynchronize(st)); cudaFree(h->adj); h->adj = nullptr; h->adj_bytes = 0; }
+    CK(cudaMalloc(&h->adj, off));
+    h->adj_bytes = off;
+  }
+  char* P = static_cast<char*>(h->adj);
+  auto mk = [&](size_t o, int g) {
+    DArr a;
+    a.p = reinterpret_cast<double*>(P + o);
+    const int nx = bn(B, 0) + 2 * g, ny = bn(B, 1) + 2 * g, nz = bn(B, 2) + 2 * g;
+    a.js = nx; a.ks = (long long)nx * ny; a.ns = (long long)nx * ny * nz;
+    a.b0 = B.lo[0] - g; a.b1 = B.lo[1] - g; a.b2 = B.lo[2] - g;
+    return a;
+  };
+  for (int d = 0; d < 3; ++d)
+    for (int l = 0; l < 3; ++l) S.ah.pair[d][l] = mk(o_pair + (l < H ? (size_t)(d * H + l) * cells(3) * 12 * 8 : 0), 3);
+  S.ah.vg = mk(o_vg, 1);
+  S.vbar_tmp = mk(o_v, 0);
+  S.ubar_tmp = mk(o_u, 3);
+  for (int d = 0; d < 3; ++d) S.ah.n[d] = bn(B, d);
+  S.ah.visc = h->sc.rhs_visc != 0;
+  CK(cudaMemsetAsync(P + o_pair, 0, cells(3) * 12 * 8 * 3 * H, st));
+  return AMRS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 amrs_status amrs_rhs_vjp_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3], amrs_array4 state,
-                             amrs_array4 vbar, amrs_array4 ubar, void* stream) {
-  (void)h; (void)bx; (void)dxinv; (void)state; (void)vbar; (void)ubar; (void)stream;
-  return AMRS_ERR_SCHEME;
+                             amrs_array4 vbar, amrs_array4 ubar, double* param_bar, void* stream) {
+  if (!h || !bx || !dxinv) return AMRS_ERR_NULL;
+  if (!box_ok(*bx)) return AMRS_ERR_BOX;
+  if (!fused_path(h->sc)) return AMRS_ERR_SCHEME;
+  if (!covers(state, *bx, NGHOST, NCONS) || !covers(vbar, *bx, 0, NCONS) || !covers(ubar, *bx, NGHOST, NCONS))
+    return AMRS_ERR_LAYOUT;
+  std::lock_guard<std::mutex> lk(h->mu);
+  CK(cudaSetDevice(h->device));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  amrs_array4 slots[3] = {state, state, state};
+  if (amrs_status s = one_box(h, bx, dxinv, slots, 3, st)) return s;
+  List& L = *h->one;
+  AdjScratch S;
+  if (amrs_status s = adj_prepare(h, *bx, S, st)) { ring_release(h, st); return s; }
+  S.ah.vbar = to_darr(vbar);
+  S.ah.ubar = to_darr(ubar);
+  cudaError_t e = launch_prims(L.tb, 0, L.tot_p, h->nsm, st);
+  if (e == cudaSuccess) e = launch_rhs_vjp(h->sc.order_keep, L.tb, S.ah, param_bar, h->nsm, st);
+  ring_release(h, st);
+  if (e != cudaSuccess) return cuda_fail(e, "amrs_rhs_vjp_box");
+  return AMRS_OK;
+}
+
+amrs_status amrs_fill_halo_box_adjoint(const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3],
+                                       amrs_array4 ubar, void* stream) {
+  if (!domain || !bc_lo || !bc_hi) return AMRS_ERR_NULL;
+  if (!box_ok(*domain)) return AMRS_ERR_BOX;
+  if (!covers(ubar, *domain, NGHOST, 1)) return AMRS_ERR_LAYOUT;
+  HaloBox hb;
+  hb.u = to_darr(ubar);
+  hb.ncomp = ubar.ncomp;
+  for (int d = 0; d < 3; ++d) {
+    if ((bc_lo[d] == -1) != (bc_hi[d] == -1)) return AMRS_ERR_BC;
+    for (int s = 0; s < 2; ++s) {
+      const int p = s ? bc_hi[d] : bc_lo[d];
+      if (p == 1 || p == 6 || p < -1 || p > 6) return AMRS_ERR_BC;
+    }
+    hb.lo[d] = domain->lo[d]; hb.hi[d] = domain->hi[d]; hb.bc_lo[d] = bc_lo[d]; hb.bc_hi[d] = bc_hi[d];
+  }
+  int nsm = 0;
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  CK(launch_adj_halo(hb, nsm, static_cast<cudaStream_t>(stream)));
+  return AMRS_OK;
+}
+
+amrs_status amrs_rk_stage_vjp_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3],
+                                  const amrs_stage_prog* prog, const int32_t bc_lo[3], const int32_t bc_hi[3],
+                                  amrs_array4 stage_in, amrs_array4 wbar, amrs_array4 s1bar, amrs_array4 inbar,
+                                  double* param_bar, void* stream) {
+  if (!h || !bx || !dxinv || !prog || !bc_lo || !bc_hi) return AMRS_ERR_NULL;
+  if (!box_ok(*bx)) return AMRS_ERR_BOX;
+  if (!fused_path(h->sc)) return AMRS_ERR_SCHEME;
+  if (!covers(stage_in, *bx, NGHOST, NCONS) || !covers(wbar, *bx, 0, NCONS) || !covers(s1bar, *bx, 0, NCONS) ||
+      !covers(inbar, *bx, 0, NCONS))
+    return AMRS_ERR_LAYOUT;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  AdjScratch S;
+  BoxRec R{};
+  {
+    std::lock_guard<std::mutex> lk(h->mu);
+    CK(cudaSetDevice(h->device));
+    amrs_array4 slots[3] = {stage_in, stage_in, stage_in};
+    if (amrs_status s = one_box(h, bx, dxinv, slots, 3, st)) return s;
+    if (amrs_status s = adj_prepare(h, *bx, S, st)) { ring_release(h, st); return s; }
+    R = h->one->hbox[0];
+    // 1. reverse of the BLAS-1 program: cotangents of S1, of the stage input
+    //    (register S2) and of dSdt
+    CK(launch_adj_prog(R, to_dprog(prog), to_darr(wbar), to_darr(s1bar), to_darr(inbar), S.vbar_tmp, 1, h->nsm, st));
+    // 2. RHS VJP of the ghost-filled stage input
+    S.ah.vbar = S.vbar_tmp;
+    S.ah.ubar = S.ubar_tmp;
+    List& L = *h->one;
+    cudaError_t e = launch_prims(L.tb, 0, L.tot_p, h->nsm, st);
+    if (e == cudaSuccess) e = launch_rhs_vjp(h->sc.order_keep, L.tb, S.ah, param_bar, h->nsm, st);
+    ring_release(h, st);
+    if (e != cudaSuccess) return cuda_fail(e, "amrs_rk_stage_vjp_box");
+  }
+  // 3. ghost fold (adjoint of FillPatch), then add into the stage input's cotangent
+  amrs_array4 ub{};
+  ub.p = S.ubar_tmp.p; ub.jstride = S.ubar_tmp.js; ub.kstride = S.ubar_tmp.ks; ub.nstride = S.ubar_tmp.ns;
+  ub.begin[0] = S.ubar_tmp.b0; ub.begin[1] = S.ubar_tmp.b1; ub.begin[2] = S.ubar_tmp.b2;
+  for (int d = 0; d < 3; ++d) ub.end[d] = bx->hi[d] + NGHOST + 1;
+  ub.ncomp = NCONS;
+  if (amrs_status s = amrs_fill_halo_box_adjoint(bx, bc_lo, bc_hi, ub, stream)) return s;
+  // inbar += valid(ubar): the reverse kernel with an empty program routes its
+  // input cotangent into the stage-input cotangent (vbar_tmp is free here)
+  amrs_stage_prog ident{};
+  ident.nops = 0;
+  DArr dummy = S.vbar_tmp;
+  CK(launch_adj_prog(R, to_dprog(&ident), S.ubar_tmp, dummy, to_darr(inbar), dummy, 1, h->nsm, st));
+  return AMRS_OK;
 }
 
 // Synchronise `stream`, then report (and clear) the device error flag set by
@@ -852,10 +1136,10 @@ amrs_status amrs_profile_stage_box(amrs_handle* h, const amrs_box* bx, const dou
   std::lock_guard<std::mutex> lk(h->mu);
   CK(cudaSetDevice(h->device));
   amrs_array4 slots[3] = {stage_in, s1, out};
-  if (amrs_status s = one_box(h, bx, dxinv, slots, 3)) return s;
-  List& L = *h->one;
-  if (!L.fused) return AMRS_ERR_SCHEME;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (amrs_status s = one_box(h, bx, dxinv, slots, 3, st)) return s;
+  List& L = *h->one;
+  if (!L.fused) { ring_release(h, st); return AMRS_ERR_SCHEME; }
   const DProg p = to_dprog(prog);
   cudaEvent_t ev[4];
   for (int i = 0; i < 4; ++i) CK(cudaEventCreate(&ev[i]));
@@ -868,7 +1152,7 @@ amrs_status amrs_profile_stage_box(amrs_handle* h, const amrs_box* bx, const dou
     if (e == cudaSuccess && L.sc.rhs_visc) e = launch_visc(L.tb, L.tot_v, h->nsm, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[2], st);
     if (e == cudaSuccess)
-      e = launch_keep_face(L.sc.order_keep, L.sc.rhs_visc != 0, L.tb, 0, 1, 2, p, 0, L.tma, h->derr, L.tot_work,
+      e = launch_keep_face(L.sc.order_keep, L.sc.rhs_visc != 0, L.tb, 0, 1, 2, p, 0, L.tma, h->derr, L.face_grid,
                            h->nsm, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[3], st);
     if (e == cudaSuccess) e = cudaEventSynchronize(ev[3]);
@@ -880,6 +1164,7 @@ amrs_status amrs_profile_stage_box(amrs_handle* h, const amrs_box* bx, const dou
     if (e != cudaSuccess) rs = cuda_fail(e, "amrs_profile_stage_box");
   }
   for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
+  ring_release(h, st);
   if (rs) return rs;
   for (int i = 0; i < 3; ++i) ms[i] = acc[i] / reps;
   ms[3] = ms[0] + ms[1] + ms[2];

@@ -131,7 +131,6 @@ keep_face_kernel(BoxTable tb, int s_in, int s_s1, int s_out, DProg prog, int rhs
   const int tid = threadIdx.x;
   double coef[3];
   keep_coeffs(ORDER, coef);
-  const int nwork = tb.fwork[tb.n];
   unsigned int phase_bits = 0u;
   const bool use_tma = tma.enabled != 0;
   if (use_tma) {
@@ -139,19 +138,19 @@ keep_face_kernel(BoxTable tb, int s_in, int s_s1, int s_out, DProg prog, int rhs
     __syncthreads();
   }
 
-  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
-    const int b = find_box_i(tb.fwork, tb.n, w);
+  // balanced static schedule: this CTA's segments cover an equal share of
+  // the (tile column x plane) work of the whole list
+  const int sbeg = tb.cta_seg[blockIdx.x], send = tb.cta_seg[blockIdx.x + 1];
+  for (int sgi = sbeg; sgi < send; ++sgi) {
+    const int4 sg = tb.seg[sgi];
+    const int b = sg.x;
     const BoxRec& R = tb.box[b];
-    const int local = w - tb.fwork[b];
-    const int ntxy = R.ntx * R.nty;
-    const int kzi = local / ntxy;
-    const int rem = local - kzi * ntxy;
-    const int tyi = rem / R.ntx, txi = rem - (rem / R.ntx) * R.ntx;
+    const int tyi = sg.y / R.ntx, txi = sg.y - (sg.y / R.ntx) * R.ntx;
     const int TX = R.tx, TY = R.ty;
     const int x0 = R.lo[0] + txi * TX, y0 = R.lo[1] + tyi * TY;
     const int txw = min(TX, R.hi[0] + 1 - x0), tyw = min(TY, R.hi[1] + 1 - y0);
-    const int k0 = R.lo[2] + kzi * R.kc;
-    const int k1 = min(k0 + R.kc, R.hi[2] + 1);
+    const int k0 = sg.z;
+    const int k1 = sg.w;
     const int QP = TX + 6, QR = TY + 2 * H, QS = QP * QR;
     const int TXP = TX + H;  // row pitch of x pair terms
     const DArr Q = R.q, VF = R.vf;
@@ -449,11 +448,10 @@ cudaError_t launch_visc(const BoxTable& tb, long long ncells, int nsm, cudaStrea
 }
 
 cudaError_t launch_keep_face(int order, bool visc, const BoxTable& tb, int s_in, int s_s1, int s_out,
-                             const DProg& prog, int rhs_only, const TmaDesc& tma, int* err, int nwork, int nsm,
+                             const DProg& prog, int rhs_only, const TmaDesc& tma, int* err, int grid, int nsm,
                              cudaStream_t st) {
-  if (nwork <= 0) return cudaSuccess;
-  const int per_sm = (order == 6) ? 1 : 2;
-  int grid = nwork < nsm * per_sm ? nwork : nsm * per_sm;
+  (void)nsm;
+  if (grid <= 0) return cudaSuccess;
   if (order == 2) return visc ? launch_face_t<2, true>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err, grid, st)
                               : launch_face_t<2, false>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err, grid, st);
   if (order == 4) return visc ? launch_face_t<4, true>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err, grid, st)
@@ -461,6 +459,8 @@ cudaError_t launch_keep_face(int order, bool visc, const BoxTable& tb, int s_in,
   return visc ? launch_face_t<6, true>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err, grid, st)
               : launch_face_t<6, false>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err, grid, st);
 }
+
+int keep_ctas_per_sm(int order) { return order == 6 ? 1 : 2; }
 
 bool keep_tile_fits(int order, int tx, int ty) {
   if (tx < 8 || ty < 1 || (tx % 2) || tx * ty > F_THREADS) return false;

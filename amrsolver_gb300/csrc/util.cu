@@ -55,6 +55,47 @@ __global__ void __launch_bounds__(256) halo_kernel(HaloBox hb) {
   }
 }
 
+// Ghost fill of every box of a list, each box being its own domain (an
+// ensemble member or an isolated box), one launch for all boxes.
+__global__ void __launch_bounds__(256) halo_list_kernel(BoxTable tb, const long long* gpre, int slot, int bl0, int bl1,
+                                                        int bl2, int bh0, int bh1, int bh2) {
+  const long long total = gpre[tb.n];
+  const int g = NGHOST;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < total;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int b = find_box_ll(gpre, tb.n, c);
+    const BoxRec& R = tb.box[b];
+    const int l = (int)(c - gpre[b]);
+    const int nx = R.hi[0] - R.lo[0] + 1 + 2 * g, ny = R.hi[1] - R.lo[1] + 1 + 2 * g;
+    const int i = l % nx + R.lo[0] - g;
+    const int t = l / nx;
+    const int j = t % ny + R.lo[1] - g;
+    const int k = t / ny + R.lo[2] - g;
+    const bool inside = i >= R.lo[0] && i <= R.hi[0] && j >= R.lo[1] && j <= R.hi[1] && k >= R.lo[2] &&
+                        k <= R.hi[2];
+    if (inside) continue;
+    const DArr U = R.slot[slot];
+    for (int n = 0; n < NCONS; ++n) {
+      bool flip = false;
+      const int si = map_coord(i, R.lo[0], R.hi[0], bl0, bh0, n, 0, flip);
+      const int sj = map_coord(j, R.lo[1], R.hi[1], bl1, bh1, n, 1, flip);
+      const int sk = map_coord(k, R.lo[2], R.hi[2], bl2, bh2, n, 2, flip);
+      const double v = U(si, sj, sk, n);
+      U(i, j, k, n) = flip ? -v : v;
+    }
+  }
+}
+
+cudaError_t launch_halo_list(const BoxTable& tb, const long long* gpre, long long total, int slot, const int bc_lo[3],
+                             const int bc_hi[3], int nsm, cudaStream_t st) {
+  long long blocks = (total + 255) / 256;
+  if (blocks > (long long)nsm * 8) blocks = (long long)nsm * 8;
+  if (blocks < 1) blocks = 1;
+  halo_list_kernel<<<(int)blocks, 256, 0, st>>>(tb, gpre, slot, bc_lo[0], bc_lo[1], bc_lo[2], bc_hi[0], bc_hi[1],
+                                                bc_hi[2]);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_halo(const HaloBox& hb, cudaStream_t st) {
   const long long total = (long long)(hb.hi[0] - hb.lo[0] + 7) * (hb.hi[1] - hb.lo[1] + 7) * (hb.hi[2] - hb.lo[2] + 7);
   long long blocks = (total + 255) / 256;

@@ -119,21 +119,21 @@ def cell_centres(n, dx, lo=(0, 0, 0), origin=(0.0, 0.0, 0.0), g=NGHOST):
 
 
 # ----------------------------------------------------------------- configs --
-def tgv(n=128, mach=0.1, gamma=1.4, g=NGHOST):
+def tgv(n=128, mach=0.1, gamma=1.4, g=NGHOST, amp=1.0):
     """Taylor-Green vortex on the periodic box [0,2pi]^3, rho = 1.
 
-    u = sin x cos y cos z, v = -cos x sin y cos z, w = 0,
-    p = 1/(gamma M^2) + (cos 2x + cos 2y)(cos 2z + 2)/16.
+    u = V0 sin x cos y cos z, v = -V0 cos x sin y cos z, w = 0,
+    p = 1/(gamma M^2) + V0^2 (cos 2x + cos 2y)(cos 2z + 2)/16, V0 = amp.
     Ghost cells hold the periodic continuation.
     """
     nn = (n, n, n)
     h = 2.0 * math.pi / n
     X, Y, Z = cell_centres(nn, (h, h, h), g=g)
     rho = np.ones_like(X)
-    u = np.sin(X) * np.cos(Y) * np.cos(Z)
-    v = -np.cos(X) * np.sin(Y) * np.cos(Z)
+    u = amp * np.sin(X) * np.cos(Y) * np.cos(Z)
+    v = -amp * np.cos(X) * np.sin(Y) * np.cos(Z)
     w = np.zeros_like(X)
-    p = 1.0 / (gamma * mach * mach) + (np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2.0) / 16.0
+    p = 1.0 / (gamma * mach * mach) + amp * amp * (np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2.0) / 16.0
     return prims_to_cons(rho, u, v, w, p, gamma), (h, h, h)
 
 

@@ -168,6 +168,16 @@ amrs_status amrs_boxlist_destroy(amrs_boxlist* bl);
 amrs_status amrs_boxlist_set_tile(amrs_boxlist* bl, int32_t nx, int32_t ny, int32_t nz, int32_t tx, int32_t ty,
                                   int32_t kchunk);
 
+/* Boundary codes applied to every box of the list as its own domain
+ * (ensemble members, isolated boxes): periodic wrap, foextrap or
+ * reflection as in amrs_fill_halo_box.  Once set, amrs_rk_step_boxlist
+ * fills each stage input's ghosts before its RHS (one launch for all boxes).
+ * NULL codes switch the fill off (ghosts kept as the caller set them). */
+amrs_status amrs_boxlist_set_bc(amrs_boxlist* bl, const int32_t bc_lo[3], const int32_t bc_hi[3]);
+/* Ghost fill of slot `slot` of every box with the codes of
+ * amrs_boxlist_set_bc. */
+amrs_status amrs_boxlist_fill_halo(amrs_boxlist* bl, int32_t slot, void* stream);
+
 /* RK stage over all boxes: stage input slot `in`, old state slot `s1`,
  * output slot `out` (valid cells).  One launch per kernel kind. */
 amrs_status amrs_rk_stage_boxlist(amrs_boxlist* bl, const amrs_stage_prog* prog, int32_t in, int32_t s1,
@@ -184,12 +194,31 @@ amrs_status amrs_rk_step_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t sta
 /* ---- adjoint ----------------------------------------------------------- */
 
 /* Vector-Jacobian product of one RHS evaluation of one box (KEEP + viscous
- * path): given the ghost-filled state and a cotangent `vbar` on the valid
- * cells, writes ubar = (d dSdt/d state)^T vbar into `ubar` over the ghosted
- * box (ghost entries hold the sensitivities to ghost values).  `ubar` is
- * overwritten. */
+ * path; no counterpart in the reference, whose lib/autodiff is absent):
+ * given the ghost-filled state and a cotangent `vbar` on the valid cells,
+ * writes ubar = (d dSdt/d state)^T vbar into `ubar` over the ghosted box
+ * (ghost entries hold the sensitivities to ghost values).  `ubar` is
+ * overwritten.  If `param_bar` (device, 2 doubles) is not NULL,
+ * vbar . d dSdt/d(visc_ref) and vbar . d dSdt/d(cond_ref) are added to it
+ * (constant-law closures only). */
 amrs_status amrs_rhs_vjp_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3], amrs_array4 state,
-                             amrs_array4 vbar, amrs_array4 ubar, void* stream);
+                             amrs_array4 vbar, amrs_array4 ubar, double* param_bar, void* stream);
+
+/* Adjoint of amrs_fill_halo_box: every valid cell of `ubar` (ghosted, in
+ * place) receives the cotangents of the ghost cells filled from it. */
+amrs_status amrs_fill_halo_box_adjoint(const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3],
+                                       amrs_array4 ubar, void* stream);
+
+/* VJP of one RK stage of one box (amrs_rk_stage_box preceded by
+ * amrs_fill_halo_box with bc_lo/bc_hi): given the cotangent `wbar` of the
+ * stage result (valid cells), ADDS the cotangent of the old state S1 to
+ * `s1bar` and the cotangent of the stage input's valid cells to `inbar`
+ * (ghost sensitivities folded back through the ghost fill).  `stage_in` is
+ * the ghost-filled stage input of the forward stage. */
+amrs_status amrs_rk_stage_vjp_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3],
+                                  const amrs_stage_prog* prog, const int32_t bc_lo[3], const int32_t bc_hi[3],
+                                  amrs_array4 stage_in, amrs_array4 wbar, amrs_array4 s1bar, amrs_array4 inbar,
+                                  double* param_bar, void* stream);
 
 /* ---- diagnostics ---------------------------------------------------- */
 

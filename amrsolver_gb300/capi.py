@@ -77,6 +77,7 @@ SIGNATURES = {
     "amrs_boxlist_destroy": (_S, [_P]),
     "amrs_boxlist_set_tile": (_S, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                    ctypes.c_int32, ctypes.c_int32]),
+    "amrs_boxlist_set_tiles": (_S, [_P, ctypes.POINTER(ctypes.c_int32)]),
     "amrs_boxlist_set_bc": (_S, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "amrs_boxlist_fill_halo": (_S, [_P, ctypes.c_int32, _P]),
     "amrs_rk_stage_boxlist": (_S, [_P, ctypes.POINTER(StageProg), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
@@ -325,6 +326,11 @@ class BoxList:
 
     def set_tile(self, n, tx, ty, kc):
         check(self._L.amrs_boxlist_set_tile(self.bl, n[0], n[1], n[2], tx, ty, kc), "amrs_boxlist_set_tile")
+
+    def set_tiles(self, tiles):
+        """tiles: per box (tx, ty, kchunk)."""
+        flat = (ctypes.c_int32 * (3 * self.n))(*[int(v) for t in tiles for v in t])
+        check(self._L.amrs_boxlist_set_tiles(self.bl, flat), "amrs_boxlist_set_tiles")
 
     def set_bc(self, bc_lo, bc_hi):
         if bc_lo is None:

@@ -789,26 +789,19 @@ amrs_status amrs_boxlist_destroy(amrs_boxlist* bl) {
   return AMRS_OK;
 }
 
-amrs_status amrs_boxlist_set_tile(amrs_boxlist* bl, int32_t nx, int32_t ny, int32_t nz, int32_t tx, int32_t ty,
-                                  int32_t kchunk) {
-  if (!bl) return AMRS_ERR_NULL;
+}  // extern "C"
+
+namespace {
+
+// Rebuild a list's tables with per-box tiles (tiles[3*b] = tx, ty, kchunk).
+amrs_status relist_with_tiles(amrs_boxlist* bl, const std::vector<int>& tiles) {
   List& L = bl->L;
-  if (!keep_tile_fits(L.sc.order_keep, tx, ty) || kchunk < 1) return AMRS_ERR_SIZE;
-  std::lock_guard<std::mutex> lk(bl->h->mu);
-  CK(cudaSetDevice(bl->h->device));
-  CK(cudaDeviceSynchronize());
-  std::vector<int> tiles(3 * L.n);
   std::vector<amrs_array4> states(L.n * L.nslots);
   std::vector<double> dxinv(3 * L.n);
   std::vector<int32_t> cidx(L.n);
   std::vector<amrs_closures> cls(L.cls.size());
   for (int b = 0; b < L.n; ++b) {
     const BoxRec& R = L.hbox[b];
-    const bool match = (nx == 0 && ny == 0 && nz == 0) ||
-                       (bn(L.boxes[b], 0) == nx && bn(L.boxes[b], 1) == ny && bn(L.boxes[b], 2) == nz);
-    tiles[3 * b] = match ? tx : R.tx;
-    tiles[3 * b + 1] = match ? ty : R.ty;
-    tiles[3 * b + 2] = match ? std::min<int>(kchunk, bn(L.boxes[b], 2)) : R.kc;
     for (int d = 0; d < 3; ++d) dxinv[3 * b + d] = R.dxinv[d];
     cidx[b] = R.cl;
     for (int s = 0; s < L.nslots; ++s) {
@@ -832,6 +825,47 @@ amrs_status amrs_boxlist_set_tile(amrs_boxlist* bl, int32_t nx, int32_t ny, int3
   if (L.graph) { cudaGraphExecDestroy(L.graph); L.graph = nullptr; }
   return list_build(bl->h, L, L.n, boxes.data(), dxinv.data(), L.nslots, states.data(), cidx.data(),
                     (int)cls.size(), cls.data(), tiles.data());
+}
+
+}  // namespace
+
+extern "C" {
+
+amrs_status amrs_boxlist_set_tile(amrs_boxlist* bl, int32_t nx, int32_t ny, int32_t nz, int32_t tx, int32_t ty,
+                                  int32_t kchunk) {
+  if (!bl) return AMRS_ERR_NULL;
+  List& L = bl->L;
+  if (!keep_tile_fits(L.sc.order_keep, tx, ty) || kchunk < 1) return AMRS_ERR_SIZE;
+  std::lock_guard<std::mutex> lk(bl->h->mu);
+  CK(cudaSetDevice(bl->h->device));
+  CK(cudaDeviceSynchronize());
+  std::vector<int> tiles(3 * L.n);
+  for (int b = 0; b < L.n; ++b) {
+    const BoxRec& R = L.hbox[b];
+    const bool match = (nx == 0 && ny == 0 && nz == 0) ||
+                       (bn(L.boxes[b], 0) == nx && bn(L.boxes[b], 1) == ny && bn(L.boxes[b], 2) == nz);
+    tiles[3 * b] = match ? tx : R.tx;
+    tiles[3 * b + 1] = match ? ty : R.ty;
+    tiles[3 * b + 2] = match ? std::min<int>(kchunk, bn(L.boxes[b], 2)) : R.kc;
+  }
+  return relist_with_tiles(bl, tiles);
+}
+
+amrs_status amrs_boxlist_set_tiles(amrs_boxlist* bl, const int32_t* tiles) {
+  if (!bl || !tiles) return AMRS_ERR_NULL;
+  List& L = bl->L;
+  std::vector<int> t(3 * L.n);
+  for (int b = 0; b < L.n; ++b) {
+    if (!keep_tile_fits(L.sc.order_keep, tiles[3 * b], tiles[3 * b + 1]) || tiles[3 * b + 2] < 1)
+      return AMRS_ERR_SIZE;
+    t[3 * b] = tiles[3 * b];
+    t[3 * b + 1] = tiles[3 * b + 1];
+    t[3 * b + 2] = std::min<int>(tiles[3 * b + 2], bn(L.boxes[b], 2));
+  }
+  std::lock_guard<std::mutex> lk(bl->h->mu);
+  CK(cudaSetDevice(bl->h->device));
+  CK(cudaDeviceSynchronize());
+  return relist_with_tiles(bl, t);
 }
 
 amrs_status amrs_boxlist_set_bc(amrs_boxlist* bl, const int32_t bc_lo[3], const int32_t bc_hi[3]) {

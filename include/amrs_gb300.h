@@ -178,6 +178,10 @@ amrs_status amrs_boxlist_set_bc(amrs_boxlist* bl, const int32_t bc_lo[3], const 
  * amrs_boxlist_set_bc. */
 amrs_status amrs_boxlist_fill_halo(amrs_boxlist* bl, int32_t slot, void* stream);
 
+/* Per-box tiles in one call: tiles[3*b + {0,1,2}] = (tx, ty, kchunk) of
+ * box b (the autotuner's output). */
+amrs_status amrs_boxlist_set_tiles(amrs_boxlist* bl, const int32_t* tiles);
+
 /* RK stage over all boxes: stage input slot `in`, old state slot `s1`,
  * output slot `out` (valid cells).  One launch per kernel kind. */
 amrs_status amrs_rk_stage_boxlist(amrs_boxlist* bl, const amrs_stage_prog* prog, int32_t in, int32_t s1,

@@ -65,6 +65,8 @@ SIGNATURES = {
     "amrs_rk_program": (_S, [ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.POINTER(StageProg),
                              ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]),
     "amrs_rhs_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double), Array4, Array4, _P]),
+    "amrs_rhs_box_noalloc": (_S, [ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ctypes.POINTER(CBox),
+                                  ctypes.POINTER(ctypes.c_double), Array4, Array4, _P]),
     "amrs_rk_stage_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(StageProg),
                                ctypes.c_double, Array4, Array4, Array4, _P]),
     "amrs_fill_halo_box": (_S, [ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),

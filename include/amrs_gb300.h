@@ -127,6 +127,20 @@ amrs_status amrs_rk_program(int32_t order_rk, int32_t stages_rk, double dt, amrs
 amrs_status amrs_rhs_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3], amrs_array4 state,
                          amrs_array4 dsdt, void* stream);
 
+/* amrs_rhs_box without any device allocation: no counterpart in the
+ * reference.  Some callers cannot call cudaMalloc (a host whose arena or
+ * memory pool owns all device memory, or one with a fixed device-memory
+ * budget); this variant of the fused KEEP + viscous RHS keeps its scratch in
+ * one static device array of the library instead of a handle.  Limits:
+ * KEEP without JST only, boxes of at most 32 cells per direction
+ * (AMRS_ERR_SIZE beyond); the array (6.9 MB) lives on every device that
+ * loads the library until exit; every call shares it, so calls that overlap
+ * on the GPU race.  The first call on a device looks the array's address up
+ * with that device current: make it before any stream capture.  Results
+ * are identical to amrs_rhs_box. */
+amrs_status amrs_rhs_box_noalloc(const amrs_scheme* scheme, const amrs_closures* closures, const amrs_box* bx,
+                                 const double dxinv[3], amrs_array4 state, amrs_array4 dsdt, void* stream);
+
 /* One RK stage of one box: RHS of the ghost-filled stage input `stage_in`
  * followed by the stage's BLAS-1 program, writing register S2 into the
  * valid cells of `out`.  `s1` holds the old state S1.  `out` must not alias

@@ -35,7 +35,7 @@ class CClosures(ctypes.Structure):
 
 class CScheme(ctypes.Structure):
     _fields_ = [("rhs_euler", ctypes.c_int32), ("rhs_visc", ctypes.c_int32), ("flux_euler", ctypes.c_int32),
-                ("order_keep", ctypes.c_int32), ("art_diss", ctypes.c_int32)]
+                ("order_keep", ctypes.c_int32), ("art_diss", ctypes.c_int32), ("weno_fast", ctypes.c_int32)]
 
 
 class CBox(ctypes.Structure):
@@ -81,6 +81,8 @@ SIGNATURES = {
                                    ctypes.c_int32, ctypes.c_int32]),
     "amrs_boxlist_set_tiles": (_S, [_P, ctypes.POINTER(ctypes.c_int32)]),
     "amrs_boxlist_set_bc": (_S, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
+    "amrs_boxlist_set_domain": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_int32),
+                                     ctypes.POINTER(ctypes.c_int32)]),
     "amrs_boxlist_fill_halo": (_S, [_P, ctypes.c_int32, _P]),
     "amrs_rk_stage_boxlist": (_S, [_P, ctypes.POINTER(StageProg), ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                    _P]),
@@ -141,7 +143,8 @@ def c_closures(cl):
 
 
 def c_scheme(sc):
-    return CScheme(int(sc.rhs_euler), int(sc.rhs_visc), int(sc.flux_euler), int(sc.order_keep), int(sc.art_diss))
+    return CScheme(int(sc.rhs_euler), int(sc.rhs_visc), int(sc.flux_euler), int(sc.order_keep), int(sc.art_diss),
+                   int(getattr(sc, "weno_fast", 0)))
 
 
 def c_box(lo, n):
@@ -255,7 +258,8 @@ class Handle:
                                             _stream_ptr(stream)), "amrs_rk_stage_vjp_box")
 
     def profile_stage_box(self, prog, Uin, U1, Uout, dxinv, lo=(0, 0, 0), reps=5, stream=None):
-        """Per-kernel ms of one fused stage: (prims, viscous cells, face kernel, total)."""
+        """Per-kernel ms of one stage: (prims [+ WENO point fluxes], viscous
+        cells, Euler face kernel [fused: + divergence + program], total)."""
         nz, ny, nx = (s - 2 * NGHOST for s in Uin.shape[1:])
         g1 = (U1.shape[1] - nz) // 2
         go = (Uout.shape[1] - nz) // 2
@@ -339,6 +343,13 @@ class BoxList:
             check(self._L.amrs_boxlist_set_bc(self.bl, None, None), "amrs_boxlist_set_bc")
         else:
             check(self._L.amrs_boxlist_set_bc(self.bl, i3(bc_lo), i3(bc_hi)), "amrs_boxlist_set_bc")
+
+    def set_domain(self, dom_lo, dom_n, bc_lo, bc_hi):
+        """The boxes tile the domain box starting at `dom_lo` with extents
+        `dom_n` (x, y, z): single-level ghost fill across the level."""
+        dom = c_box(dom_lo, dom_n)
+        check(self._L.amrs_boxlist_set_domain(self.bl, ctypes.byref(dom), i3(bc_lo), i3(bc_hi)),
+              "amrs_boxlist_set_domain")
 
     def fill_halo(self, slot, stream=None):
         check(self._L.amrs_boxlist_fill_halo(self.bl, slot, _stream_ptr(stream)), "amrs_boxlist_fill_halo")

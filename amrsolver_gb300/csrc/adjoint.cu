@@ -26,6 +26,7 @@ struct AdjRec {
   DArr ubar;    // output cotangent of the state, grow(box,3)
   DArr pair[3][3];  // [d][l-1]: NQA comps lo-end (0..5) + hi-end (6..11) over grow(box,3)
   DArr vg;      // viscous cotangents over grow(box,1): centre u,v,w,T (0..3), gradients (4..15)
+  int visc;     // vg holds data (the viscous reverse pass ran)
 };
 constexpr int NQA = 6;  // rho, u, v, w, T, p (e = cv*T folded into T)
 
@@ -250,7 +251,10 @@ __global__ void __launch_bounds__(256) adj_gather_kernel(BoxTable tb, AdjRec ar,
     const int k = t / ny + R.lo[2] - g3;
     const DArr Ub = ar.ubar;
     const long long ou = Ub.off(i, j, k);
-    const int gact = gpair > 2 ? gpair : 2;  // cells any cotangent reaches
+    // cells any cotangent of this pass reaches (viscous stencils: 2 ghosts);
+    // beyond them Q is not computed and ubar is zero
+    const int gvisc = ar.visc ? 2 : 0;
+    const int gact = gpair > gvisc ? gpair : gvisc;
     if (i < R.lo[0] - gact || i > R.hi[0] + gact || j < R.lo[1] - gact || j > R.hi[1] + gact ||
         k < R.lo[2] - gact || k > R.hi[2] + gact) {
 #pragma unroll
@@ -273,8 +277,8 @@ __global__ void __launch_bounds__(256) adj_gather_kernel(BoxTable tb, AdjRec ar,
     }
     const DArr G = ar.vg;
     auto inside1 = [&](int a, int b, int c) {
-      return a >= R.lo[0] - 1 && a <= R.hi[0] + 1 && b >= R.lo[1] - 1 && b <= R.hi[1] + 1 && c >= R.lo[2] - 1 &&
-             c <= R.hi[2] + 1;
+      return ar.visc && a >= R.lo[0] - 1 && a <= R.hi[0] + 1 && b >= R.lo[1] - 1 && b <= R.hi[1] + 1 &&
+             c >= R.lo[2] - 1 && c <= R.hi[2] + 1;
     };
     if (inside1(i, j, k)) {
       const long long o = G.off(i, j, k);
@@ -441,18 +445,21 @@ cudaError_t launch_rhs_vjp(int order, const BoxTable& tb, const AdjRecHost& ah, 
   for (int d = 0; d < 3; ++d)
     for (int l = 0; l < 3; ++l) ar.pair[d][l] = ah.pair[d][l];
   ar.vg = ah.vg;
+  ar.visc = ah.visc;
   const int H = order / 2;
   const long long n0 = ah.n[0], n1 = ah.n[1], n2 = ah.n[2];
   long long npair = 0;
   for (int d = 0; d < 3; ++d)
     for (int l = 1; l <= H; ++l) npair += (n0 + (d == 0) * l) * (n1 + (d == 1) * l) * (n2 + (d == 2) * l);
+  // order 0: no KEEP pairs (the viscous part of another scheme's RHS)
   if (order == 2) adj_pair_kernel<2><<<grid256(npair, nsm), 256, 0, st>>>(tb, ar, npair);
   else if (order == 4) adj_pair_kernel<4><<<grid256(npair, nsm), 256, 0, st>>>(tb, ar, npair);
-  else adj_pair_kernel<6><<<grid256(npair, nsm), 256, 0, st>>>(tb, ar, npair);
+  else if (order == 6) adj_pair_kernel<6><<<grid256(npair, nsm), 256, 0, st>>>(tb, ar, npair);
   const long long nv = (n0 + 2) * (n1 + 2) * (n2 + 2);
   if (ah.visc) adj_visc_kernel<<<grid256(nv, nsm), 256, 0, st>>>(tb, ar, nv, pbar);
   const long long ng = (n0 + 6) * (n1 + 6) * (n2 + 6);
-  if (order == 2) adj_gather_kernel<2><<<grid256(ng, nsm), 256, 0, st>>>(tb, ar, ng, H);
+  if (order == 0) adj_gather_kernel<0><<<grid256(ng, nsm), 256, 0, st>>>(tb, ar, ng, 0);
+  else if (order == 2) adj_gather_kernel<2><<<grid256(ng, nsm), 256, 0, st>>>(tb, ar, ng, H);
   else if (order == 4) adj_gather_kernel<4><<<grid256(ng, nsm), 256, 0, st>>>(tb, ar, ng, H);
   else adj_gather_kernel<6><<<grid256(ng, nsm), 256, 0, st>>>(tb, ar, ng, H);
   return cudaGetLastError();

@@ -88,13 +88,16 @@ __device__ __forceinline__ void keep_pair(const double* q1, const double* q2, do
   const double cy = t8 * (q1[QV] + q2[QV]);
   const double cz = t8 * (q1[QW] + q2[QW]);
   const double ce = t8 * (q1[QE] + q2[QE]);
-  const double fdiv = 0.5 * (q1[QPRES] + q2[QPRES]);           // fDiv
-  const double fgdiv = 0.5 * (q1[QPRES] * q2[QN] + q2[QPRES] * q1[QN]);  // fgDiv
+  // fDiv = 0.5*(p1+p2) and fgDiv = 0.5*(p1*un2 + p2*un1) enter sums; the
+  // products by 0.5 are exact, so fma(0.5, s, x) rounds exactly like
+  // x + 0.5*s evaluated in two steps (one FP64 instruction fewer each).
+  const double psum = q1[QPRES] + q2[QPRES];
+  const double pu = q1[QPRES] * q2[QN] + q2[QPRES] * q1[QN];
   T[URHO] = coef * massflx;
-  T[UMX] = coef * (D == 0 ? (cx + fdiv) : cx);
-  T[UMY] = coef * (D == 1 ? (cy + fdiv) : cy);
-  T[UMZ] = coef * (D == 2 ? (cz + fdiv) : cz);
-  T[UET] = coef * (massflx * ke + ce + fgdiv);
+  T[UMX] = coef * (D == 0 ? fma(0.5, psum, cx) : cx);
+  T[UMY] = coef * (D == 1 ? fma(0.5, psum, cy) : cy);
+  T[UMZ] = coef * (D == 2 ? fma(0.5, psum, cz) : cz);
+  T[UET] = coef * fma(0.5, pu, massflx * ke + ce);
 }
 
 // Cell-centred viscous fluxes (src/rhs/CNS_hydro_K.h:108-172) from the

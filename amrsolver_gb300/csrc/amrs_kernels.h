@@ -38,7 +38,13 @@ struct FaceTable {
 cudaError_t launch_keep_faces_plain(int order, const BoxTable& tb, const FaceTable& ft, long long nfaces[3],
                                     int nsm, cudaStream_t st);
 cudaError_t launch_weno(const BoxTable& tb, const FaceTable& ft, int s_in, long long ngcells, long long nfaces[3],
-                        int nsm, cudaStream_t st);
+                        bool ref_order, int nsm, cudaStream_t st);
+// physical fluxes and lambda only (the forward values the WENO adjoint reads)
+cudaError_t launch_weno_point(const BoxTable& tb, const FaceTable& ft, int s_in, long long ngcells, int nsm,
+                              cudaStream_t st);
+// the WENO face kernel alone (point fluxes already current)
+cudaError_t launch_weno_faces(const BoxTable& tb, const FaceTable& ft, int s_in, long long nfaces[3], bool ref_order,
+                              int nsm, cudaStream_t st);
 cudaError_t launch_riemann(const BoxTable& tb, const FaceTable& ft, const long long* spre_d[3],
                            long long nslope[3], long long nfaces[3], int nsm, cudaStream_t st);
 cudaError_t launch_jst(const BoxTable& tb, const FaceTable& ft, int s_in, long long ngcells, long long nvalid,
@@ -65,13 +71,25 @@ struct AdjRecHost {
   int n[3];
   int visc;
 };
+// order 0: viscous part and cons2prim reverse only (no KEEP pairs)
 cudaError_t launch_rhs_vjp(int order, const BoxTable& tb, const AdjRecHost& ah, double* pbar, int nsm,
                            cudaStream_t st);
+// WENO5 Euler part of the RHS VJP, added to ubar (adjoint_weno.cu)
+size_t weno_vjp_buffer_bytes(const int n[3]);
+cudaError_t launch_weno_vjp(const BoxTable& tb, const FaceRec& fr, const DArr& vbar, const DArr& ubar, double* buf,
+                            const int n[3], int nsm, cudaStream_t st);
 cudaError_t launch_adj_prog(const BoxRec& R, const DProg& prog, const DArr& wbar, const DArr& s1bar, const DArr& inbar,
                             const DArr& vbar, int accumulate, int nsm, cudaStream_t st);
 cudaError_t launch_adj_halo(const HaloBox& hb, int nsm, cudaStream_t st);
 cudaError_t launch_halo_list(const BoxTable& tb, const long long* gpre, long long total, int slot, const int bc_lo[3],
                              const int bc_hi[3], int nsm, cudaStream_t st);
+// domain of a level whose boxes tile it, with its physical boundary codes
+struct LevelDomain {
+  int lo[3], hi[3];
+  int bc_lo[3], bc_hi[3];
+};
+cudaError_t launch_halo_level(const BoxTable& tb, const long long* gpre, const int* owner, long long total, int slot,
+                              const LevelDomain& dom, int nsm, cudaStream_t st);
 cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t st);
 cudaError_t launch_estdt(const BoxTable& tb, int s_in, long long nvalid, double cfl, unsigned long long* bits,
                          double* dt_out, int nsm, cudaStream_t st);

@@ -76,6 +76,7 @@ amrs_status check_scheme(const amrs_scheme& s) {
   if (s.flux_euler < 0 || s.flux_euler > 2) return AMRS_ERR_SCHEME;
   if (s.flux_euler == 1 && !(s.order_keep == 2 || s.order_keep == 4 || s.order_keep == 6)) return AMRS_ERR_SCHEME;
   if (s.art_diss != 0 && s.art_diss != 1) return AMRS_ERR_SCHEME;
+  if (s.weno_fast != 0 && s.weno_fast != 1) return AMRS_ERR_SCHEME;
   return AMRS_OK;
 }
 
@@ -147,12 +148,18 @@ struct List {
   int graph_key[6] = {0, 0, 0, 0, 0, 0};
   double graph_dt = 0.0;
   int graph_result = -1;
-  int has_bc = 0;  // fill each stage input's ghosts, every box its own domain
+  // ghost fill of each stage input: 0 none (ghosts frozen), 1 every box its
+  // own domain (amrs_boxlist_set_bc), 2 the boxes tile one domain
+  // (amrs_boxlist_set_domain: neighbour copies, periodic images, physical BCs)
+  int has_bc = 0;
   int bc_lo[3] = {-1, -1, -1}, bc_hi[3] = {-1, -1, -1};
+  LevelDomain dom{};
+  int* d_owner = nullptr;  // has_bc == 2: owning box of every grown cell's source (-1: valid cell)
   ~List() {
     if (graph) cudaGraphExecDestroy(graph);
     if (dtab) cudaFree(dtab);
     if (dscr) cudaFree(dscr);
+    if (d_owner) cudaFree(d_owner);
   }
 };
 
@@ -476,7 +483,7 @@ amrs_status list_stage(amrs_handle* h, List& L, const DProg& prog, int s_in, int
     }
   if (sc.rhs_euler) {
     if (sc.flux_euler == 1) CK(launch_keep_faces_plain(sc.order_keep, L.tb, L.ft, nf, nsm, st));
-    else if (sc.flux_euler == 2) CK(launch_weno(L.tb, L.ft, s_in, L.tot_g, nf, nsm, st));
+    else if (sc.flux_euler == 2) CK(launch_weno(L.tb, L.ft, s_in, L.tot_g, nf, sc.weno_fast == 0, nsm, st));
     else {
       long long ns[3] = {L.tot_s[0], L.tot_s[1], L.tot_s[2]};
       CK(launch_riemann(L.tb, L.ft, L.d_spre, ns, nf, nsm, st));
@@ -827,6 +834,86 @@ amrs_status relist_with_tiles(amrs_boxlist* bl, const std::vector<int>& tiles) {
                     (int)cls.size(), cls.data(), tiles.data());
 }
 
+// Host mirror of the device map_coord (coordinates only): the domain cell a
+// ghost coordinate reads under periodic / foextrap / reflecting boundaries.
+int map_coord_host(int c, int lo, int hi, int bcl, int bch) {
+  if (c >= lo && c <= hi) return c;
+  const int n = hi - lo + 1;
+  const bool low = c < lo;
+  const int phys = low ? bcl : bch;
+  if (phys == -1) {
+    int r = (c - lo) % n;
+    if (r < 0) r += n;
+    return lo + r;
+  }
+  if (phys == 2) return low ? lo : hi;
+  return low ? 2 * lo - c - 1 : 2 * hi - c + 1;
+}
+
+bool box_has(const amrs_box& b, int i, int j, int k) {
+  return i >= b.lo[0] && i <= b.hi[0] && j >= b.lo[1] && j <= b.hi[1] && k >= b.lo[2] && k <= b.hi[2];
+}
+
+bool boxes_meet(const amrs_box& a, const amrs_box& b) {
+  for (int d = 0; d < 3; ++d)
+    if (a.hi[d] < b.lo[d] || b.hi[d] < a.lo[d]) return false;
+  return true;
+}
+
+// Owner table of a level tiling `dom`: for every cell of every grow(box,3)
+// (in the order of the flattened ghost-fill launch) the box whose valid
+// cell the ghost reads, -1 for valid cells.  Boxes must be disjoint and
+// every source cell covered (AMRS_ERR_BOX otherwise).
+amrs_status level_owner_table(const List& L, const LevelDomain& dom, std::vector<int>& owner) {
+  constexpr int BS = 8;  // bins of 8^3 domain cells listing the boxes that meet them
+  int nb[3];
+  for (int d = 0; d < 3; ++d) nb[d] = (dom.hi[d] - dom.lo[d] + BS) / BS;
+  std::vector<std::vector<int>> bins((size_t)nb[0] * nb[1] * nb[2]);
+  auto bin_of = [&](int i, int j, int k) {
+    return ((size_t)((k - dom.lo[2]) / BS) * nb[1] + (size_t)((j - dom.lo[1]) / BS)) * nb[0] +
+           (size_t)((i - dom.lo[0]) / BS);
+  };
+  for (int b = 0; b < L.n; ++b) {
+    const amrs_box& B = L.boxes[b];
+    int b0[3], b1[3];
+    for (int d = 0; d < 3; ++d) { b0[d] = (B.lo[d] - dom.lo[d]) / BS; b1[d] = (B.hi[d] - dom.lo[d]) / BS; }
+    for (int z = b0[2]; z <= b1[2]; ++z)
+      for (int y = b0[1]; y <= b1[1]; ++y)
+        for (int x = b0[0]; x <= b1[0]; ++x) {
+          auto& v = bins[((size_t)z * nb[1] + y) * nb[0] + x];
+          for (int o : v)
+            if (boxes_meet(L.boxes[o], B)) return AMRS_ERR_BOX;  // overlapping boxes
+          v.push_back(b);
+        }
+  }
+  owner.assign((size_t)L.gcell[L.n], -1);
+  const int g = NGHOST;
+  for (int b = 0; b < L.n; ++b) {
+    const amrs_box& B = L.boxes[b];
+    size_t idx = (size_t)L.gcell[b];
+    for (int k = B.lo[2] - g; k <= B.hi[2] + g; ++k)
+      for (int j = B.lo[1] - g; j <= B.hi[1] + g; ++j)
+        for (int i = B.lo[0] - g; i <= B.hi[0] + g; ++i, ++idx) {
+          if (box_has(B, i, j, k)) continue;
+          const int si = map_coord_host(i, dom.lo[0], dom.hi[0], dom.bc_lo[0], dom.bc_hi[0]);
+          const int sj = map_coord_host(j, dom.lo[1], dom.hi[1], dom.bc_lo[1], dom.bc_hi[1]);
+          const int sk = map_coord_host(k, dom.lo[2], dom.hi[2], dom.bc_lo[2], dom.bc_hi[2]);
+          int src = -1;
+          for (int o : bins[bin_of(si, sj, sk)])
+            if (box_has(L.boxes[o], si, sj, sk)) { src = o; break; }
+          if (src < 0) return AMRS_ERR_BOX;  // the level does not cover this source cell
+          owner[idx] = src;
+        }
+  }
+  return AMRS_OK;
+}
+
+// Ghost fill of one state slot of every box of a list (before a stage).
+cudaError_t list_fill(amrs_handle* h, List& L, int slot, cudaStream_t st) {
+  if (L.has_bc == 2) return launch_halo_level(L.tb, L.ft.gpre, L.d_owner, L.tot_g, slot, L.dom, h->nsm, st);
+  return launch_halo_list(L.tb, L.ft.gpre, L.tot_g, slot, L.bc_lo, L.bc_hi, h->nsm, st);
+}
+
 }  // namespace
 
 extern "C" {
@@ -891,14 +978,45 @@ amrs_status amrs_boxlist_set_bc(amrs_boxlist* bl, const int32_t bc_lo[3], const 
   return AMRS_OK;
 }
 
+amrs_status amrs_boxlist_set_domain(amrs_boxlist* bl, const amrs_box* domain, const int32_t bc_lo[3],
+                                    const int32_t bc_hi[3]) {
+  if (!bl || !domain || !bc_lo || !bc_hi) return AMRS_ERR_NULL;
+  List& L = bl->L;
+  if (!box_ok(*domain)) return AMRS_ERR_BOX;
+  LevelDomain dom{};
+  for (int d = 0; d < 3; ++d) {
+    if ((bc_lo[d] == -1) != (bc_hi[d] == -1)) return AMRS_ERR_BC;
+    for (int s = 0; s < 2; ++s) {
+      const int p = s ? bc_hi[d] : bc_lo[d];
+      if (p == 1 || p == 6 || p < -1 || p > 6) return AMRS_ERR_BC;
+    }
+    // reflections and periodic images stay inside a domain of >= 3 cells
+    if (bn(*domain, d) < NGHOST) return AMRS_ERR_BOX;
+    dom.lo[d] = domain->lo[d]; dom.hi[d] = domain->hi[d];
+    dom.bc_lo[d] = bc_lo[d]; dom.bc_hi[d] = bc_hi[d];
+  }
+  for (int b = 0; b < L.n; ++b)
+    for (int d = 0; d < 3; ++d)
+      if (L.boxes[b].lo[d] < dom.lo[d] || L.boxes[b].hi[d] > dom.hi[d]) return AMRS_ERR_BOX;
+  std::vector<int> owner;
+  if (amrs_status s = level_owner_table(L, dom, owner)) return s;
+  CK(cudaSetDevice(bl->h->device));
+  if (L.d_owner) { CK(cudaDeviceSynchronize()); cudaFree(L.d_owner); L.d_owner = nullptr; }
+  CK(cudaMalloc(&L.d_owner, owner.size() * sizeof(int)));
+  CK(cudaMemcpy(L.d_owner, owner.data(), owner.size() * sizeof(int), cudaMemcpyHostToDevice));
+  L.dom = dom;
+  L.has_bc = 2;
+  if (L.graph) { cudaGraphExecDestroy(L.graph); L.graph = nullptr; }
+  return AMRS_OK;
+}
+
 amrs_status amrs_boxlist_fill_halo(amrs_boxlist* bl, int32_t slot, void* stream) {
   if (!bl) return AMRS_ERR_NULL;
   List& L = bl->L;
   if (!L.has_bc) return AMRS_ERR_STATE;
   if (slot < 0 || slot >= L.nslots) return AMRS_ERR_SIZE;
   CK(cudaSetDevice(bl->h->device));
-  CK(launch_halo_list(L.tb, L.ft.gpre, L.tot_g, slot, L.bc_lo, L.bc_hi, bl->h->nsm,
-                      static_cast<cudaStream_t>(stream)));
+  CK(list_fill(bl->h, L, slot, static_cast<cudaStream_t>(stream)));
   return AMRS_OK;
 }
 
@@ -934,7 +1052,7 @@ amrs_status amrs_rk_step_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t sta
       const int in = (progs[i].src_state == 0) ? s1 : cur;
       int out = outs[which];
       if (out == in) { which ^= 1; out = outs[which]; }
-      if (L.has_bc) CK(launch_halo_list(L.tb, L.ft.gpre, L.tot_g, in, L.bc_lo, L.bc_hi, bl->h->nsm, s));
+      if (L.has_bc) CK(list_fill(bl->h, L, in, s));
       if (amrs_status e = list_stage(bl->h, L, to_dprog(&progs[i]), in, s1, out, 0, s)) return e;
       cur = out;
       which ^= 1;
@@ -979,16 +1097,29 @@ namespace {
 struct AdjScratch {
   AdjRecHost ah;
   DArr vbar_tmp, ubar_tmp;
+  double* wbuf = nullptr;  // WENO per-face cotangent slots
+  int order = 0;           // KEEP order of the pair pass (0: none)
 };
 
+// Schemes with a reverse pass: KEEP (+ viscous), WENO5 LLF (+ viscous), viscous only.
+bool vjp_scheme(const amrs_scheme& s) {
+  if (s.art_diss) return false;
+  if (!s.rhs_euler) return s.rhs_visc != 0;
+  return s.flux_euler == 1 || s.flux_euler == 2;
+}
+bool weno_scheme(const amrs_scheme& s) { return s.rhs_euler && s.flux_euler == 2; }
+
 amrs_status adj_prepare(amrs_handle* h, const amrs_box& B, AdjScratch& S, cudaStream_t st) {
-  const int H = h->sc.order_keep / 2;
+  S.order = fused_path(h->sc) ? h->sc.order_keep : 0;
+  const int H = S.order / 2;
+  const int nb[3] = {bn(B, 0), bn(B, 1), bn(B, 2)};
   auto cells = [&](int g) { return (size_t)grown_cells(B, g); };
   size_t off = 0;
   const size_t o_pair = off; off = align_up(off + cells(3) * 12 * 8 * 3 * H, 256);
   const size_t o_vg = off; off = align_up(off + cells(1) * 16 * 8, 256);
   const size_t o_v = off; off = align_up(off + cells(0) * 5 * 8, 256);
   const size_t o_u = off; off = align_up(off + cells(3) * 5 * 8, 256);
+  const size_t o_w = off; off = align_up(off + (weno_scheme(h->sc) ? weno_vjp_buffer_bytes(nb) : 0), 256);
   if (off > h->adj_bytes) {
     if (h->adj) { CK(cudaStreamSynchronize(st)); cudaFree(h->adj); h->adj = nullptr; h->adj_bytes = 0; }
     CK(cudaMalloc(&h->adj, off));
@@ -1010,8 +1141,24 @@ amrs_status adj_prepare(amrs_handle* h, const amrs_box& B, AdjScratch& S, cudaSt
   S.ubar_tmp = mk(o_u, 3);
   for (int d = 0; d < 3; ++d) S.ah.n[d] = bn(B, d);
   S.ah.visc = h->sc.rhs_visc != 0;
-  CK(cudaMemsetAsync(P + o_pair, 0, cells(3) * 12 * 8 * 3 * H, st));
+  S.wbuf = reinterpret_cast<double*>(P + o_w);
+  if (H > 0) CK(cudaMemsetAsync(P + o_pair, 0, cells(3) * 12 * 8 * 3 * H, st));
   return AMRS_OK;
+}
+
+// Reverse pass of one RHS of the list's single box (state in slot 0):
+// primitives, then the KEEP-pair / viscous / cons2prim reverse kernels,
+// then the WENO5 Euler part.
+cudaError_t rhs_vjp_launch(amrs_handle* h, List& L, const amrs_box& B, AdjScratch& S, double* param_bar,
+                           cudaStream_t st) {
+  cudaError_t e = launch_prims(L.tb, 0, L.tot_p, h->nsm, st);
+  if (e == cudaSuccess) e = launch_rhs_vjp(S.order, L.tb, S.ah, param_bar, h->nsm, st);
+  if (e == cudaSuccess && weno_scheme(h->sc)) {
+    const int nb[3] = {bn(B, 0), bn(B, 1), bn(B, 2)};
+    e = launch_weno_point(L.tb, L.ft, 0, L.tot_g, h->nsm, st);
+    if (e == cudaSuccess) e = launch_weno_vjp(L.tb, L.hface[0], S.ah.vbar, S.ah.ubar, S.wbuf, nb, h->nsm, st);
+  }
+  return e;
 }
 
 }  // namespace
@@ -1022,7 +1169,7 @@ amrs_status amrs_rhs_vjp_box(amrs_handle* h, const amrs_box* bx, const double dx
                              amrs_array4 vbar, amrs_array4 ubar, double* param_bar, void* stream) {
   if (!h || !bx || !dxinv) return AMRS_ERR_NULL;
   if (!box_ok(*bx)) return AMRS_ERR_BOX;
-  if (!fused_path(h->sc)) return AMRS_ERR_SCHEME;
+  if (!vjp_scheme(h->sc)) return AMRS_ERR_SCHEME;
   if (!covers(state, *bx, NGHOST, NCONS) || !covers(vbar, *bx, 0, NCONS) || !covers(ubar, *bx, NGHOST, NCONS))
     return AMRS_ERR_LAYOUT;
   std::lock_guard<std::mutex> lk(h->mu);
@@ -1035,8 +1182,7 @@ amrs_status amrs_rhs_vjp_box(amrs_handle* h, const amrs_box* bx, const double dx
   if (amrs_status s = adj_prepare(h, *bx, S, st)) { ring_release(h, st); return s; }
   S.ah.vbar = to_darr(vbar);
   S.ah.ubar = to_darr(ubar);
-  cudaError_t e = launch_prims(L.tb, 0, L.tot_p, h->nsm, st);
-  if (e == cudaSuccess) e = launch_rhs_vjp(h->sc.order_keep, L.tb, S.ah, param_bar, h->nsm, st);
+  cudaError_t e = rhs_vjp_launch(h, L, *bx, S, param_bar, st);
   ring_release(h, st);
   if (e != cudaSuccess) return cuda_fail(e, "amrs_rhs_vjp_box");
   return AMRS_OK;
@@ -1072,7 +1218,7 @@ amrs_status amrs_rk_stage_vjp_box(amrs_handle* h, const amrs_box* bx, const doub
                                   double* param_bar, void* stream) {
   if (!h || !bx || !dxinv || !prog || !bc_lo || !bc_hi) return AMRS_ERR_NULL;
   if (!box_ok(*bx)) return AMRS_ERR_BOX;
-  if (!fused_path(h->sc)) return AMRS_ERR_SCHEME;
+  if (!vjp_scheme(h->sc)) return AMRS_ERR_SCHEME;
   if (!covers(stage_in, *bx, NGHOST, NCONS) || !covers(wbar, *bx, 0, NCONS) || !covers(s1bar, *bx, 0, NCONS) ||
       !covers(inbar, *bx, 0, NCONS))
     return AMRS_ERR_LAYOUT;
@@ -1093,8 +1239,7 @@ amrs_status amrs_rk_stage_vjp_box(amrs_handle* h, const amrs_box* bx, const doub
     S.ah.vbar = S.vbar_tmp;
     S.ah.ubar = S.ubar_tmp;
     List& L = *h->one;
-    cudaError_t e = launch_prims(L.tb, 0, L.tot_p, h->nsm, st);
-    if (e == cudaSuccess) e = launch_rhs_vjp(h->sc.order_keep, L.tb, S.ah, param_bar, h->nsm, st);
+    cudaError_t e = rhs_vjp_launch(h, L, *bx, S, param_bar, st);
     ring_release(h, st);
     if (e != cudaSuccess) return cuda_fail(e, "amrs_rk_stage_vjp_box");
   }
@@ -1173,35 +1318,54 @@ amrs_status amrs_profile_stage_box(amrs_handle* h, const amrs_box* bx, const dou
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (amrs_status s = one_box(h, bx, dxinv, slots, 3, st)) return s;
   List& L = *h->one;
-  if (!L.fused) { ring_release(h, st); return AMRS_ERR_SCHEME; }
+  const amrs_scheme& sc = L.sc;
+  // the face-array path is profiled for WENO5 (point fluxes timed with the
+  // primitives) and the unshared KEEP baseline
+  const bool plain_ok = sc.rhs_euler && !sc.art_diss && (sc.flux_euler == 1 || sc.flux_euler == 2);
+  if (!L.fused && !plain_ok) { ring_release(h, st); return AMRS_ERR_SCHEME; }
   const DProg p = to_dprog(prog);
-  cudaEvent_t ev[4];
-  for (int i = 0; i < 4; ++i) CK(cudaEventCreate(&ev[i]));
-  double acc[3] = {0, 0, 0};
+  cudaEvent_t ev[5];
+  for (int i = 0; i < 5; ++i) CK(cudaEventCreate(&ev[i]));
+  double acc[4] = {0, 0, 0, 0};
+  long long nf[3] = {L.tot_f[0], L.tot_f[1], L.tot_f[2]};
   amrs_status rs = AMRS_OK;
   for (int r = 0; r < reps && rs == AMRS_OK; ++r) {
     cudaError_t e = cudaEventRecord(ev[0], st);
     if (e == cudaSuccess) e = launch_prims(L.tb, 0, L.tot_p, h->nsm, st);
+    if (e == cudaSuccess && !L.fused && sc.flux_euler == 2) e = launch_weno_point(L.tb, L.ft, 0, L.tot_g, h->nsm, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
-    if (e == cudaSuccess && L.sc.rhs_visc) e = launch_visc(L.tb, L.tot_v, h->nsm, st);
+    if (e == cudaSuccess && sc.rhs_visc) e = launch_visc(L.tb, L.tot_v, h->nsm, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[2], st);
-    if (e == cudaSuccess)
-      e = launch_keep_face(L.sc.order_keep, L.sc.rhs_visc != 0, L.tb, 0, 1, 2, p, 0, L.tma, h->derr, L.face_grid,
+    if (e == cudaSuccess && L.fused)
+      e = launch_keep_face(sc.order_keep, sc.rhs_visc != 0, L.tb, 0, 1, 2, p, 0, L.tma, h->derr, L.face_grid,
                            h->nsm, st);
+    else if (e == cudaSuccess && sc.flux_euler == 2)
+      e = launch_weno_faces(L.tb, L.ft, 0, nf, sc.weno_fast == 0, h->nsm, st);
+    else if (e == cudaSuccess)
+      e = launch_keep_faces_plain(sc.order_keep, L.tb, L.ft, nf, h->nsm, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[3], st);
-    if (e == cudaSuccess) e = cudaEventSynchronize(ev[3]);
+    if (e == cudaSuccess && !L.fused) {
+      if (sc.rhs_visc) e = launch_visc_face_add(L.tb, L.ft, nf, h->nsm, st);
+      if (e == cudaSuccess) e = launch_div_stage(L.tb, L.ft, 0, 1, 2, p, 0, L.tot_valid, h->nsm, st);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(ev[4], st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[4]);
     for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
       float t = 0.f;
       e = cudaEventElapsedTime(&t, ev[i], ev[i + 1]);
       acc[i] += t;
     }
+    if (e == cudaSuccess) {
+      float t = 0.f;
+      e = cudaEventElapsedTime(&t, ev[0], ev[4]);
+      acc[3] += t;
+    }
     if (e != cudaSuccess) rs = cuda_fail(e, "amrs_profile_stage_box");
   }
-  for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
+  for (int i = 0; i < 5; ++i) cudaEventDestroy(ev[i]);
   ring_release(h, st);
   if (rs) return rs;
-  for (int i = 0; i < 3; ++i) ms[i] = acc[i] / reps;
-  ms[3] = ms[0] + ms[1] + ms[2];
+  for (int i = 0; i < 4; ++i) ms[i] = acc[i] / reps;
   return AMRS_OK;
 }
 

@@ -11,7 +11,10 @@
 // Operation order follows the cited reference functions and the file is
 // built with -fmad=false, so results match the reference's CPU build
 // (WENO5 squares its smoothness terms directly, where the reference calls
-// pow(x, 2); the two can differ in the last bit).
+// pow(x, 2); the two can differ in the last bit).  The default WENO5 face
+// kernel instead forms the nonlinear weights over a common denominator
+// with explicit fused multiply-adds (weno5js_cd): the same function in
+// exact arithmetic, a quarter of the divisions, rounding differences only.
 #include "amrs_kernels.h"
 
 namespace amrs {
@@ -135,27 +138,75 @@ __global__ void __launch_bounds__(256) weno_flux_lambda_kernel(BoxTable tb, Face
 }
 
 // WENO5-JS (src/rhs/High_resolution.h:124-159), beta[1] with the fourth power.
+// Operation order of the reference; a sum x + 2^k*y (power-of-two factor,
+// exact product) is one fma, which rounds exactly like the reference's
+// separate multiply and add.
 __device__ __forceinline__ double weno5js(const double s0, const double s1, const double s2, const double s3,
                                           const double s4) {
   const double eps = 1e-40;
-  const double beta0 = (13.0 / 12.0) * (s0 - 2.0 * s1 + s2) * (s0 - 2.0 * s1 + s2) +
-                       0.25 * (s0 - 4.0 * s1 + 3.0 * s2) * (s0 - 4.0 * s1 + 3.0 * s2);
-  const double beta1 = (13.0 / 12.0) * (s1 - 2.0 * s2 + s3) * (s1 - 2.0 * s2 + s3) +
-                       0.25 * (s1 - s3) * (s1 - s3) * (s1 - s3) * (s1 - s3);
-  const double beta2 = (13.0 / 12.0) * (s2 - 2.0 * s3 + s4) * (s2 - 2.0 * s3 + s4) +
-                       0.25 * (3.0 * s2 - 4.0 * s3 + s4) * (3.0 * s2 - 4.0 * s3 + s4);
+  const double a = fma(-2.0, s1, s0) + s2;         // s0 - 2 s1 + s2
+  const double b = fma(-4.0, s1, s0) + 3.0 * s2;   // s0 - 4 s1 + 3 s2
+  const double c = fma(-2.0, s2, s1) + s3;         // s1 - 2 s2 + s3
+  const double g = s1 - s3;
+  const double d = fma(-2.0, s3, s2) + s4;         // s2 - 2 s3 + s4
+  const double f = fma(-4.0, s3, 3.0 * s2) + s4;   // 3 s2 - 4 s3 + s4
+  const double beta0 = (13.0 / 12.0) * a * a + 0.25 * b * b;
+  const double beta1 = (13.0 / 12.0) * c * c + 0.25 * g * g * g * g;
+  const double beta2 = (13.0 / 12.0) * d * d + 0.25 * f * f;
   const double e0 = eps + beta0, e1 = eps + beta1, e2 = eps + beta2;
   const double alpha0 = 0.1 / (e0 * e0);
   const double alpha1 = 0.6 / (e1 * e1);
   const double alpha2 = 0.3 / (e2 * e2);
   const double sum = 1.0 / (alpha0 + alpha1 + alpha2);
-  const double vl0 = 2.0 * s0 - 7.0 * s1 + 11.0 * s2;
-  const double vl1 = -s1 + 5.0 * s2 + 2.0 * s3;
-  const double vl2 = 2.0 * s2 + 5.0 * s3 - s4;
+  const double vl0 = fma(2.0, s0, -(7.0 * s1)) + 11.0 * s2;  // 2 s0 - 7 s1 + 11 s2
+  const double vl1 = fma(2.0, s3, -s1 + 5.0 * s2);          // -s1 + 5 s2 + 2 s3
+  const double vl2 = fma(2.0, s2, 5.0 * s3) - s4;           // 2 s2 + 5 s3 - s4
   return (1.0 / 6.0) * sum * (alpha0 * vl0 + alpha1 * vl1 + alpha2 * vl2);
 }
 
+// The same reconstruction with its weights over a common denominator, for
+// inputs t = 2s (the LLF halves are folded into the caller):
+//   w_k = a_k / (a0+a1+a2),  a_k = c_k / e_k^2,  e_k = beta_k + eps
+//   sum_k w_k v_k / 6 = (sum_k c_k v_k P_k) / (6 sum_k c_k P_k),  P_k = prod_{j!=k} e_j^2.
+// 4 beta(s) is evaluated from t and eps becomes 4 eps, so the weights are
+// unchanged in exact arithmetic; the 1/6 and the final 1/2 go into the v_k coefficients.
+// One division instead of four; every product and sum is a fused
+// multiply-add where one fits.  Range: the products P_k stay finite for
+// |t| up to about 1e38 and normal for eps = 4e-40 (P_k >= 2.6e-158).
+__device__ __forceinline__ double weno5js_cd(const double t0, const double t1, const double t2, const double t3,
+                                             const double t4) {
+  constexpr double eps4 = 4e-40;
+  constexpr double c1312 = 13.0 / 12.0;
+  // beta_0: (13/12) d1^2 + (1/4) d2^2
+  const double d1 = fma(-2.0, t1, t0) + t2;
+  const double d2 = fma(3.0, t2, fma(-4.0, t1, t0));
+  const double e0 = fma(c1312 * d1, d1, fma(0.25 * d2, d2, eps4));
+  // beta_1: (13/12) d3^2 + (1/4) (s1 - s3)^4; its fourth-power term is not
+  // homogeneous of degree 2, so in t = 2s: 4 beta_1 = (13/12) d3^2 + (1/16) g^4
+  const double d3 = fma(-2.0, t2, t1) + t3;
+  const double g = t1 - t3;
+  const double g2 = g * g;
+  const double e1 = fma(c1312 * d3, d3, fma(0.0625 * g2, g2, eps4));
+  // beta_2: (13/12) d4^2 + (1/4) d5^2
+  const double d4 = fma(-2.0, t3, t2) + t4;
+  const double d5 = fma(-4.0, t3, fma(3.0, t2, t4));
+  const double e2 = fma(c1312 * d4, d4, fma(0.25 * d5, d5, eps4));
+  const double E0 = e0 * e0, E1 = e1 * e1, E2 = e2 * e2;
+  const double P0 = E1 * E2, P1 = E0 * E2, P2 = E0 * E1;
+  const double den = fma(0.1, P0, fma(0.6, P1, 0.3 * P2));
+  // c_k v_k / 12 with v0 = 2t0 - 7t1 + 11t2, v1 = -t1 + 5t2 + 2t3, v2 = 2t2 + 5t3 - t4
+  constexpr double k0 = 0.1 / 12.0, k1 = 0.6 / 12.0, k2 = 0.3 / 12.0;
+  const double v0 = fma(11.0 * k0, t2, fma(-7.0 * k0, t1, (2.0 * k0) * t0));
+  const double v1 = fma(2.0 * k1, t3, fma(5.0 * k1, t2, -k1 * t1));
+  const double v2 = fma(-k2, t4, fma(5.0 * k2, t3, (2.0 * k2) * t2));
+  const double num = fma(v0, P0, fma(v1, P1, v2 * P2));
+  return num / den;
+}
+
 // LLF-split WENO face flux for all components (src/rhs/High_resolution.h:162-246).
+// REF_ORDER: the reference's operation order; otherwise the split halves
+// 0.5 (f +- alpha U) enter weno5js_cd doubled as fma(+-alpha, U, f).
+template <bool REF_ORDER>
 __global__ void __launch_bounds__(256) weno_face_kernel(BoxTable tb, FaceTable ft, int s_in, long long total) {
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
        g += (long long)gridDim.x * blockDim.x) {
@@ -169,26 +220,56 @@ __global__ void __launch_bounds__(256) weno_face_kernel(BoxTable tb, FaceTable f
     const long long st = (f.d == 0) ? 1 : (f.d == 1 ? L.js : L.ks);
     const long long su = (f.d == 0) ? 1 : (f.d == 1 ? U.js : U.ks);
     const long long ol = L.off(f.i, f.j, f.k) + f.d * L.ns;
-    double me = rmax(L.p[ol - 3 * st], L.p[ol - 2 * st]);
-    me = rmax(me, L.p[ol - st]);
-    me = rmax(me, L.p[ol]);
-    me = rmax(me, L.p[ol + st]);
-    me = rmax(me, L.p[ol + 2 * st]);
+    double me;
+    if (REF_ORDER) {
+      me = rmax(L.p[ol - 3 * st], L.p[ol - 2 * st]);
+      me = rmax(me, L.p[ol - st]);
+      me = rmax(me, L.p[ol]);
+      me = rmax(me, L.p[ol + st]);
+      me = rmax(me, L.p[ol + 2 * st]);
+    } else {
+      // lambda >= 0: the integer order of the bit patterns is the order of
+      // the values, and the maximum needs no FP64 instruction
+      long long m = __double_as_longlong(L.p[ol - 3 * st]);
+#pragma unroll
+      for (int q = -2; q <= 2; ++q) m = max(m, __double_as_longlong(L.p[ol + q * st]));
+      me = __longlong_as_double(m);
+    }
     const long long ou = U.off(f.i, f.j, f.k), opf = PF.off(f.i, f.j, f.k);
     const DArr Fd = FR.f[f.d];
     const long long of = Fd.off(f.i, f.j, f.k);
-    for (int n = 0; n < 5; ++n) {
-      double df[6], p[6];
+    if (!REF_ORDER) {
+#pragma unroll 1
+      for (int n = 0; n < 5; ++n) {
+        double u[6], p[6];
 #pragma unroll
-      for (int q = 0; q < 6; ++q) {
-        df[q] = me * U.p[ou + (q - 3) * su + n * U.ns];
-        p[q] = PF.p[opf + (q - 3) * su + n * PF.ns];
+        for (int q = 0; q < 6; ++q) {
+          u[q] = U.p[ou + (q - 3) * su + n * U.ns];
+          p[q] = PF.p[opf + (q - 3) * su + n * PF.ns];
+        }
+        const double flx = weno5js_cd(fma(me, u[0], p[0]), fma(me, u[1], p[1]), fma(me, u[2], p[2]),
+                                      fma(me, u[3], p[3]), fma(me, u[4], p[4])) +
+                           weno5js_cd(fma(-me, u[5], p[5]), fma(-me, u[4], p[4]), fma(-me, u[3], p[3]),
+                                      fma(-me, u[2], p[2]), fma(-me, u[1], p[1]));
+        Fd.p[of + n * Fd.ns] = flx;
       }
-      double flx = weno5js(0.5 * (p[0] + df[0]), 0.5 * (p[1] + df[1]), 0.5 * (p[2] + df[2]), 0.5 * (p[3] + df[3]),
-                           0.5 * (p[4] + df[4]));
-      flx += weno5js(0.5 * (p[5] - df[5]), 0.5 * (p[4] - df[4]), 0.5 * (p[3] - df[3]), 0.5 * (p[2] - df[2]),
-                     0.5 * (p[1] - df[1]));
-      Fd.p[of + n * Fd.ns] = flx;
+    } else {
+      // 0.5*(p + me*U) == fma(0.5, p, (0.5*me)*U): halving is exact, so the
+      // split stencils round exactly as in the reference (normal range)
+      const double hme = 0.5 * me;
+      for (int n = 0; n < 5; ++n) {
+        double h[6], p[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+          h[q] = hme * U.p[ou + (q - 3) * su + n * U.ns];
+          p[q] = PF.p[opf + (q - 3) * su + n * PF.ns];
+        }
+        double flx = weno5js(fma(0.5, p[0], h[0]), fma(0.5, p[1], h[1]), fma(0.5, p[2], h[2]),
+                             fma(0.5, p[3], h[3]), fma(0.5, p[4], h[4]));
+        flx += weno5js(fma(0.5, p[5], -h[5]), fma(0.5, p[4], -h[4]), fma(0.5, p[3], -h[3]),
+                       fma(0.5, p[2], -h[2]), fma(0.5, p[1], -h[1]));
+        Fd.p[of + n * Fd.ns] = flx;
+      }
     }
   }
 }
@@ -518,11 +599,24 @@ cudaError_t launch_keep_faces_plain(int order, const BoxTable& tb, const FaceTab
   return cudaGetLastError();
 }
 
-cudaError_t launch_weno(const BoxTable& tb, const FaceTable& ft, int s_in, long long ngcells, long long nfaces[3],
-                        int nsm, cudaStream_t st) {
+cudaError_t launch_weno_point(const BoxTable& tb, const FaceTable& ft, int s_in, long long ngcells, int nsm,
+                              cudaStream_t st) {
   weno_flux_lambda_kernel<<<grid_for(ngcells, nsm), 256, 0, st>>>(tb, ft, s_in, ngcells);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_weno_faces(const BoxTable& tb, const FaceTable& ft, int s_in, long long nfaces[3], bool ref_order,
+                              int nsm, cudaStream_t st) {
   const long long tot = nfaces[0] + nfaces[1] + nfaces[2];
-  weno_face_kernel<<<grid_for(tot, nsm), 256, 0, st>>>(tb, ft, s_in, tot);
+  if (ref_order) weno_face_kernel<true><<<grid_for(tot, nsm), 256, 0, st>>>(tb, ft, s_in, tot);
+  else weno_face_kernel<false><<<grid_for(tot, nsm), 256, 0, st>>>(tb, ft, s_in, tot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_weno(const BoxTable& tb, const FaceTable& ft, int s_in, long long ngcells, long long nfaces[3],
+                        bool ref_order, int nsm, cudaStream_t st) {
+  weno_flux_lambda_kernel<<<grid_for(ngcells, nsm), 256, 0, st>>>(tb, ft, s_in, ngcells);
+  launch_weno_faces(tb, ft, s_in, nfaces, ref_order, nsm, st);
   return cudaGetLastError();
 }
 

@@ -86,6 +86,51 @@ __global__ void __launch_bounds__(256) halo_list_kernel(BoxTable tb, const long 
   }
 }
 
+// Single-level FillPatch of a level whose boxes tile the domain: a ghost
+// cell of box b maps to a cell of the domain exactly as in halo_kernel
+// (periodic images, physical BCs) and takes that cell's value from the box
+// that owns it (owner table built on the host, one entry per cell of every
+// grow(box,3), in the gpre order).  Sources are valid cells only, so the
+// fill has no order dependence between boxes and is bit-identical to the
+// fill of one box covering the domain.
+__global__ void __launch_bounds__(256) halo_level_kernel(BoxTable tb, const long long* gpre, const int* owner,
+                                                         int slot, LevelDomain dom) {
+  const long long total = gpre[tb.n];
+  const int g = NGHOST;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < total;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int src = owner[c];
+    if (src < 0) continue;  // a valid cell
+    const int b = find_box_ll(gpre, tb.n, c);
+    const BoxRec& R = tb.box[b];
+    const int l = (int)(c - gpre[b]);
+    const int nx = R.hi[0] - R.lo[0] + 1 + 2 * g, ny = R.hi[1] - R.lo[1] + 1 + 2 * g;
+    const int i = l % nx + R.lo[0] - g;
+    const int t = l / nx;
+    const int j = t % ny + R.lo[1] - g;
+    const int k = t / ny + R.lo[2] - g;
+    const DArr U = R.slot[slot];
+    const DArr S = tb.box[src].slot[slot];
+    for (int n = 0; n < NCONS; ++n) {
+      bool flip = false;
+      const int si = map_coord(i, dom.lo[0], dom.hi[0], dom.bc_lo[0], dom.bc_hi[0], n, 0, flip);
+      const int sj = map_coord(j, dom.lo[1], dom.hi[1], dom.bc_lo[1], dom.bc_hi[1], n, 1, flip);
+      const int sk = map_coord(k, dom.lo[2], dom.hi[2], dom.bc_lo[2], dom.bc_hi[2], n, 2, flip);
+      const double v = S(si, sj, sk, n);
+      U(i, j, k, n) = flip ? -v : v;
+    }
+  }
+}
+
+cudaError_t launch_halo_level(const BoxTable& tb, const long long* gpre, const int* owner, long long total, int slot,
+                              const LevelDomain& dom, int nsm, cudaStream_t st) {
+  long long blocks = (total + 255) / 256;
+  if (blocks > (long long)nsm * 8) blocks = (long long)nsm * 8;
+  if (blocks < 1) blocks = 1;
+  halo_level_kernel<<<(int)blocks, 256, 0, st>>>(tb, gpre, owner, slot, dom);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_halo_list(const BoxTable& tb, const long long* gpre, long long total, int slot, const int bc_lo[3],
                              const int bc_hi[3], int nsm, cudaStream_t st) {
   long long blocks = (total + 255) / 256;

@@ -68,12 +68,18 @@ class Closures:
 
 @dataclasses.dataclass
 class Scheme:
-    """cns.* switches: flux_euler 0 = MUSCL/Riemann, 1 = KEEP, 2 = WENO5-JS LLF."""
+    """cns.* switches: flux_euler 0 = MUSCL/Riemann, 1 = KEEP, 2 = WENO5-JS LLF.
+
+    weno_fast (not a reference switch): 0 (default) evaluates WENO5 in the
+    reference's operation order (bit-identical results); 1 forms the weights
+    over a common denominator (faster, rounding differences only).
+    """
     rhs_euler: int = 1
     rhs_visc: int = 1
     flux_euler: int = 1
     order_keep: int = 4
     art_diss: int = 0
+    weno_fast: int = 0
 
 
 @dataclasses.dataclass

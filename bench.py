@@ -13,6 +13,11 @@ Also reported on the same JSON line:
             the oracle's operation counts;
   batched   512 uneven boxes, one SSPRK3 step: one persistent launch per
             kernel kind captured in a CUDA graph vs per-box launches;
+  ensemble  64 periodic TGV members of 48^3 with per-member closures;
+  adjoint   TGV 64^3: VJP of one SSPRK3 step against the forward step;
+  large     256^3 random-phase turbulence, WENO5-LLF + viscous: 20 SSPRK3
+            steps and the adjoint of the final step, with the roofline
+            fraction of the whole step;
   cpu_baseline  the CPU oracle on the host cores (bounded sample).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
@@ -37,6 +42,21 @@ sys.path.insert(0, ROOT)
 METRIC = "cell-updates/s per RK3 step"
 UNIT = "cell-updates/s"
 WORKLOAD = "Taylor-Green vortex 128^3 periodic, M=0.1 Re=1600 Pr=0.71, KEEP4 + viscous, SSPRK3"
+
+# --scheme: (switches, op-count key, dominant kernel, its ncu summary, kernels of ours per stage, label)
+SCHEMES = {
+    "keep4": (dict(flux_euler=1, order_keep=4, rhs_visc=1), "keep4_visc", "keep_face_kernel<4,true>",
+              "keep_face_kernel_tgv96.md", 4, "KEEP4 + viscous"),
+    "weno": (dict(flux_euler=2, rhs_visc=1), "weno_visc", "weno_face_kernel<true> (reference operation order)",
+             "weno_face_kernel_tgv96.md", 7, "WENO5-LLF + viscous, reference operation order"),
+    "weno_fast": (dict(flux_euler=2, rhs_visc=1, weno_fast=1), "weno_visc",
+                  "weno_face_kernel<false> (common-denominator weights)", "weno_fast_face_kernel_tgv96.md", 7,
+                  "WENO5-LLF + viscous, common-denominator weights"),
+}
+
+
+def workload_name(scheme, n):
+    return "Taylor-Green vortex %d^3 periodic, M=0.1 Re=1600 Pr=0.71, %s, SSPRK3" % (n, SCHEMES[scheme][5])
 
 
 # --------------------------------------------------------------- helpers --
@@ -99,22 +119,40 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def face_kernel_flops(orc, scheme, closures, n, prog_flops_per_comp):
+OP_COUNTS = os.path.join(ROOT, "tests", "golden", "op_counts.json")
+
+
+def rhs_phase_flops(scheme_name, n):
+    """Algorithmic flops per phase of one RHS over an n^3 box: the oracle's
+    operation counts (+,-,*,/,sqrt each 1; no FMA in the oracle) as exact
+    cubics in n, committed in tests/golden/op_counts.json by
+    tests/golden/make_op_counts.py."""
+    phases = json.load(open(OP_COUNTS))["schemes"][scheme_name]["phases"]
+    return {ph: c[0] * n ** 3 + c[1] * n ** 2 + c[2] * n + c[3] for ph, c in phases.items()}
+
+
+def face_kernel_flops(scheme_name, n, prog_flops_per_comp):
     """Algorithmic FP64 flops of one fused face-kernel launch over an n^3 box:
-    the oracle's operation counts (+,-,*,/,sqrt each 1; no FMA in the oracle)
-    of the Euler face fluxes, viscous face averages and divergence, per face
-    and per cell, scaled to the box, plus the stage program."""
-    from amrsolver_gb300 import problems as P
-    m = 16
-    U, dx = P.tgv(m)
-    per = orc.rhs_counts(scheme, closures, U, [1.0 / h for h in dx], per_phase=True)
-    f = lambda d: d["add"] + d["mul"] + d["div"] + d["sqrt"]
-    faces_m = 3 * (m + 1) * m * m
-    faces_n = 3 * (n + 1) * n * n
-    per_face = (f(per["euler_faces"]) + f(per["visc_faces"])) / faces_m
-    per_cell_div = f(per["divergence"]) / m ** 3
-    total = per_face * faces_n + (per_cell_div + 5 * prog_flops_per_comp) * n ** 3
+    Euler face fluxes, viscous face averages and divergence, plus the stage
+    program."""
+    per = rhs_phase_flops(scheme_name, n)
+    total = per["euler_faces"] + per["visc_faces"] + per["divergence"] + 5 * prog_flops_per_comp * n ** 3
     return total, per
+
+
+def weno_face_flops(scheme_name, n):
+    """Flops of the WENO5 face kernel alone: the Euler phase minus its
+    per-cell point fluxes (cons2eulerflux_lambda over grow(box,3), whose
+    count is the constant term of the phase's cubic divided by 6^3)."""
+    c = json.load(open(OP_COUNTS))["schemes"][scheme_name]["phases"]["euler_faces"]
+    per_point = c[3] // 216
+    return c[0] * n ** 3 + c[1] * n ** 2 + c[2] * n + c[3] - per_point * (n + 6) ** 3
+
+
+def prog_flops(progs):
+    """FP64 flops per component of the stage programs (LinComb 3, Saxpy 2,
+    Xpay 2, Copy 0)."""
+    return sum({0: 3, 1: 2, 2: 2, 3: 0}[p.ops[o].kind] for p in progs for o in range(p.nops))
 
 
 # ----------------------------------------------------------- reference arm --
@@ -303,6 +341,117 @@ def bench_adjoint(torch, P, steps=3):
             "forward_keeping_stages_ms": fwd_save, "adjoint_ms": adj, "adjoint_over_forward": adj / fwd}
 
 
+def bench_level(torch, capi, P, n=128, box=32, steps=10, warmup=3):
+    """TGV n^3 as the reference runs it: a level of (n/box)^3 boxes of box^3
+    cells whose ghosts come from their neighbours (single-level FillPatch
+    across the level, periodic images included), one CUDA graph per SSPRK3
+    step; the same number of cell updates as the single-box headline."""
+    U, dx = P.tgv(n)
+    cl = P.Closures.nondimensional(1.0 / 1600.0)
+    h = capi.Handle(P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1), cl)
+    g = P.NGHOST
+    los, slots = [], []
+    m = n // box
+    for kz in range(m):
+        for ky in range(m):
+            for kx in range(m):
+                B = U[:, kz * box:kz * box + box + 2 * g, ky * box:ky * box + box + 2 * g,
+                      kx * box:kx * box + box + 2 * g]
+                t = torch.from_numpy(np.ascontiguousarray(B)).cuda()
+                slots.append([t, torch.empty_like(t), torch.empty_like(t)])
+                los.append((kx * box, ky * box, kz * box))
+    bl = capi.BoxList(h, los, slots, [1.0 / v for v in dx])
+    bl.set_domain((0, 0, 0), (n, n, n), (-1, -1, -1), (-1, -1, -1))
+    dt = 1e-3
+    for _ in range(warmup):
+        r = bl.step(3, 3, dt, 0, 1, 2, use_graph=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        # the same graph every step: result slot copied back is not needed for timing
+        r = bl.step(3, 3, dt, 0, 1, 2, use_graph=True)
+    e1.record()
+    torch.cuda.synchronize()
+    h.sync_check()
+    ms = e0.elapsed_time(e1) / steps
+    return {"workload": "TGV %d^3 as %d boxes of %d^3, ghosts from neighbours (level FillPatch in the graph), "
+                        "KEEP4 + viscous, one SSPRK3 step" % (n, m ** 3, box),
+            "ms_per_step": ms, "cell_updates_per_s": n ** 3 / (ms * 1e-3), "result_slot": r}
+
+
+def bench_large(torch, capi, P, peak, n=256, steps=20):
+    """Periodic 256^3 random-phase turbulence (E(k) ~ k^4 exp(-2 (k/4)^2),
+    turbulent Mach 0.6, rho = 1, p = 1/gamma), mu = 1e-4, Pr = 0.71, WENO5-LLF +
+    viscous, SSPRK3 at a fixed dt (CFL 0.3 of the initial state): 20 steps,
+    then the adjoint of the final step (cotangent: gradient of the mean
+    kinetic energy).  Both WENO5 weight evaluations: the reference's
+    operation order (bit-identical) and the common-denominator form."""
+    import gc
+    from amrsolver_gb300 import adjoint, cns
+    U, dx = P.random_turbulence(n, mach_t=0.6)
+    cl = P.Closures.nondimensional(1e-4)
+    per = rhs_phase_flops("weno_visc", n)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    res = {"workload": "periodic %d^3 random-phase turbulence (Mt=0.6, E(k)~k^4 exp(-2(k/4)^2)), mu=1e-4, "
+                       "Pr=0.71, WENO5-LLF + viscous, SSPRK3: %d steps then the adjoint of the final step"
+                       % (n, steps),
+           "cells": n ** 3, "algorithmic_flops_per_rhs": sum(per.values()), "dt": None}
+    dt = None
+    for fast in (0, 1):
+        lev = cns.CNSLevel(P.Scheme(flux_euler=2, rhs_visc=1, weno_fast=fast), cl, U, dx)
+        if dt is None:
+            dt = lev.est_time_step(0.3)
+            res["dt"] = dt
+        progs = capi.rk_program(3, 3, dt)
+        flops_step = 3 * sum(per.values()) + 5 * prog_flops(progs) * n ** 3
+        # one untimed warm-up step, then restart from the initial state
+        lev.advance(lev.time, dt)
+        lev.bufs[lev.cur].copy_(torch.from_numpy(U))
+        lev.time = 0.0
+        tot0 = lev.totals()
+        torch.cuda.synchronize()
+        e0, e1, e2, e3 = ev(), ev(), ev(), ev()
+        e0.record()
+        for _ in range(steps - 1):
+            lev.advance(lev.time, dt)
+        e1.record()
+        S_last = lev.S.clone()
+        e2.record()
+        lev.advance(lev.time, dt)
+        e3.record()
+        torch.cuda.synchronize()
+        ms_fwd = (e0.elapsed_time(e1) + e2.elapsed_time(e3)) / steps
+        tot1 = lev.totals()
+        final = lev.valid().clone()
+        wbar = adjoint.kinetic_energy_grad(final)
+        f0, f1, f2 = ev(), ev(), ev()
+        f0.record()
+        stages, out = adjoint._forward_step(lev, S_last, dt)
+        f1.record()
+        ubar, _ = adjoint._step_vjp(lev, stages, dt, wbar)
+        f2.record()
+        torch.cuda.synchronize()
+        lev.h.sync_check()
+        same = bool(torch.equal(out[:, 3:-3, 3:-3, 3:-3], final))
+        # periodic box: totals change by round-off only (relative to sum |U_n|)
+        scale = (lev.valid().abs().reshape(5, -1).sum(dim=1) * (2 * math.pi) ** 3).cpu().numpy()
+        cons = max(abs(float(a) - float(b)) / float(c) for a, b, c in zip(tot0, tot1, scale))
+        achieved = flops_step / (ms_fwd * 1e-3) / 1e12
+        res["weno_fast" if fast else "weno_reference_order"] = {
+            "ms_per_step": ms_fwd, "cell_updates_per_s": n ** 3 / (ms_fwd * 1e-3),
+            "achieved_tflops_algorithmic": achieved, "frac_of_measured_fp64_peak": achieved / peak,
+            "forward_step_keeping_stages_ms": f0.elapsed_time(f1), "adjoint_step_ms": f1.elapsed_time(f2),
+            "adjoint_over_forward": f1.elapsed_time(f2) / ms_fwd,
+            "recomputed_final_step_bit_identical": same,
+            "conserved_totals_max_rel_change": cons,
+            "ubar_norm": float(torch.linalg.vector_norm(ubar))}
+        del lev, stages, out, S_last, final, wbar, ubar
+        gc.collect()
+        torch.cuda.empty_cache()
+    return res
+
+
 def run_gpu(args, rank, world, local):
     import torch
     from amrsolver_gb300 import capi, cns
@@ -312,7 +461,7 @@ def run_gpu(args, rank, world, local):
     n = args.n
     U, dx = P.tgv(n)
     cl = P.Closures.nondimensional(1.0 / 1600.0)
-    sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1)
+    sc = P.Scheme(**SCHEMES[args.scheme][0])
     dt = 1e-3
     lev = cns.CNSLevel(sc, cl, U, dx, device=local)
     stream = torch.cuda.current_stream()
@@ -369,11 +518,16 @@ def run_gpu(args, rank, world, local):
     result = None
     if rank == 0:
         # ---- dominant kernel: fused face kernel, timed alone on the stream
-        from oracle import pyoracle
-        orc = pyoracle.oracle()
         progs = capi.rk_program(3, 3, dt)
         # stage 2 program: Xpay (2 flops) + LinComb (3 flops) per component
-        face_flops, per = face_kernel_flops(orc, sc, cl, n, 5)
+        spec = SCHEMES[args.scheme]
+        if args.scheme == "keep4":
+            face_flops, per = face_kernel_flops(spec[1], n, prog_flops(progs[1:2]))
+            algo_bytes_face = n ** 3 * (3 * 40)  # reads U_s, U^n, writes U_{s+1}: 120 B/cell
+        else:
+            face_flops = weno_face_flops(spec[1], n)
+            # reads U (40), point fluxes (120) and lambda (24) per cell, writes 3 x 5 face values
+            algo_bytes_face = n ** 3 * (40 + 120 + 24) + 3 * (n + 1) * n * n * 40
         peak = lev.h.probe_fp64_tflops()
         S0 = lev.S
         out = torch.empty_like(S0)
@@ -386,7 +540,7 @@ def run_gpu(args, rank, world, local):
         tf = kms[2]
         achieved = face_flops / (tf * 1e-3) / 1e12
         roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                    "traffic": None, "kernel": "keep_face_kernel<4,true>",
+                    "traffic": None, "kernel": spec[2],
                     "peak_source": "measured: DFMA-chain probe kernel (amrs_probe_fp64_tflops), FMA = 2 flops",
                     "algorithmic_flops_per_launch": face_flops, "ms_per_launch": tf,
                     "stage_kernel_ms": {"prims": kms[0], "visc_cells": kms[1], "faces": kms[2]},
@@ -396,9 +550,8 @@ def run_gpu(args, rank, world, local):
             roofline["hbm_peak_gbs_measured"] = mp.get("hbm_gbs")
         except Exception:
             pass
-        algo_bytes_face = n ** 3 * (3 * 40)  # reads U_s, U^n, writes U_{s+1}: 120 B/cell
         roofline["hbm_achieved_gbs_algorithmic"] = algo_bytes_face / (tf * 1e-3) / 1e9
-        prof = os.path.join(ROOT, "profiles", "keep_face_kernel_tgv96.md")
+        prof = os.path.join(ROOT, "profiles", spec[3])
         t96 = read_traffic(prof)
         # traffic grows with the cells processed: scale the 96^3 capture to this box
         roofline["traffic"] = None if t96 is None else t96 * (n ** 3) / 96 ** 3
@@ -406,19 +559,23 @@ def run_gpu(args, rank, world, local):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_all, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "cells": n ** 3, "l2": "inputs larger than L2 (3 ghosted states + "
-                       "scratch ~0.7 GB)", "parallelism": "replicas" if world > 1 else "single GPU",
+            "config": {"workload": workload_name(args.scheme, n), "cells": n ** 3,
+                       "l2": "inputs larger than L2 (3 ghosted states + scratch, %.2f GB of states alone)"
+                       % (3 * U.nbytes / 1e9), "parallelism": "replicas" if world > 1 else "single GPU",
                        "tma": lev.h.tma_enabled()},
             "e2e": {"value": world * n ** 3 / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes},
             "roofline": roofline,
-            "gpu_launches": args.steps * 3 * 4,
+            "gpu_launches": args.steps * 3 * spec[4],
             "clocks": clk,
         }
         if not args.skip_batched:
             result["batched"] = bench_batched(torch, capi, P)
             result["ensemble"] = bench_ensemble(torch, capi, P)
             result["adjoint"] = bench_adjoint(torch, P)
+            result["level"] = bench_level(torch, capi, P, n=n)
+        if not args.skip_large:
+            result["large"] = bench_large(torch, capi, P, peak)
         if not args.skip_cpu:
             result["cpu_baseline"] = cpu_baseline_sample()
     return result
@@ -441,6 +598,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--skip-large", action="store_true", help="skip the 256^3 WENO5 + viscous section")
+    ap.add_argument("--scheme", default="keep4", choices=sorted(SCHEMES),
+                    help="scheme of the TGV line (keep4 is the headline; weno* for profiling the WENO path)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=128, help="TGV box edge (128 for the headline; smaller for profiling)")
     args = ap.parse_args()

@@ -68,6 +68,15 @@ typedef struct amrs_closures {
  * (src/rhs/High_resolution.h).  order_keep: 2, 4 or 6.  art_diss: JST. */
 typedef struct amrs_scheme {
   int32_t rhs_euler, rhs_visc, flux_euler, order_keep, art_diss;
+  /* WENO5 only (no counterpart in the reference's switches).  0: the
+   * reference's operation order (src/rhs/High_resolution.h:124-159),
+   * bit-identical to its CPU build.  1: each reconstruction forms its three
+   * nonlinear weights over a common denominator with fused multiply-adds
+   * (one division instead of four, about 1.7x faster): the same function in
+   * exact arithmetic, rounding differences only, which the flux
+   * differencing amplifies where the RHS is small next to the split fluxes
+   * (near-incompressible flow: up to ~1e-9 relative on the mass RHS). */
+  int32_t weno_fast;
 } amrs_scheme;
 
 /* Cell-centred index box, inclusive bounds (amrex::Box). */
@@ -188,8 +197,21 @@ amrs_status amrs_boxlist_set_tile(amrs_boxlist* bl, int32_t nx, int32_t ny, int3
  * fills each stage input's ghosts before its RHS (one launch for all boxes).
  * NULL codes switch the fill off (ghosts kept as the caller set them). */
 amrs_status amrs_boxlist_set_bc(amrs_boxlist* bl, const int32_t bc_lo[3], const int32_t bc_hi[3]);
+/* The boxes of the list form one level tiling (part of) `domain`:
+ * single-level FillPatch as the reference's stages call it
+ * (src/tim/CNS_advance.cpp:54-161 with the BC mapping of
+ * src/set/CNS_setup.cpp:18-31): every ghost cell reads the domain cell
+ * that periodic images or the physical boundary codes map it to, from the
+ * box that owns that cell (neighbour copies inside the domain).  Results
+ * equal those of one box covering the same cells.  Replaces
+ * amrs_boxlist_set_bc; amrs_rk_step_boxlist and amrs_boxlist_fill_halo
+ * then fill the whole level in one launch.  Boxes must be disjoint, inside
+ * `domain`, and cover every cell a ghost reads (AMRS_ERR_BOX otherwise).
+ * Host-synchronising (uploads the owner table). */
+amrs_status amrs_boxlist_set_domain(amrs_boxlist* bl, const amrs_box* domain, const int32_t bc_lo[3],
+                                    const int32_t bc_hi[3]);
 /* Ghost fill of slot `slot` of every box with the codes of
- * amrs_boxlist_set_bc. */
+ * amrs_boxlist_set_bc or the level of amrs_boxlist_set_domain. */
 amrs_status amrs_boxlist_fill_halo(amrs_boxlist* bl, int32_t slot, void* stream);
 
 /* Per-box tiles in one call: tiles[3*b + {0,1,2}] = (tx, ty, kchunk) of
@@ -211,8 +233,10 @@ amrs_status amrs_rk_step_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t sta
 
 /* ---- adjoint ----------------------------------------------------------- */
 
-/* Vector-Jacobian product of one RHS evaluation of one box (KEEP + viscous
- * path; no counterpart in the reference, whose lib/autodiff is absent):
+/* Vector-Jacobian product of one RHS evaluation of one box (KEEP, WENO5
+ * LLF or no Euler flux, each with or without viscous fluxes; JST and MUSCL
+ * Riemann return AMRS_ERR_SCHEME; no counterpart in the reference, whose
+ * lib/autodiff is absent):
  * given the ghost-filled state and a cotangent `vbar` on the valid cells,
  * writes ubar = (d dSdt/d state)^T vbar into `ubar` over the ghosted box
  * (ghost entries hold the sensitivities to ghost values).  `ubar` is
@@ -248,10 +272,11 @@ amrs_status amrs_sync_check(amrs_handle* h, void* stream);
  * by a DFMA-chain kernel: the roofline denominator of this FP64-bound path.
  * Host-synchronising. */
 amrs_status amrs_probe_fp64_tflops(amrs_handle* h, double* tflops);
-/* Per-kernel timing of one RK stage of one box on the fused KEEP path:
- * CUDA events around the primitive, viscous-cell and face kernels on
- * `stream`, averaged over `reps`; ms[0..3] = prims, viscous cells, face
- * kernel, whole stage.  Host-synchronising. */
+/* Per-kernel timing of one RK stage of one box: CUDA events around the
+ * kernels on `stream`, averaged over `reps`.  ms[0] primitives (plus the
+ * WENO5 point fluxes), ms[1] viscous cell fluxes, ms[2] the Euler face
+ * kernel (on the fused KEEP path: faces + viscous averages + divergence +
+ * stage program), ms[3] the whole stage.  Host-synchronising. */
 amrs_status amrs_profile_stage_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3],
                                    const amrs_stage_prog* prog, amrs_array4 stage_in, amrs_array4 s1,
                                    amrs_array4 out, int32_t reps, void* stream, double* ms);

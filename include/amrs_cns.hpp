@@ -1,7 +1,7 @@
 // amrs_cns.hpp - C++ drop-in with the reference's CNS call surface over the
 // C ABI of amrs_gb300.h (header-only; link libamrs_gb300.so and cudart).
 //
-// Mirrors, for one level whose domain is one box:
+// Mirrors, for one level (a BoxArray tiling the domain):
 //   CNS::compute_rhs(MultiFab& S, MultiFab& dSdt, Real dt, FluxRegister*, FluxRegister*)
 //       src/CNS.h:51, src/tim/CNS_advance.cpp:186-427
 //   CNS::advance(Real time, Real dt, int iteration, int ncycle)
@@ -119,9 +119,11 @@ struct Geometry {
 
 struct FluxRegister;  // reflux is commented out in the reference; the pointers are accepted and unused
 
-// One level whose domain is a single box (the box list of amrs_boxlist_*
-// carries many isolated boxes; intra-level exchange between boxes is not
-// part of this adapter).
+// One level: a BoxArray `grids` tiling the domain (default: the domain as one
+// box).  FillPatch is single-level FillPatch across the level (neighbour
+// copies, periodic images, physical BCs: amrs_boxlist_set_domain);
+// compute_rhs is the reference's MFIter loop of per-box calls; advance runs
+// each RK stage over all boxes at once (amrs_rk_stage_boxlist).
 class CNS {
  public:
   static constexpr int NCONS = 5;
@@ -129,26 +131,44 @@ class CNS {
 
   CNS(const Geometry& geom, const amrs_scheme& scheme, const amrs_closures& closures, int order_rk = 3,
       int stages_rk = 3, int device = 0)
-      : geom_(geom), order_rk_(order_rk), stages_rk_(stages_rk) {
+      : CNS(geom, std::vector<Box>{geom.domain}, scheme, closures, order_rk, stages_rk, device) {}
+
+  CNS(const Geometry& geom, const std::vector<Box>& grids, const amrs_scheme& scheme,
+      const amrs_closures& closures, int order_rk = 3, int stages_rk = 3, int device = 0)
+      : geom_(geom), grids_(grids), order_rk_(order_rk), stages_rk_(stages_rk) {
     check(amrs_create(&h_, &scheme, &closures, device), "amrs_create");
-    std::vector<Box> g{geom.domain};
-    for (int i = 0; i < 3; ++i) state_[i].define(g, NCONS, NGHOST);
-    dSdt_.define(g, NCONS, 0);
+    for (int i = 0; i < 3; ++i) state_[i].define(grids, NCONS, NGHOST);
     for (int d = 0; d < 3; ++d) dxinv_[d] = 1.0 / geom.dx[d];
-    if (cudaMalloc(&dt_dev_, sizeof(Real)) != cudaSuccess) throw Error(AMRS_ERR_ALLOC, "CNS");
+    const int n = (int)grids.size();
+    std::vector<amrs_box> boxes(n);
+    std::vector<double> dx3(3 * n);
+    std::vector<amrs_array4> arrs(3 * n);
+    for (int b = 0; b < n; ++b) {
+      boxes[b] = grids[b].c();
+      for (int d = 0; d < 3; ++d) dx3[3 * b + d] = dxinv_[d];
+      for (int s = 0; s < 3; ++s) arrs[3 * b + s] = state_[s].array(b);
+    }
+    check(amrs_boxlist_create(h_, n, boxes.data(), dx3.data(), 3, arrs.data(), nullptr, 0, nullptr, &bl_),
+          "amrs_boxlist_create");
+    amrs_box dom = geom.domain.c();
+    check(amrs_boxlist_set_domain(bl_, &dom, geom.lo_bc, geom.hi_bc), "amrs_boxlist_set_domain");
+    if (cudaMalloc(&dt_dev_, n * sizeof(Real)) != cudaSuccess) throw Error(AMRS_ERR_ALLOC, "CNS");
   }
   ~CNS() {
     if (dt_dev_) cudaFree(dt_dev_);
+    if (bl_) amrs_boxlist_destroy(bl_);
     if (h_) amrs_destroy(h_);
   }
   CNS(const CNS&) = delete;
   CNS& operator=(const CNS&) = delete;
 
   MultiFab& get_new_data() { return state_[cur_]; }
+  const std::vector<Box>& boxArray() const { return grids_; }
   Real curTime() const { return time_; }
   void setStream(cudaStream_t s) { stream_ = s; }
 
-  // CNS::compute_rhs: S ghost-filled (3 ghosts), dSdt valid-only.
+  // CNS::compute_rhs: S ghost-filled (3 ghosts), dSdt valid-only; the
+  // reference's MFIter loop, one amrs_rhs_box per box.
   void compute_rhs(MultiFab& S, MultiFab& dSdt, Real /*dt*/, FluxRegister* = nullptr, FluxRegister* = nullptr) {
     for (int i = 0; i < S.size(); ++i) {
       amrs_box b = S.box(i).c();
@@ -156,8 +176,15 @@ class CNS {
     }
   }
 
-  // FillPatch for the single-box level (periodic images and physical BCs).
+  // Single-level FillPatch of one of this level's state MultiFabs, or of a
+  // caller MultiFab made of the domain as one box.
   void FillPatch(MultiFab& S) {
+    for (int s = 0; s < 3; ++s)
+      if (&S == &state_[s]) {
+        check(amrs_boxlist_fill_halo(bl_, s, stream_), "amrs_boxlist_fill_halo");
+        return;
+      }
+    if (S.size() != 1) throw Error(AMRS_ERR_STATE, "FillPatch of a multi-box MultiFab outside the level");
     amrs_box d = geom_.domain.c();
     check(amrs_fill_halo_box(&d, geom_.lo_bc, geom_.hi_bc, S.array(0), stream_), "amrs_fill_halo_box");
   }
@@ -172,15 +199,12 @@ class CNS {
     for (int i = 0; i < 3; ++i)
       if (i != s1) work[w++] = i;
     int cur = s1, which = 0;
-    amrs_box b = geom_.domain.c();
     for (int i = 0; i < ns; ++i) {
       const int src = progs[i].src_state == 0 ? s1 : cur;
       int out = work[which];
       if (out == src) { which ^= 1; out = work[which]; }
-      FillPatch(state_[src]);
-      check(amrs_rk_stage_box(h_, &b, dxinv_, &progs[i], dt, state_[src].array(0), state_[s1].array(0),
-                              state_[out].array(0), stream_),
-            "amrs_rk_stage_box");
+      check(amrs_boxlist_fill_halo(bl_, src, stream_), "amrs_boxlist_fill_halo");
+      check(amrs_rk_stage_boxlist(bl_, &progs[i], src, s1, out, stream_), "amrs_rk_stage_boxlist");
       cur = out;
       which ^= 1;
     }
@@ -189,16 +213,19 @@ class CNS {
     return dt;
   }
 
-  // CNS::estTimeStep: cfl * min dx/(|u|+c) (host-synchronising).
+  // CNS::estTimeStep: cfl * min over the level of dx/(|u|+c) (host-synchronising).
   Real estTimeStep(Real cfl) {
-    amrs_box b = geom_.domain.c();
-    check(amrs_est_timestep_box(h_, &b, geom_.dx, cfl, state_[cur_].array(0), dt_dev_, stream_),
-          "amrs_est_timestep_box");
-    Real dt = 0;
-    if (cudaMemcpyAsync(&dt, dt_dev_, sizeof(Real), cudaMemcpyDeviceToHost, stream_) != cudaSuccess ||
+    const int n = (int)grids_.size();
+    for (int b = 0; b < n; ++b) {
+      amrs_box bx = grids_[b].c();
+      check(amrs_est_timestep_box(h_, &bx, geom_.dx, cfl, state_[cur_].array(b), dt_dev_ + b, stream_),
+            "amrs_est_timestep_box");
+    }
+    std::vector<Real> dts(n);
+    if (cudaMemcpyAsync(dts.data(), dt_dev_, n * sizeof(Real), cudaMemcpyDeviceToHost, stream_) != cudaSuccess ||
         cudaStreamSynchronize(stream_) != cudaSuccess)
       throw Error(AMRS_ERR_CUDA, "estTimeStep");
-    return dt;
+    return *std::min_element(dts.begin(), dts.end());
   }
 
   // CNS::computeNewDt for one level: growth capped at 1.1x, last step clamped to stop_time.
@@ -210,13 +237,15 @@ class CNS {
   }
 
   amrs_handle* handle() { return h_; }
+  amrs_boxlist* boxlist() { return bl_; }
 
  private:
   Geometry geom_;
+  std::vector<Box> grids_;
   int order_rk_, stages_rk_;
   amrs_handle* h_ = nullptr;
+  amrs_boxlist* bl_ = nullptr;
   MultiFab state_[3];
-  MultiFab dSdt_;
   int cur_ = 0;
   Real time_ = 0.0;
   Real dxinv_[3];

@@ -1,5 +1,6 @@
 """The C++ drop-in (include/amrs_cns.hpp) used from C++: compute_rhs and
-advance through the CNS-like class give the oracle's bits."""
+advance through the CNS-like class give the oracle's bits, for the domain as
+one box and as a level of 27 uneven boxes (ghosts from neighbours)."""
 import os
 import subprocess
 
@@ -14,7 +15,8 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def test_cpp_adapter_bitexact(orc, tmp_path):
+@pytest.mark.parametrize("m", [1, 3])
+def test_cpp_adapter_bitexact(orc, tmp_path, m):
     assert torch.cuda.is_available()
     lib = B.build()
     exe = str(tmp_path / "cns_adapter")
@@ -26,7 +28,7 @@ def test_cpp_adapter_bitexact(orc, tmp_path):
     fin = tmp_path / "in.bin"
     U.tofile(fin)
     subprocess.check_call([exe, str(fin), str(tmp_path / "rhs.bin"), str(tmp_path / "state.bin"), str(n),
-                           str(nsteps), repr(dt), repr(mu)])
+                           str(nsteps), repr(dt), repr(mu), str(m)])
     R = np.fromfile(tmp_path / "rhs.bin").reshape(5, n, n, n)
     S = np.fromfile(tmp_path / "state.bin").reshape(5, n, n, n)
     cl = P.Closures.nondimensional(mu)

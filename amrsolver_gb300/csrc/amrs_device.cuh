@@ -81,9 +81,13 @@ __device__ __forceinline__ void keep_pair(const double* q1, const double* q2, do
   constexpr int QN = QU + D;
   const double rhoS = q1[QRHO] + q2[QRHO];
   const double unS = q1[QN] + q2[QN];
-  const double massflx = 0.25 * rhoS * unS;                    // fgQuad
-  const double ke = 0.5 * (q1[QU] * q2[QU] + q1[QV] * q2[QV] + q1[QW] * q2[QW]);
-  const double t8 = 0.1250 * rhoS * unS;                       // common factor of fghCubic
+  // t8 = 0.125*rhoS*unS is the common factor of every fghCubic term.  The
+  // reference's fgQuad massflx = 0.25*rhoS*unS equals 2*t8 and its
+  // ke = 0.5*(u1u2+v1v2+w1w2) equals s3/2, both exactly (binary scalings
+  // commute with rounding), so coef*massflx == (2*coef)*t8 and
+  // massflx*ke == t8*s3 to the bit, with three FP64 operations fewer.
+  const double t8 = 0.1250 * rhoS * unS;
+  const double s3 = q1[QU] * q2[QU] + q1[QV] * q2[QV] + q1[QW] * q2[QW];
   const double cx = t8 * (q1[QU] + q2[QU]);
   const double cy = t8 * (q1[QV] + q2[QV]);
   const double cz = t8 * (q1[QW] + q2[QW]);
@@ -93,11 +97,11 @@ __device__ __forceinline__ void keep_pair(const double* q1, const double* q2, do
   // x + 0.5*s evaluated in two steps (one FP64 instruction fewer each).
   const double psum = q1[QPRES] + q2[QPRES];
   const double pu = q1[QPRES] * q2[QN] + q2[QPRES] * q1[QN];
-  T[URHO] = coef * massflx;
+  T[URHO] = (2.0 * coef) * t8;
   T[UMX] = coef * (D == 0 ? fma(0.5, psum, cx) : cx);
   T[UMY] = coef * (D == 1 ? fma(0.5, psum, cy) : cy);
   T[UMZ] = coef * (D == 2 ? fma(0.5, psum, cz) : cz);
-  T[UET] = coef * fma(0.5, pu, massflx * ke + ce);
+  T[UET] = coef * fma(0.5, pu, t8 * s3 + ce);
 }
 
 // Cell-centred viscous fluxes (src/rhs/CNS_hydro_K.h:108-172) from the

@@ -117,6 +117,23 @@ void default_tile(const amrs_box& b, int order, int& tx, int& ty, int& kc, int n
   kc = std::min(kc, nz);
 }
 
+// Time a CTA of the fused face kernel spends on one plane of a txw x tyw
+// tile column, in units of one KEEP pair evaluation by one thread.  The
+// kernel's phases are separated by barriers and deal their items
+// round-robin over F_THREADS threads, so a phase costs its rounds: phase 1
+// the H z pairs of a column plus the x/y stored pairs of separation >= 2,
+// phase 2 the x and y faces (~1.5 pairs each with their sums and viscous
+// averages), phase 3 the divergence (~0.5), plus a fixed ~1 per plane
+// (barriers, the wait for the plane's load).  A thin partial tile thus
+// costs about half a full one per plane, not its share of cells.
+double face_plane_cost(int H, int txw, int tyw) {
+  int nxy = 0;
+  for (int l = 2; l <= H; ++l) nxy += (txw + l) * tyw + txw * (tyw + l);
+  const int nf = (txw + 1) * tyw + txw * (tyw + 1);
+  auto rounds = [](int items) { return (double)((items + F_THREADS - 1) / F_THREADS); };
+  return 1.0 + H + rounds(nxy) + 1.5 * rounds(nf) + 0.5;
+}
+
 // -------------------------------------------------------------- list ----
 // Host + device state of one box list (a level, or one box for the per-box
 // entry points).
@@ -326,9 +343,10 @@ amrs_status list_build(amrs_handle* h, List& L, int n, const amrs_box* boxes, co
   for (int d = 0; d < 3; ++d) { L.tot_f[d] = L.fpre[d][n]; L.tot_s[d] = L.spre[d][n]; }
 
   // Balanced static schedule of the fused face kernel: the (tile column x
-  // plane) work of all boxes, weighted by the column's cells, is cut into
-  // G equal shares (G = resident CTAs); a share is a run of segments
-  // (box, column, k0, k1), each segment costing one z-prologue.
+  // plane) work of all boxes, weighted by the time a CTA spends on one plane
+  // of that column (face_plane_cost), is cut into G equal shares (G =
+  // resident CTAs); a share is a run of segments (box, column, k0, k1),
+  // each segment costing one z-prologue.
   std::vector<int4> segs;
   std::vector<int> cta_seg;
   L.face_grid = 0;
@@ -341,7 +359,7 @@ amrs_status list_build(amrs_handle* h, List& L, int n, const amrs_box* boxes, co
         const int txi = c % R.ntx, tyi = c / R.ntx;
         const int txw = std::min(R.tx, R.hi[0] + 1 - (R.lo[0] + txi * R.tx));
         const int tyw = std::min(R.ty, R.hi[1] + 1 - (R.lo[1] + tyi * R.ty));
-        total += (double)txw * tyw * bn(boxes[b], 2);
+        total += face_plane_cost(order / 2, txw, tyw) * bn(boxes[b], 2);
         colplanes += bn(boxes[b], 2);
       }
     }
@@ -356,7 +374,7 @@ amrs_status list_build(amrs_handle* h, List& L, int n, const amrs_box* boxes, co
         const int txi = c % R.ntx, tyi = c / R.ntx;
         const int txw = std::min(R.tx, R.hi[0] + 1 - (R.lo[0] + txi * R.tx));
         const int tyw = std::min(R.ty, R.hi[1] + 1 - (R.lo[1] + tyi * R.ty));
-        const double w = (double)txw * tyw;
+        const double w = face_plane_cost(order / 2, txw, tyw);
         int k = R.lo[2];
         while (k <= R.hi[2]) {
           const double boundary = (cta + 1) * per;

@@ -521,17 +521,33 @@ inline void cns_riemann(int i, int j, int k, int d, const Arr<R>& f, const Arr<R
 // Cell-centred viscous fluxes: src/rhs/CNS_hydro_K.h:108-172.
 template <class R>
 inline void viscous_fluxes(int i, int j, int k, const Arr<R>& q, const Arr<R> pf[3], const double dxinv[3],
-                           const Closures& cl) {
+                           const Closures& cl, int loc = -1) {
+  // loc -1: ViscousFluxes (src/rhs/CNS_hydro_K.h:108-172); loc 0 / 1:
+  // ViscousWallFluxes at the ghost row of a lower / upper y wall (:177-251),
+  // one-sided second-order y derivatives
   R ux = q(i, j, k, QU);
   R dudx = (q(i + 1, j, k, QU) - q(i - 1, j, k, QU)) * R(0.5) * R(dxinv[0]);
   R dvdx = (q(i + 1, j, k, QV) - q(i - 1, j, k, QV)) * R(0.5) * R(dxinv[0]);
   R dwdx = (q(i + 1, j, k, QW) - q(i - 1, j, k, QW)) * R(0.5) * R(dxinv[0]);
   R dTdx = (q(i + 1, j, k, QT) - q(i - 1, j, k, QT)) * R(0.5) * R(dxinv[0]);
   R uy = q(i, j, k, QV);
-  R dudy = (q(i, j + 1, k, QU) - q(i, j - 1, k, QU)) * R(0.5) * R(dxinv[1]);
-  R dvdy = (q(i, j + 1, k, QV) - q(i, j - 1, k, QV)) * R(0.5) * R(dxinv[1]);
-  R dwdy = (q(i, j + 1, k, QW) - q(i, j - 1, k, QW)) * R(0.5) * R(dxinv[1]);
-  R dTdy = (q(i, j + 1, k, QT) - q(i, j - 1, k, QT)) * R(0.5) * R(dxinv[1]);
+  R dudy, dvdy, dwdy, dTdy;
+  if (loc == 0) {
+    dudy = (-q(i, j + 2, k, QU) + R(4) * q(i, j + 1, k, QU) - R(3) * q(i, j, k, QU)) * R(0.5) * R(dxinv[1]);
+    dvdy = (-q(i, j + 2, k, QV) + R(4) * q(i, j + 1, k, QV) - R(3) * q(i, j, k, QV)) * R(0.5) * R(dxinv[1]);
+    dwdy = (-q(i, j + 2, k, QW) + R(4) * q(i, j + 1, k, QW) - R(3) * q(i, j, k, QW)) * R(0.5) * R(dxinv[1]);
+    dTdy = (-q(i, j + 2, k, QT) + R(4) * q(i, j + 1, k, QT) - R(3) * q(i, j, k, QT)) * R(0.5) * R(dxinv[1]);
+  } else if (loc == 1) {
+    dudy = (R(3) * q(i, j, k, QU) - R(4) * q(i, j - 1, k, QU) + q(i, j - 2, k, QU)) * R(0.5) * R(dxinv[1]);
+    dvdy = (R(3) * q(i, j, k, QV) - R(4) * q(i, j - 1, k, QV) + q(i, j - 2, k, QV)) * R(0.5) * R(dxinv[1]);
+    dwdy = (R(3) * q(i, j, k, QW) - R(4) * q(i, j - 1, k, QW) + q(i, j - 2, k, QW)) * R(0.5) * R(dxinv[1]);
+    dTdy = (R(3) * q(i, j, k, QT) - R(4) * q(i, j - 1, k, QT) + q(i, j - 2, k, QT)) * R(0.5) * R(dxinv[1]);
+  } else {
+    dudy = (q(i, j + 1, k, QU) - q(i, j - 1, k, QU)) * R(0.5) * R(dxinv[1]);
+    dvdy = (q(i, j + 1, k, QV) - q(i, j - 1, k, QV)) * R(0.5) * R(dxinv[1]);
+    dwdy = (q(i, j + 1, k, QW) - q(i, j - 1, k, QW)) * R(0.5) * R(dxinv[1]);
+    dTdy = (q(i, j + 1, k, QT) - q(i, j - 1, k, QT)) * R(0.5) * R(dxinv[1]);
+  }
   R uz = q(i, j, k, QW);
   R dudz = (q(i, j, k + 1, QU) - q(i, j, k - 1, QU)) * R(0.5) * R(dxinv[2]);
   R dvdz = (q(i, j, k + 1, QV) - q(i, j, k - 1, QV)) * R(0.5) * R(dxinv[2]);
@@ -630,9 +646,16 @@ template <class R> R* pool(int slot, size_t n) {
 // u: ghosted (NGHOST) conserved state; dsdt: valid-only output.
 // Only faces the divergence reads are evaluated (the reference also computes
 // x-fluxes on j,k = hi+1 etc., which never reach dsdt).
+// y walls of the domain with boundary code 6 (user-defined, ext_dir): the
+// reference's wall treatment for boxes that touch them.
+struct Walls {
+  int lo, hi;          // code 6 on the lower / upper y side
+  int dom_lo, dom_hi;  // the domain's y extent
+};
+
 template <class R>
 void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const double dxinv[3],
-                     const R* uptr, R* dsdt, int nthreads) {
+                     const R* uptr, R* dsdt, int nthreads, const Walls* walls = nullptr) {
   const int g = NGHOST;
   const long long ncg = (long long)(bx.n(0) + 2 * g) * (bx.n(1) + 2 * g) * (bx.n(2) + 2 * g);
   Arr<R> u = make_arr<R>(const_cast<R*>(uptr), bx, g);
@@ -727,6 +750,32 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
       }
     }
 
+    // Order reduction next to y walls (:226-229, Flux_2nd_Order_KEEP in
+    // src/rhs/CentralKEEP.h:232-287): KEEPy with halfsten 1 and coefficient
+    // 1 overwrites the y faces j in [lo, lo+H-1] of a box on a lower wall and
+    // [hi-H+1, hi] (not the wall face hi+1) of a box on an upper wall.
+    if (sc.flux_euler == 1 && sc.order_keep != 2 && walls) {
+      const double c2[3] = {1.0, 0.0, 0.0};
+      const int H = sc.order_keep / 2;
+      for (int side = 0; side < 2; ++side) {
+        int j0, j1;
+        if (side == 0) {
+          if (!(walls->lo && lo1 == walls->dom_lo)) continue;
+          j0 = lo1; j1 = lo1 + H - 1;
+        } else {
+          if (!(walls->hi && hi1 == walls->dom_hi)) continue;
+          j0 = hi1 - H + 1; j1 = hi1;
+        }
+        for (int k = lo2; k <= hi2; ++k)
+          for (int j = j0; j <= j1; ++j)
+            for (int i = lo0; i <= hi0; ++i) {
+              R f[NCONS];
+              keep_face(i, j, k, 1, 1, c2, q, f, cl);
+              for (int n = 0; n < NCONS; ++n) F[1](i, j, k, n) = f[n];
+            }
+      }
+    }
+
     // JST artificial dissipation (:235-265): sensor/lambda on the valid box,
     // zero elsewhere, then subtracted on every face.
     if (sc.art_diss == 1) {
@@ -767,7 +816,14 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
 #endif
     for (int k = lo2 - 1; k <= hi2 + 1; ++k)
       for (int j = lo1 - 1; j <= hi1 + 1; ++j)
-        for (int i = lo0 - 1; i <= hi0 + 1; ++i) viscous_fluxes(i, j, k, q, VF, dxinv, cl);
+        for (int i = lo0 - 1; i <= hi0 + 1; ++i) {
+          // wall rows (:300-333): the ghost row below a lower / above an
+          // upper y wall of a box that touches it
+          int loc = -1;
+          if (walls && walls->lo && lo1 == walls->dom_lo && j == lo1 - 1) loc = 0;
+          if (walls && walls->hi && hi1 == walls->dom_hi && j == hi1 + 1) loc = 1;
+          viscous_fluxes(i, j, k, q, VF, dxinv, cl, loc);
+        }
     // ViscousNumericalFluxes: src/rhs/CNS_hydro_K.h:254-261
     set_phase(4);
     for (int d = 0; d < 3; ++d) {
@@ -1010,6 +1066,18 @@ int orc_compute_rhs(const OrcScheme* s, const OrcClosures* c, const int* lo, con
   Box b = to_box(lo, hi);
   for (int d = 0; d < 3; ++d) if (b.n(d) < 1) return 2;
   compute_rhs_box<double>(to_sc(s), to_cl(c), b, dxinv, U, dSdt, nthreads);
+  return 0;
+}
+
+// dS/dt of one ghost-filled box of a domain whose y sides may be code-6
+// walls: walls4 = {wall_lo, wall_hi, dom_lo_y, dom_hi_y}.
+int orc_compute_rhs_walls(const OrcScheme* s, const OrcClosures* c, const int* lo, const int* hi,
+                          const double* dxinv, const double* U, double* dSdt, int nthreads, const int* walls4) {
+  if (!s || !c || !lo || !hi || !dxinv || !U || !dSdt || !walls4) return 1;
+  Box b = to_box(lo, hi);
+  for (int d = 0; d < 3; ++d) if (b.n(d) < 1) return 2;
+  Walls w{walls4[0], walls4[1], walls4[2], walls4[3]};
+  compute_rhs_box<double>(to_sc(s), to_cl(c), b, dxinv, U, dSdt, nthreads, &w);
   return 0;
 }
 

@@ -67,6 +67,9 @@ class Oracle:
         L.orc_compute_rhs.argtypes = [ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ip, ip, dp,
                                       dp, dp, ctypes.c_int]
         L.orc_compute_rhs.restype = ctypes.c_int
+        L.orc_compute_rhs_walls.argtypes = [ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ip, ip, dp,
+                                            dp, dp, ctypes.c_int, ip]
+        L.orc_compute_rhs_walls.restype = ctypes.c_int
         L.orc_fill_halo.argtypes = [ip, ip, ip, ip, dp, ctypes.c_int]
         L.orc_fill_halo.restype = ctypes.c_int
         L.orc_est_timestep.argtypes = [ctypes.POINTER(CClosures), ip, ip, dp, dp, ctypes.c_int,
@@ -85,12 +88,21 @@ class Oracle:
             L.orc_compute_rhs_count.restype = ctypes.c_int
 
     # -------------------------------------------------------------- calls --
-    def rhs(self, scheme, closures, U, dxinv, lo=(0, 0, 0), nthreads=1):
+    def rhs(self, scheme, closures, U, dxinv, lo=(0, 0, 0), nthreads=1, walls=None):
+        """dS/dt of one ghost-filled box.  walls = (wall_lo, wall_hi, dom_lo_y,
+        dom_hi_y): y sides of the domain with boundary code 6."""
         U = np.ascontiguousarray(U, dtype=np.float64)
         nz, ny, nx = (s - 2 * NG for s in U.shape[1:])
         hi = (lo[0] + nx - 1, lo[1] + ny - 1, lo[2] + nz - 1)
         out = np.empty((NCONS, nz, ny, nx))
         sc, cl = c_scheme(scheme), c_closures(closures)
+        if walls is not None:
+            w4 = (ctypes.c_int * 4)(*[int(v) for v in walls])
+            rc = self.lib.orc_compute_rhs_walls(ctypes.byref(sc), ctypes.byref(cl), _i3(lo), _i3(hi), _d3(dxinv),
+                                                _ptr(U), _ptr(out), int(nthreads), w4)
+            if rc:
+                raise RuntimeError("orc_compute_rhs_walls failed: %d" % rc)
+            return out
         rc = self.lib.orc_compute_rhs(ctypes.byref(sc), ctypes.byref(cl), _i3(lo), _i3(hi), _d3(dxinv),
                                       _ptr(U), _ptr(out), int(nthreads))
         if rc:

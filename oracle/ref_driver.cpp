@@ -246,6 +246,26 @@ int orc_compute_rhs(const OrcScheme* s, const OrcClosures* c, const int* lo, con
   return 0;
 }
 
+// The same with y sides of boundary code 6 where walls4 = {wall_lo, wall_hi,
+// dom_lo_y, dom_hi_y} says so (x, z periodic; a non-wall y side outflow):
+// the reference's own Flux_2nd_Order_KEEP and ViscousWallFluxes branches of
+// compute_rhs run.  The box must be the domain.
+int orc_compute_rhs_walls(const OrcScheme* s, const OrcClosures* c, const int* lo, const int* hi,
+                          const double* dxinv, const double* U, double* dSdt, int /*nthreads*/, const int* walls4) {
+  if (walls4[2] != lo[1] || walls4[3] != hi[1]) return 20;
+  if (int rc = set_closures(c)) return rc;
+  set_scheme(s);
+  static CNS lev;
+  static Amr amr;
+  int bl[3] = {-1, walls4[0] ? 6 : 2, -1}, bh[3] = {-1, walls4[1] ? 6 : 2, -1};
+  setup_level(lev, amr, lo, hi, dxinv, bl, bh);
+  MultiFab& Sborder = CNS::VSborder[0];
+  copy_in(Sborder, U);
+  lev.compute_rhs(Sborder, CNS::VdSdt[0], 0.0, nullptr, nullptr);
+  copy_valid_out(CNS::VdSdt[0], dSdt, 0);
+  return 0;
+}
+
 int orc_fill_halo(const int* lo, const int* hi, const int* bc_lo, const int* bc_hi, double* U, int ncomp) {
   Box dom(IntVect(lo[0], lo[1], lo[2]), IntVect(hi[0], hi[1], hi[2]));
   Geometry geom;

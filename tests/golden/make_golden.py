@@ -55,10 +55,33 @@ RHS_CASES = [
     ("riemann_suth", "suth", dict(flux_euler=0, rhs_visc=1), (6, 5, 4), (0, 0, 0), (50.0, 50.0, 50.0)),
 ]
 
+WALL_CASES = [
+    # name, scheme kwargs, box shape, lo, dxinv, (wall_lo, wall_hi): y sides with boundary code 6
+    ("keep4_visc", dict(flux_euler=1, order_keep=4, rhs_visc=1), (6, 7, 4), (1, -2, 0), (2.0, 3.0, 2.5), (1, 1)),
+    ("keep6_euler", dict(flux_euler=1, order_keep=6, rhs_visc=0), (5, 8, 4), (0, 0, 3), (2.0, 2.0, 2.0), (1, 0)),
+    ("weno_visc", dict(flux_euler=2, rhs_visc=1), (5, 6, 4), (0, 3, 0), (2.0, 2.5, 3.0), (0, 1)),
+]
+
 ADV_CASES = [
     # name, order_rk, stages_rk
     ("ssprk3", 3, 3), ("ssprk43", 3, 4), ("ssprkm2_3", 2, 3), ("euler", 1, 1), ("heun", -2, 2), ("rhsonly", 0, 1),
 ]
+
+
+def write_wall_cases():
+    """RHS of boxes on code-6 y walls (the reference's Flux_2nd_Order_KEEP and
+    ViscousWallFluxes branches); the box is the domain."""
+    cl = closures("const")
+    ref = pyoracle.reference(cl)
+    for i, (name, skw, n, lo, dxinv, walls) in enumerate(WALL_CASES):
+        sc = P.Scheme(**skw)
+        U = P.random_state(n, seed=300 + i)
+        w = (walls[0], walls[1], lo[1], lo[1] + n[1] - 1)
+        R = ref.rhs(sc, cl, U, dxinv, lo=lo, walls=w)
+        np.savez_compressed(os.path.join(HERE, "wall_%s.npz" % name), U=U, dSdt=R, lo=np.array(lo),
+                            dxinv=np.array(dxinv), walls=np.array(w),
+                            scheme=np.array([sc.rhs_euler, sc.rhs_visc, sc.flux_euler, sc.order_keep, sc.art_diss]),
+                            closures="const")
 
 
 def main():
@@ -103,6 +126,7 @@ def main():
         halo["U_" + tag] = A
         halo["bc_" + tag] = np.array([bl, bh])
     np.savez_compressed(os.path.join(HERE, "halo.npz"), V=V, **halo)
+    write_wall_cases()
     print("wrote golden fixtures:", sorted(os.listdir(HERE)))
 
 

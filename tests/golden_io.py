@@ -28,6 +28,20 @@ def rhs_cases():
     return out
 
 
+def wall_cases():
+    """RHS fixtures of boxes on code-6 y walls (walls = wall_lo, wall_hi, dom_lo_y, dom_hi_y)."""
+    out = []
+    for f in sorted(glob.glob(os.path.join(HERE, "wall_*.npz"))):
+        z = np.load(f)
+        s = z["scheme"]
+        sc = P.Scheme(rhs_euler=int(s[0]), rhs_visc=int(s[1]), flux_euler=int(s[2]), order_keep=int(s[3]),
+                      art_diss=int(s[4]))
+        out.append(dict(name=os.path.basename(f)[5:-4], U=z["U"], dSdt=z["dSdt"], lo=tuple(int(v) for v in z["lo"]),
+                        dxinv=tuple(float(v) for v in z["dxinv"]), walls=tuple(int(v) for v in z["walls"]),
+                        scheme=sc, closures=closures(z["closures"])))
+    return out
+
+
 def adv_cases():
     out = []
     for f in sorted(glob.glob(os.path.join(HERE, "adv_*.npz"))):

@@ -21,6 +21,12 @@ def test_rhs_golden(orc, case):
     assert G.relmax(R, case["dSdt"]) <= TOL
 
 
+@pytest.mark.parametrize("case", G.wall_cases(), ids=lambda c: c["name"])
+def test_rhs_walls_golden(orc, case):
+    R = orc.rhs(case["scheme"], case["closures"], case["U"], case["dxinv"], lo=case["lo"], walls=case["walls"])
+    assert G.relmax(R, case["dSdt"]) <= TOL
+
+
 @pytest.mark.parametrize("case", G.adv_cases(), ids=lambda c: c["name"])
 def test_advance_golden(orc, case):
     cl = G.closures("const")

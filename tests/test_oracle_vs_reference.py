@@ -29,6 +29,25 @@ def test_rhs_bitexact(orc, skw):
     np.testing.assert_array_equal(orc.rhs(sc, CL, U, dxinv, lo=lo), REF.rhs(sc, CL, U, dxinv, lo=lo))
 
 
+WALL_SCHEMES = [dict(flux_euler=1, order_keep=o, rhs_visc=v) for o in (2, 4, 6) for v in (0, 1)] + \
+    [dict(flux_euler=2, rhs_visc=1), dict(flux_euler=0, rhs_visc=1)]
+
+
+@pytest.mark.parametrize("walls", [(1, 1), (1, 0), (0, 1)])
+@pytest.mark.parametrize("skw", WALL_SCHEMES, ids=lambda d: "-".join("%s%s" % kv for kv in d.items()))
+def test_rhs_walls_bitexact(orc, skw, walls):
+    """y sides with boundary code 6: the reference's own Flux_2nd_Order_KEEP
+    and ViscousWallFluxes branches of compute_rhs against the restatement."""
+    sc = P.Scheme(**skw)
+    rng = np.random.default_rng(len(str(skw)) + 7 * walls[0] + walls[1])
+    n = tuple(int(v) for v in rng.integers(4, 10, 3))
+    U = P.random_state(n, seed=int(rng.integers(1 << 30)), amp=0.2)
+    lo = tuple(int(v) for v in rng.integers(-5, 5, 3))
+    dxinv = tuple(float(v) for v in rng.uniform(1.0, 5.0, 3))
+    w = (walls[0], walls[1], lo[1], lo[1] + n[1] - 1)
+    np.testing.assert_array_equal(orc.rhs(sc, CL, U, dxinv, lo=lo, walls=w), REF.rhs(sc, CL, U, dxinv, lo=lo, walls=w))
+
+
 @pytest.mark.parametrize("ork,srk", [(3, 3), (3, 4), (2, 2), (2, 4), (1, 1), (0, 1), (-2, 2)])
 def test_advance_bitexact(orc, ork, srk):
     sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1)

@@ -58,6 +58,7 @@ SIGNATURES = {
     "amrs_create": (_S, [ctypes.POINTER(_P), ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ctypes.c_int]),
     "amrs_destroy": (_S, [_P]),
     "amrs_set_closures": (_S, [_P, ctypes.POINTER(CClosures)]),
+    "amrs_set_domain": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32)]),
     "amrs_status_string": (ctypes.c_char_p, [_S]),
     "amrs_last_cuda_error": (ctypes.c_char_p, []),
     "amrs_version": (ctypes.c_int32, []),
@@ -205,6 +206,15 @@ class Handle:
             self.close()
         except Exception:
             pass
+
+    def set_domain(self, dom_lo, dom_n, bc_lo, bc_hi):
+        """amrs_set_domain: domain box (lo, extents x,y,z) and boundary codes of
+        the per-box calls; code 6 on a y side is a wall.  None clears."""
+        if dom_lo is None:
+            check(self._L.amrs_set_domain(self.h, None, None, None), "amrs_set_domain")
+            return
+        dom = c_box(dom_lo, dom_n)
+        check(self._L.amrs_set_domain(self.h, ctypes.byref(dom), i3(bc_lo), i3(bc_hi)), "amrs_set_domain")
 
     def rhs_box(self, U, dxinv, out, lo=(0, 0, 0), stream=None):
         """dSdt of one ghost-filled box into `out` (ncomp, nz, ny, nx)."""

@@ -33,8 +33,11 @@ class CNSLevel:
         U0 = np.ascontiguousarray(U0, dtype=np.float64)
         self.shape = U0.shape
         self.n = tuple(s - 2 * NGHOST for s in U0.shape[1:][::-1])  # (nx, ny, nz)
-        self.bufs = [torch.from_numpy(U0).to(self.dev), torch.empty_like(torch.from_numpy(U0), device=self.dev),
-                     torch.empty_like(torch.from_numpy(U0), device=self.dev)]
+        # all three buffers start as U0: ghost cells beyond ext_dir sides
+        # (codes 1, 6) are the caller's and keep these values
+        first = torch.from_numpy(U0).to(self.dev)
+        self.bufs = [first, first.clone(), first.clone()]
+        self.h.set_domain(self.lo, self.n, self.bc_lo, self.bc_hi)
         self.cur = 0
         self.time = 0.0
         self.dt_dev = torch.zeros(1, dtype=torch.float64, device=self.dev)

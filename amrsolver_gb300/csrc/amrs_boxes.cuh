@@ -18,6 +18,13 @@ struct BoxRec {
   int cl;                // closure index
   int tx, ty, kc;        // tile shape and z chunk of the face kernel
   int ntx, nty, nkz;     // tiles per direction
+  // y walls of boundary code 6 that this box touches (walls == 0: none):
+  // viscous cell fluxes of rows wrow_lo / wrow_hi use one-sided y
+  // derivatives (ViscousWallFluxes); KEEP y faces j <= red_lo or
+  // red_hi <= j <= hi[1] take the second-order pair (Flux_2nd_Order_KEEP)
+  int walls;
+  int wrow_lo, wrow_hi;
+  int red_lo, red_hi;
 };
 
 // Prefix tables for flattening launches over boxes.

@@ -108,22 +108,20 @@ __device__ __forceinline__ void keep_pair(const double* q1, const double* q2, do
 // primitive values at the cell and its six neighbours.  Output: x, y, z
 // blocks of (UMX..UET); the mass entries are zero in the reference.
 // `qc` centre, `qxm/qxp`, `qym/qyp`, `qzm/qzp` neighbours (u,v,w,T read).
-__device__ __forceinline__ void viscous_cell(const double* qc, const double* qxm, const double* qxp,
-                                             const double* qym, const double* qyp, const double* qzm,
-                                             const double* qzp, const double dxinv[3], const DClosures& c,
-                                             double f[NVF]) {
+// The same with the four y derivatives (u, v, w, T) given: the body shared
+// by the interior form and the wall rows' one-sided form.
+__device__ __forceinline__ void viscous_cell_dy(const double* qc, const double* qxm, const double* qxp,
+                                                const double dy[4], const double* qzm, const double* qzp,
+                                                const double dxinv[3], const DClosures& c, double f[NVF]) {
   // (a-b)*0.5*dxinv == (a-b)*(0.5*dxinv) exactly: the 0.5 scalings are exact.
-  const double hx = 0.5 * dxinv[0], hy = 0.5 * dxinv[1], hz = 0.5 * dxinv[2];
+  const double hx = 0.5 * dxinv[0], hz = 0.5 * dxinv[2];
   const double ux = qc[QU];
   const double dudx = (qxp[QU] - qxm[QU]) * hx;
   const double dvdx = (qxp[QV] - qxm[QV]) * hx;
   const double dwdx = (qxp[QW] - qxm[QW]) * hx;
   const double dTdx = (qxp[QT] - qxm[QT]) * hx;
   const double uy = qc[QV];
-  const double dudy = (qyp[QU] - qym[QU]) * hy;
-  const double dvdy = (qyp[QV] - qym[QV]) * hy;
-  const double dwdy = (qyp[QW] - qym[QW]) * hy;
-  const double dTdy = (qyp[QT] - qym[QT]) * hy;
+  const double dudy = dy[0], dvdy = dy[1], dwdy = dy[2], dTdy = dy[3];
   const double uz = qc[QW];
   const double dudz = (qzp[QU] - qzm[QU]) * hz;
   const double dvdz = (qzp[QV] - qzm[QV]) * hz;
@@ -152,6 +150,36 @@ __device__ __forceinline__ void viscous_cell(const double* qc, const double* qxm
   f[9] = -tauyz;
   f[10] = -tauzz;
   f[11] = -lambda * dTdz - tauxz * ux - tauyz * uy - tauzz * uz;
+}
+
+__device__ __forceinline__ void viscous_cell(const double* qc, const double* qxm, const double* qxp,
+                                             const double* qym, const double* qyp, const double* qzm,
+                                             const double* qzp, const double dxinv[3], const DClosures& c,
+                                             double f[NVF]) {
+  const double hy = 0.5 * dxinv[1];
+  const double dy[4] = {(qyp[QU] - qym[QU]) * hy, (qyp[QV] - qym[QV]) * hy, (qyp[QW] - qym[QW]) * hy,
+                        (qyp[QT] - qym[QT]) * hy};
+  viscous_cell_dy(qc, qxm, qxp, dy, qzm, qzp, dxinv, c, f);
+}
+
+// ViscousWallFluxes (src/rhs/CNS_hydro_K.h:177-251): the cell viscous fluxes
+// of the ghost row next to a y wall with second-order one-sided y
+// derivatives; loc 0 (lower wall) reads rows j, j+1, j+2 as (q0, q1, q2),
+// loc 1 (upper wall) rows j, j-1, j-2.  -a + 4b and 3c - 4b are single fmas
+// (the factor 4 is exact).
+__device__ __forceinline__ void viscous_wall_cell(int loc, const double* qc, const double* qxm, const double* qxp,
+                                                  const double* q1, const double* q2, const double* qzm,
+                                                  const double* qzp, const double dxinv[3], const DClosures& c,
+                                                  double f[NVF]) {
+  const double hy = 0.5 * dxinv[1];
+  double dy[4];
+#pragma unroll
+  for (int n = 0; n < 4; ++n) {
+    const int m = QU + n;
+    dy[n] = (loc == 0) ? (fma(4.0, q1[m], -q2[m]) - 3.0 * qc[m]) * hy
+                       : (fma(-4.0, q1[m], 3.0 * qc[m]) + q2[m]) * hy;
+  }
+  viscous_cell_dy(qc, qxm, qxp, dy, qzm, qzp, dxinv, c, f);
 }
 
 // RK stage program (AMReX BLAS-1 semantics), registers S1, S2, dS.

@@ -134,6 +134,26 @@ double face_plane_cost(int H, int txw, int tyw) {
   return 1.0 + H + rounds(nxy) + 1.5 * rounds(nf) + 0.5;
 }
 
+// y sides of the domain with boundary code 6 (user-defined walls) and the
+// domain's y extent: the reference's wall treatment in compute_rhs
+// (src/tim/CNS_advance.cpp:226-229, :300-333) for boxes that touch them.
+struct WallCfg {
+  int lo = 0, hi = 0;
+  int dom_lo = 0, dom_hi = 0;
+};
+
+void set_walls(BoxRec& R, const WallCfg& w, const amrs_scheme& sc) {
+  const bool tl = w.lo && R.lo[1] == w.dom_lo, th = w.hi && R.hi[1] == w.dom_hi;
+  const bool reduce = sc.rhs_euler && sc.flux_euler == 1 && sc.order_keep != 2;
+  const int H = sc.order_keep / 2;
+  const int none = -(1 << 29);
+  R.walls = (tl || th) ? 1 : 0;
+  R.wrow_lo = tl ? R.lo[1] - 1 : none;
+  R.wrow_hi = th ? R.hi[1] + 1 : none;
+  R.red_lo = (tl && reduce) ? R.lo[1] + H - 1 : none;
+  R.red_hi = (th && reduce) ? R.hi[1] - H + 1 : (1 << 29);
+}
+
 // -------------------------------------------------------------- list ----
 // Host + device state of one box list (a level, or one box for the per-box
 // entry points).
@@ -172,6 +192,7 @@ struct List {
   int bc_lo[3] = {-1, -1, -1}, bc_hi[3] = {-1, -1, -1};
   LevelDomain dom{};
   int* d_owner = nullptr;  // has_bc == 2: owning box of every grown cell's source (-1: valid cell)
+  WallCfg wall{};          // code-6 y walls of the list's domain (amrs_boxlist_set_domain)
   ~List() {
     if (graph) cudaGraphExecDestroy(graph);
     if (dtab) cudaFree(dtab);
@@ -192,6 +213,7 @@ struct amrs_handle {
   bool tma_ok = true;
   void* encode_fn = nullptr;
   List* one = nullptr;               // reusable single-box list for per-box calls
+  WallCfg wall{};                    // code-6 y walls of the per-box calls' domain (amrs_set_domain)
   void* adj = nullptr;               // adjoint scratch (pair and viscous cotangents), grow-only
   size_t adj_bytes = 0;
   BoxRec* dring = nullptr;           // per-call box records of per-box calls (device ring)
@@ -296,6 +318,7 @@ amrs_status list_build(amrs_handle* h, List& L, int n, const amrs_box* boxes, co
       R.dx[d] = 1.0 / dxinv3[3 * b + d];
     }
     for (int s = 0; s < nslots && s < MAX_SLOTS; ++s) R.slot[s] = to_darr(states[b * nslots + s]);
+    set_walls(R, L.wall, h->sc);
     auto mk = [&](size_t o, int g, int nodal_d, int ncomp_unused) {
       (void)ncomp_unused;
       DArr a;
@@ -565,6 +588,7 @@ amrs_status one_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3], c
   if (h->ring_used[i]) CK(cudaEventSynchronize(h->ring_ev[i]));
   BoxRec R = L->hbox[0];
   for (int s = 0; s < nslots; ++s) R.slot[s] = to_darr(slots[s]);
+  set_walls(R, h->wall, h->sc);
   if (dx_override)
     for (int d = 0; d < 3; ++d) R.dx[d] = dx_override[d];
   h->hring[i] = R;
@@ -663,6 +687,24 @@ amrs_status amrs_set_closures(amrs_handle* h, const amrs_closures* closures) {
   return AMRS_OK;
 }
 
+amrs_status amrs_set_domain(amrs_handle* h, const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3]) {
+  if (!h) return AMRS_ERR_NULL;
+  std::lock_guard<std::mutex> lk(h->mu);
+  if (!domain || !bc_lo || !bc_hi) {
+    h->wall = WallCfg{};
+    return AMRS_OK;
+  }
+  if (!box_ok(*domain)) return AMRS_ERR_BOX;
+  for (int d = 0; d < 3; ++d) {
+    if ((bc_lo[d] == -1) != (bc_hi[d] == -1)) return AMRS_ERR_BC;
+    if (bc_lo[d] < -1 || bc_lo[d] > 6 || bc_hi[d] < -1 || bc_hi[d] > 6) return AMRS_ERR_BC;
+  }
+  WallCfg w;
+  w.lo = bc_lo[1] == 6; w.hi = bc_hi[1] == 6; w.dom_lo = domain->lo[1]; w.dom_hi = domain->hi[1];
+  h->wall = w;
+  return AMRS_OK;
+}
+
 amrs_status amrs_rk_program(int32_t order_rk, int32_t stages_rk, double dt, amrs_stage_prog* st, int32_t cap,
                             int32_t* nstages) {
   if (!st || !nstages) return AMRS_ERR_NULL;
@@ -753,7 +795,7 @@ amrs_status amrs_fill_halo_box(const amrs_box* domain, const int32_t bc_lo[3], c
     if ((bc_lo[d] == -1) != (bc_hi[d] == -1)) return AMRS_ERR_BC;
     for (int s = 0; s < 2; ++s) {
       const int p = s ? bc_hi[d] : bc_lo[d];
-      if (p == 1 || p == 6 || p < -1 || p > 6) return AMRS_ERR_BC;
+      if (p < -1 || p > 6) return AMRS_ERR_BC;  // 1, 6: ext_dir, caller-filled
     }
     if (bn(*domain, d) < NGHOST && bc_lo[d] != -1 && bc_lo[d] != 2) return AMRS_ERR_BOX;
     hb.lo[d] = domain->lo[d]; hb.hi[d] = domain->hi[d]; hb.bc_lo[d] = bc_lo[d]; hb.bc_hi[d] = bc_hi[d];
@@ -913,6 +955,14 @@ amrs_status level_owner_table(const List& L, const LevelDomain& dom, std::vector
       for (int j = B.lo[1] - g; j <= B.hi[1] + g; ++j)
         for (int i = B.lo[0] - g; i <= B.hi[0] + g; ++i, ++idx) {
           if (box_has(B, i, j, k)) continue;
+          // beyond an ext_dir side (codes 1, 6) the caller's values stay
+          bool ext = false;
+          const int cc[3] = {i, j, k};
+          for (int d = 0; d < 3; ++d) {
+            const int p = cc[d] < dom.lo[d] ? dom.bc_lo[d] : (cc[d] > dom.hi[d] ? dom.bc_hi[d] : 0);
+            if (p == 1 || p == 6) ext = true;
+          }
+          if (ext) continue;
           const int si = map_coord_host(i, dom.lo[0], dom.hi[0], dom.bc_lo[0], dom.bc_hi[0]);
           const int sj = map_coord_host(j, dom.lo[1], dom.hi[1], dom.bc_lo[1], dom.bc_hi[1]);
           const int sk = map_coord_host(k, dom.lo[2], dom.hi[2], dom.bc_lo[2], dom.bc_hi[2]);
@@ -983,7 +1033,7 @@ amrs_status amrs_boxlist_set_bc(amrs_boxlist* bl, const int32_t bc_lo[3], const 
       if ((bc_lo[d] == -1) != (bc_hi[d] == -1)) return AMRS_ERR_BC;
       for (int s = 0; s < 2; ++s) {
         const int p = s ? bc_hi[d] : bc_lo[d];
-        if (p == 1 || p == 6 || p < -1 || p > 6) return AMRS_ERR_BC;
+        if (p < -1 || p > 6) return AMRS_ERR_BC;  // 1, 6: ext_dir, caller-filled
       }
       for (int b = 0; b < L.n; ++b)
         if (bn(L.boxes[b], d) < NGHOST && bc_lo[d] != -1 && bc_lo[d] != 2) return AMRS_ERR_BOX;
@@ -1006,7 +1056,7 @@ amrs_status amrs_boxlist_set_domain(amrs_boxlist* bl, const amrs_box* domain, co
     if ((bc_lo[d] == -1) != (bc_hi[d] == -1)) return AMRS_ERR_BC;
     for (int s = 0; s < 2; ++s) {
       const int p = s ? bc_hi[d] : bc_lo[d];
-      if (p == 1 || p == 6 || p < -1 || p > 6) return AMRS_ERR_BC;
+      if (p < -1 || p > 6) return AMRS_ERR_BC;  // 1, 6: ext_dir, caller-filled
     }
     // reflections and periodic images stay inside a domain of >= 3 cells
     if (bn(*domain, d) < NGHOST) return AMRS_ERR_BOX;
@@ -1016,6 +1066,20 @@ amrs_status amrs_boxlist_set_domain(amrs_boxlist* bl, const amrs_box* domain, co
   for (int b = 0; b < L.n; ++b)
     for (int d = 0; d < 3; ++d)
       if (L.boxes[b].lo[d] < dom.lo[d] || L.boxes[b].hi[d] > dom.hi[d]) return AMRS_ERR_BOX;
+  WallCfg w;
+  w.lo = bc_lo[1] == 6; w.hi = bc_hi[1] == 6; w.dom_lo = dom.lo[1]; w.dom_hi = dom.hi[1];
+  if (w.lo != L.wall.lo || w.hi != L.wall.hi || w.dom_lo != L.wall.dom_lo || w.dom_hi != L.wall.dom_hi) {
+    // the box records carry the wall rows: rebuild the tables with the current tiles
+    L.wall = w;
+    std::vector<int> tiles(3 * L.n);
+    for (int b = 0; b < L.n; ++b) {
+      tiles[3 * b] = L.hbox[b].tx; tiles[3 * b + 1] = L.hbox[b].ty; tiles[3 * b + 2] = L.hbox[b].kc;
+    }
+    std::lock_guard<std::mutex> lk(bl->h->mu);
+    CK(cudaSetDevice(bl->h->device));
+    CK(cudaDeviceSynchronize());
+    if (amrs_status s = relist_with_tiles(bl, tiles)) return s;
+  }
   std::vector<int> owner;
   if (amrs_status s = level_owner_table(L, dom, owner)) return s;
   CK(cudaSetDevice(bl->h->device));
@@ -1187,7 +1251,7 @@ amrs_status amrs_rhs_vjp_box(amrs_handle* h, const amrs_box* bx, const double dx
                              amrs_array4 vbar, amrs_array4 ubar, double* param_bar, void* stream) {
   if (!h || !bx || !dxinv) return AMRS_ERR_NULL;
   if (!box_ok(*bx)) return AMRS_ERR_BOX;
-  if (!vjp_scheme(h->sc)) return AMRS_ERR_SCHEME;
+  if (!vjp_scheme(h->sc) || h->wall.lo || h->wall.hi) return AMRS_ERR_SCHEME;
   if (!covers(state, *bx, NGHOST, NCONS) || !covers(vbar, *bx, 0, NCONS) || !covers(ubar, *bx, NGHOST, NCONS))
     return AMRS_ERR_LAYOUT;
   std::lock_guard<std::mutex> lk(h->mu);
@@ -1236,7 +1300,7 @@ amrs_status amrs_rk_stage_vjp_box(amrs_handle* h, const amrs_box* bx, const doub
                                   double* param_bar, void* stream) {
   if (!h || !bx || !dxinv || !prog || !bc_lo || !bc_hi) return AMRS_ERR_NULL;
   if (!box_ok(*bx)) return AMRS_ERR_BOX;
-  if (!vjp_scheme(h->sc)) return AMRS_ERR_SCHEME;
+  if (!vjp_scheme(h->sc) || h->wall.lo || h->wall.hi) return AMRS_ERR_SCHEME;
   if (!covers(stage_in, *bx, NGHOST, NCONS) || !covers(wbar, *bx, 0, NCONS) || !covers(s1bar, *bx, 0, NCONS) ||
       !covers(inbar, *bx, 0, NCONS))
     return AMRS_ERR_LAYOUT;

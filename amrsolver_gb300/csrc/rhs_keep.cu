@@ -76,7 +76,20 @@ __global__ void __launch_bounds__(256) visc_cell_kernel(BoxTable tb) {
       qzp[n] = Q.p[o + sz + n * sn];
     }
     double f[NVF];
-    viscous_cell(qc, qxm, qxp, qym, qyp, qzm, qzp, R.dxinv, tb.cls[R.cl], f);
+    if (R.walls && (j == R.wrow_lo || j == R.wrow_hi)) {
+      // ghost row of a code-6 y wall: one-sided y derivatives into the box
+      const int loc = (j == R.wrow_lo) ? 0 : 1;
+      const long long s1 = loc == 0 ? sy : -sy;
+      double q1[NQ], q2[NQ];
+#pragma unroll
+      for (int n = QU; n <= QT; ++n) {
+        q1[n] = Q.p[o + s1 + n * sn];
+        q2[n] = Q.p[o + 2 * s1 + n * sn];
+      }
+      viscous_wall_cell(loc, qc, qxm, qxp, q1, q2, qzm, qzp, R.dxinv, tb.cls[R.cl], f);
+    } else {
+      viscous_cell(qc, qxm, qxp, qym, qyp, qzm, qzp, R.dxinv, tb.cls[R.cl], f);
+    }
     const long long ov = R.vf.off(i, j, k);
 #pragma unroll
     for (int n = 0; n < NVF; ++n) R.vf.p[ov + n * R.vf.ns] = f[n];
@@ -363,15 +376,21 @@ keep_face_kernel(BoxTable tb, int s_in, int s_s1, int s_out, DProg prog, int rhs
             const int f = r / txw, col = r - (r / txw) * txw;
             ld_qs(qs, (f + H) * QP + col + 3, QS, q1);
             ld_qs(qs, (f - 1 + H) * QP + col + 3, QS, q2);
-            keep_pair<1>(q1, q2, coef[0], F);
+            const int jf = y0 + f;
+            if (R.walls && (jf <= R.red_lo || (jf >= R.red_hi && jf <= R.hi[1]))) {
+              // next to a code-6 y wall: second-order KEEP (halfsten 1, coefficient 1)
+              keep_pair<1>(q1, q2, 1.0, F);
+            } else {
+              keep_pair<1>(q1, q2, coef[0], F);
 #pragma unroll
-            for (int l = 2; l <= H; ++l)
+              for (int l = 2; l <= H; ++l)
 #pragma unroll
-              for (int m = 0; m < l; ++m) {
-                const double* src = tsy + (l - 2) * 5 * C::T_CAP + (f - l + m + l) * TX + col;
+                for (int m = 0; m < l; ++m) {
+                  const double* src = tsy + (l - 2) * 5 * C::T_CAP + (f - l + m + l) * TX + col;
 #pragma unroll
-                for (int n = 0; n < 5; ++n) F[n] = F[n] + src[n * C::T_CAP];
-              }
+                  for (int n = 0; n < 5; ++n) F[n] = F[n] + src[n * C::T_CAP];
+                }
+            }
             if (VISC) {
               const long long oR = VF.off(x0 + col, y0 + f, k);
 #pragma unroll

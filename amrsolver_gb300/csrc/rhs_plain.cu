@@ -78,19 +78,25 @@ __global__ void __launch_bounds__(256) keep_faces_plain_kernel(BoxTable tb, Face
     const BoxRec& R = tb.box[f.b];
     const DArr Q = R.q;
     const int di = f.d == 0, dj = f.d == 1, dk = f.d == 2;
+    // y faces next to a code-6 wall: second-order KEEP, coefficient 1
+    // (Flux_2nd_Order_KEEP, src/rhs/CentralKEEP.h:232-287)
+    const bool red = f.d == 1 && R.walls && (f.j <= R.red_lo || (f.j >= R.red_hi && f.j <= R.hi[1]));
+    const int hs = red ? 1 : H;
     double F[5] = {0, 0, 0, 0, 0};
 #pragma unroll
     for (int l = 1; l <= H; ++l)
 #pragma unroll
       for (int m = 0; m < l; ++m) {
+        if (l > hs) continue;
         double q1[NQ], q2[NQ], T[5];
         const long long o1 = Q.off(f.i + m * di, f.j + m * dj, f.k + m * dk);
         const long long o2 = Q.off(f.i + (m - l) * di, f.j + (m - l) * dj, f.k + (m - l) * dk);
 #pragma unroll
         for (int n = 0; n < NQ; ++n) { q1[n] = Q.p[o1 + n * Q.ns]; q2[n] = Q.p[o2 + n * Q.ns]; }
-        if (f.d == 0) keep_pair<0>(q1, q2, coef[l - 1], T);
-        else if (f.d == 1) keep_pair<1>(q1, q2, coef[l - 1], T);
-        else keep_pair<2>(q1, q2, coef[l - 1], T);
+        const double c = red ? 1.0 : coef[l - 1];
+        if (f.d == 0) keep_pair<0>(q1, q2, c, T);
+        else if (f.d == 1) keep_pair<1>(q1, q2, c, T);
+        else keep_pair<2>(q1, q2, c, T);
 #pragma unroll
         for (int n = 0; n < 5; ++n) F[n] = F[n] + T[n];
       }

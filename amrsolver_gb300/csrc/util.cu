@@ -30,6 +30,13 @@ __device__ __forceinline__ int map_coord(int c, int lo, int hi, int bcl, int bch
   return low ? 2 * lo - c - 1 : 2 * hi - c + 1;
 }
 
+// A ghost coordinate beyond an ext_dir side (codes 1 inflow and 6
+// user-defined: the problem's bcnormal fills those cells, src/set/bcs.cpp):
+// the library leaves such cells, corners included, as the caller stored them.
+__device__ __forceinline__ bool ext_dir_ghost(int c, int lo, int hi, int bcl, int bch) {
+  return (c < lo && (bcl == 1 || bcl == 6)) || (c > hi && (bch == 1 || bch == 6));
+}
+
 __global__ void __launch_bounds__(256) halo_kernel(HaloBox hb) {
   const int g = NGHOST;
   const int nx = hb.hi[0] - hb.lo[0] + 1 + 2 * g, ny = hb.hi[1] - hb.lo[1] + 1 + 2 * g,
@@ -44,6 +51,10 @@ __global__ void __launch_bounds__(256) halo_kernel(HaloBox hb) {
     const bool inside = i >= hb.lo[0] && i <= hb.hi[0] && j >= hb.lo[1] && j <= hb.hi[1] && k >= hb.lo[2] &&
                         k <= hb.hi[2];
     if (inside) continue;
+    if (ext_dir_ghost(i, hb.lo[0], hb.hi[0], hb.bc_lo[0], hb.bc_hi[0]) ||
+        ext_dir_ghost(j, hb.lo[1], hb.hi[1], hb.bc_lo[1], hb.bc_hi[1]) ||
+        ext_dir_ghost(k, hb.lo[2], hb.hi[2], hb.bc_lo[2], hb.bc_hi[2]))
+      continue;
     for (int n = 0; n < hb.ncomp; ++n) {
       bool flip = false;
       const int si = map_coord(i, hb.lo[0], hb.hi[0], hb.bc_lo[0], hb.bc_hi[0], n, 0, flip);
@@ -74,6 +85,9 @@ __global__ void __launch_bounds__(256) halo_list_kernel(BoxTable tb, const long 
     const bool inside = i >= R.lo[0] && i <= R.hi[0] && j >= R.lo[1] && j <= R.hi[1] && k >= R.lo[2] &&
                         k <= R.hi[2];
     if (inside) continue;
+    if (ext_dir_ghost(i, R.lo[0], R.hi[0], bl0, bh0) || ext_dir_ghost(j, R.lo[1], R.hi[1], bl1, bh1) ||
+        ext_dir_ghost(k, R.lo[2], R.hi[2], bl2, bh2))
+      continue;
     const DArr U = R.slot[slot];
     for (int n = 0; n < NCONS; ++n) {
       bool flip = false;

@@ -112,6 +112,18 @@ typedef struct amrs_handle amrs_handle;
 amrs_status amrs_create(amrs_handle** out, const amrs_scheme* scheme, const amrs_closures* closures, int device);
 amrs_status amrs_destroy(amrs_handle* h);
 amrs_status amrs_set_closures(amrs_handle* h, const amrs_closures* closures);
+/* The physical domain and boundary codes (cns.lo_bc / cns.hi_bc) of the
+ * level the handle's per-box calls work on; NULL arguments clear them.
+ * y sides with code 6 (user-defined wall) switch on the reference's wall
+ * treatment in compute_rhs (src/tim/CNS_advance.cpp:226-229, :300-333) for
+ * boxes that touch them: the KEEP y faces of the order_keep/2 planes next to
+ * the wall take the second-order pair (Flux_2nd_Order_KEEP,
+ * src/rhs/CentralKEEP.h:232-287) and the viscous cell fluxes of the wall's
+ * ghost row use one-sided y derivatives (ViscousWallFluxes,
+ * src/rhs/CNS_hydro_K.h:177-251).  Ghost cells beyond code-1/6 sides are the
+ * caller's (the problem's bcnormal fills them); the library's fills leave
+ * them untouched.  The VJP entry points reject a handle with walls. */
+amrs_status amrs_set_domain(amrs_handle* h, const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3]);
 const char* amrs_status_string(amrs_status s);
 /* Last CUDA error string recorded by the library (thread-local). */
 const char* amrs_last_cuda_error(void);

@@ -861,7 +861,8 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
 // then z) over the whole ghost region.  bc code per side: -1 periodic,
 // 2 outflow (foextrap), 3/4 symmetry/slip wall (reflect_even, normal
 // velocity reflect_odd), 5 no-slip (reflect_even, all velocities reflect_odd).
-// Codes 1 and 6 (ext_dir through the problem's bcnormal) are not supported.
+// Codes 1 and 6 (ext_dir through the problem's bcnormal) leave the cells
+// beyond those sides, corners included, as the caller stored them.
 enum BCT { BC_INT = 0, BC_FOEXTRAP = 2, BC_EVEN = 3, BC_ODD = 4 };
 
 inline int comp_bc_type(int phys, int comp, int dir) {
@@ -883,6 +884,15 @@ void fill_halo_box(const Box& dom, const int bc_lo[3], const int bc_hi[3], R* up
   Arr<R> u = make_arr<R>(uptr, dom, g);
   int glo[3], ghi[3];
   for (int d = 0; d < 3; ++d) { glo[d] = dom.lo[d] - g; ghi[d] = dom.hi[d] + g; }
+  // cells beyond an ext_dir side (codes 1, 6: the problem's bcnormal fills
+  // them, src/set/bcs.cpp) are the caller's and are not touched here
+  auto ext_dir = [&](const int c[3]) {
+    for (int d = 0; d < 3; ++d) {
+      if (c[d] < dom.lo[d] && (bc_lo[d] == 1 || bc_lo[d] == 6)) return true;
+      if (c[d] > dom.hi[d] && (bc_hi[d] == 1 || bc_hi[d] == 6)) return true;
+    }
+    return false;
+  };
   // periodic directions: image of every ghost cell whose other coordinates are
   // inside the domain or already filled; applying directions in order and
   // sweeping the full ghost extent of earlier directions reproduces the corner
@@ -898,6 +908,7 @@ void fill_halo_box(const Box& dom, const int bc_lo[3], const int bc_hi[3], R* up
         for (int i = glo[0]; i <= ghi[0]; ++i) {
           int c[3] = {i, j, k};
           if (c[d] >= dom.lo[d] && c[d] <= dom.hi[d]) continue;
+          if (ext_dir(c)) continue;
           int s[3] = {i, j, k};
           s[d] = (c[d] < dom.lo[d]) ? c[d] + n : c[d] - n;
           for (int m = 0; m < ncomp; ++m) u(i, j, k, m) = u(s[0], s[1], s[2], m);
@@ -906,7 +917,7 @@ void fill_halo_box(const Box& dom, const int bc_lo[3], const int bc_hi[3], R* up
   for (int d = 0; d < 3; ++d) {
     for (int side = 0; side < 2; ++side) {
       const int phys = side ? bc_hi[d] : bc_lo[d];
-      if (phys == -1 || phys == 0) continue;
+      if (phys == -1 || phys == 0 || phys == 1 || phys == 6) continue;
 #ifdef _OPENMP
       #pragma omp parallel for schedule(static) if (u.ns > 100000)
 #endif
@@ -915,7 +926,7 @@ void fill_halo_box(const Box& dom, const int bc_lo[3], const int bc_hi[3], R* up
           for (int i = glo[0]; i <= ghi[0]; ++i) {
             int c[3] = {i, j, k};
             const bool outside = side ? (c[d] > dom.hi[d]) : (c[d] < dom.lo[d]);
-            if (!outside) continue;
+            if (!outside || ext_dir(c)) continue;
             for (int m = 0; m < ncomp; ++m) {
               const int t = comp_bc_type(phys, m, d);
               int s[3] = {i, j, k};
@@ -1122,7 +1133,7 @@ int orc_fill_halo(const int* lo, const int* hi, const int* bc_lo, const int* bc_
     if ((bc_lo[d] == -1) != (bc_hi[d] == -1)) return 3;
     for (int s = 0; s < 2; ++s) {
       int p = s ? bc_hi[d] : bc_lo[d];
-      if (p == 1 || p == 6 || p < -1 || p > 6) return 4;
+      if (p < -1 || p > 6) return 4;  // 1, 6: ext_dir, cells left to the caller
     }
   }
   fill_halo_box<double>(to_box(lo, hi), bc_lo, bc_hi, U, ncomp);
@@ -1168,18 +1179,14 @@ int orc_advance(const OrcScheme* s, const OrcClosures* c, const int* lo, const i
           for (int i = b.lo[0]; i <= b.hi[0]; ++i) a2(i, j, k, n) = a1(i, j, k, n);
   }
   for (int is = 0; is < ns; ++is) {
-    // FillPatch: copy the source state's valid cells, then fill ghosts
-    Arr<double>& src = st[is].src ? a2 : a1;
-#ifdef _OPENMP
-#pragma omp parallel for collapse(2) num_threads(nthreads > 0 ? nthreads : 1) schedule(static)
-#endif
-    for (int n = 0; n < NCONS; ++n)
-      for (int k = b.lo[2]; k <= b.hi[2]; ++k)
-        for (int j = b.lo[1]; j <= b.hi[1]; ++j)
-          for (int i = b.lo[0]; i <= b.hi[0]; ++i) ab(i, j, k, n) = src(i, j, k, n);
+    // FillPatch: copy the source state (ghost cells beyond ext_dir sides, the
+    // caller's, come with it), then fill the other ghosts
+    std::memcpy(sborder.data(), st[is].src ? S2 : S1, sizeof(double) * ng * NCONS);
     int rc = orc_fill_halo(lo, hi, bc_lo, bc_hi, sborder.data(), NCONS);
     if (rc) return rc;
-    compute_rhs_box<double>(sc, cl, b, dxinv, sborder.data(), ds.data(), nthreads);
+    // code-6 y sides of this single-box domain are walls
+    Walls w{bc_lo && bc_lo[1] == 6, bc_hi && bc_hi[1] == 6, b.lo[1], b.hi[1]};
+    compute_rhs_box<double>(sc, cl, b, dxinv, sborder.data(), ds.data(), nthreads, &w);
 #ifdef _OPENMP
 #pragma omp parallel for collapse(2) num_threads(nthreads > 0 ? nthreads : 1) schedule(static)
 #endif

@@ -165,7 +165,9 @@ class Oracle:
                 lo=(0, 0, 0), nthreads=1):
         """One CNS::advance step; returns S2 (ghosted; valid cells meaningful)."""
         S1 = np.ascontiguousarray(S1, dtype=np.float64).copy()
-        S2 = np.zeros_like(S1)
+        # S2 starts as S1: its ghost cells beyond ext_dir sides (codes 1, 6)
+        # are the caller's values, as in every state buffer of a level
+        S2 = S1.copy()
         nz, ny, nx = (s - 2 * NG for s in S1.shape[1:])
         hi = (lo[0] + nx - 1, lo[1] + ny - 1, lo[2] + nz - 1)
         sc, cl = c_scheme(scheme), c_closures(closures)

@@ -156,6 +156,8 @@ def test_bad_inputs_fail_loudly():
     with pytest.raises(capi.AmrsError):
         h.rhs_box(U, (1.0, 1.0, 1.0), out)
     with pytest.raises(capi.AmrsError):
-        capi.fill_halo_box(U, (1, -1, -1), (1, -1, -1))  # inflow needs the problem's bcnormal
+        capi.fill_halo_box(U, (7, -1, -1), (7, -1, -1))  # no such boundary code
+    with pytest.raises(capi.AmrsError):
+        capi.fill_halo_box(U, (-1, -1, -1), (2, -1, -1))  # periodic on one side only
     with pytest.raises(capi.AmrsError):
         capi.Handle(P.Scheme(flux_euler=1, order_keep=3), P.Closures.nondimensional(1e-3))

@@ -90,6 +90,12 @@ SIGNATURES = {
     "amrs_rk_step_boxlist": (_S, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_int32,
                                   ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P,
                                   ctypes.POINTER(ctypes.c_int32)]),
+    "amrs_rk_run_boxlist": (_S, [_P, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                 ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                 ctypes.c_int32, _P]),
+    "amrs_boxlist_run_state": (_S, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(ctypes.c_int32), _P]),
+    "amrs_boxlist_totals": (_S, [_P, ctypes.c_int32, ctypes.c_double, _P, _P]),
     "amrs_rhs_vjp_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double), Array4, Array4, Array4,
                               _P, _P]),
     "amrs_fill_halo_box_adjoint": (_S, [ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_int32),
@@ -376,3 +382,24 @@ class BoxList:
 
     def tma_enabled(self):
         return int(self._L.amrs_boxlist_tma_enabled(self.bl))
+
+    def run(self, order_rk, stages_rk, stop_time, max_steps, cfl=0.0, dt=0.0, time=0.0, s1=0, w1=1, w2=2,
+            stream=None):
+        """amrs_rk_run_boxlist: the whole time loop as one device launch
+        (CFL-controlled dt when cfl > 0, else fixed dt); state in slot s1."""
+        check(self._L.amrs_rk_run_boxlist(self.bl, order_rk, stages_rk, float(cfl), float(dt), float(time),
+                                          float(stop_time), int(max_steps), s1, w1, w2, _stream_ptr(stream)),
+              "amrs_rk_run_boxlist")
+
+    def run_state(self, stream=None):
+        """(time, dt, steps) of the last run (host-synchronising)."""
+        t, d, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
+        check(self._L.amrs_boxlist_run_state(self.bl, ctypes.byref(t), ctypes.byref(d), ctypes.byref(n),
+                                             _stream_ptr(stream)), "amrs_boxlist_run_state")
+        return t.value, d.value, n.value
+
+    def totals(self, slot, scale, out, stream=None):
+        """Conserved totals of `slot` times `scale` into the cuda tensor `out` (5 doubles)."""
+        check(self._L.amrs_boxlist_totals(self.bl, slot, float(scale), ctypes.c_void_p(out.data_ptr()),
+                                          _stream_ptr(stream)), "amrs_boxlist_totals")
+        return out

@@ -38,7 +38,12 @@ struct BoxTable {
   const DClosures* cls;
   int n;
   int gq;                  // ghost depth of the primitive region
+  // device-resident time loop: every kernel of a step returns at once while
+  // *active == 0 (steps after the stop time); null outside such loops
+  const int* active;
 };
+
+__device__ __forceinline__ bool list_idle(const BoxTable& tb) { return tb.active && *tb.active == 0; }
 
 __device__ __forceinline__ int find_box_ll(const long long* pref, int n, long long x) {
   int lo = 0, hi = n;  // pref[lo] <= x < pref[hi]

@@ -183,14 +183,36 @@ __device__ __forceinline__ void viscous_wall_cell(int loc, const double* qc, con
 }
 
 // RK stage program (AMReX BLAS-1 semantics), registers S1, S2, dS.
+// fa/fb: 0 the coefficient is a / b; 1 it is dt * a / dt * b; 2 it is
+// dt / a / dt / b, with dt read from device memory (dtp) when the kernel
+// starts: the device-resident time loop changes dt without new launches.
 struct DOp {
   int kind, dst, x, y;
   double a, b;
+  int fa, fb;
 };
 struct DProg {
   int nops;
   DOp ops[3];
+  const double* dtp;
 };
+
+__device__ __forceinline__ double dt_coef(int form, double c, double dt) {
+  return form == 1 ? dt * c : (form == 2 ? dt / c : c);
+}
+// The program with its dt-dependent coefficients evaluated (dt * c and
+// dt / c round exactly as the host's CNS::advance arithmetic).
+__device__ __forceinline__ DProg resolve_prog(DProg p) {
+  if (p.dtp) {
+    const double dt = *p.dtp;
+#pragma unroll
+    for (int o = 0; o < 3; ++o) {
+      p.ops[o].a = dt_coef(p.ops[o].fa, p.ops[o].a, dt);
+      p.ops[o].b = dt_coef(p.ops[o].fb, p.ops[o].b, dt);
+    }
+  }
+  return p;
+}
 
 __device__ __forceinline__ void apply_prog(const DProg& p, double reg[3]) {
 #pragma unroll

@@ -83,6 +83,21 @@ cudaError_t launch_adj_prog(const BoxRec& R, const DProg& prog, const DArr& wbar
 cudaError_t launch_adj_halo(const HaloBox& hb, int nsm, cudaStream_t st);
 cudaError_t launch_halo_list(const BoxTable& tb, const long long* gpre, long long total, int slot, const int bc_lo[3],
                              const int bc_hi[3], int nsm, cudaStream_t st);
+// Device state of a time loop over a box list (amrs_rk_run_boxlist); the
+// list's kernels read `active` through BoxTable::active.
+struct RunCtl {
+  double time, dt, stop, cfl, change_max;
+  int step, max_steps, use_cfl, active;
+  unsigned long long bits;  // cns_estdt reduction cell (ordered bits of the minimum)
+};
+cudaError_t launch_run_estdt(const BoxTable& tb, int s_in, long long nvalid, RunCtl* c, int nsm, cudaStream_t st);
+cudaError_t launch_run_step_done(RunCtl* c, cudaGraphConditionalHandle cond, cudaStream_t st);
+cudaError_t launch_run_begin(RunCtl* c, cudaStream_t st);
+cudaError_t launch_copy_slot(const BoxTable& tb, int from, int to, long long nvalid, int nsm, cudaStream_t st);
+int totals_blocks(long long nvalid, int nsm);
+cudaError_t launch_totals(const BoxTable& tb, int slot, long long nvalid, double scale, double* part, double* out,
+                          int nsm, cudaStream_t st);
+
 // domain of a level whose boxes tile it, with its physical boundary codes
 struct LevelDomain {
   int lo[3], hi[3];

@@ -134,6 +134,70 @@ double face_plane_cost(int H, int txw, int tyw) {
   return 1.0 + H + rounds(nxy) + 1.5 * rounds(nf) + 0.5;
 }
 
+// Stage programs of CNS::advance (src/tim/CNS_advance.cpp:51-166) for
+// (order_rk, stages_rk): numeric coefficients for `dt` into `st`, and, when
+// `forms` is given, the same programs with every dt-dependent coefficient
+// kept as its form (dt * c or dt / c, exactly as the reference writes it)
+// for kernels that read dt from device memory.
+struct Cf {
+  int f;     // 0 constant c, 1 dt * c, 2 dt / c
+  double c;
+};
+double cf_val(Cf x, double dt) { return x.f == 1 ? dt * x.c : (x.f == 2 ? dt / x.c : x.c); }
+
+amrs_status rk_build(int order_rk, int stages_rk, double dt, amrs_stage_prog* st, int cap, int32_t* nstages,
+                     DProg* forms) {
+  const Cf K0{0, 0.0}, DT{1, 1.0};
+  auto K = [](double v) { return Cf{0, v}; };
+  const int S1 = 0, S2 = 1, DS = 2;
+  int n = -1;
+  if (order_rk == -2) n = 2;
+  else if (order_rk == 0 || order_rk == 1) n = 1;
+  else if (order_rk == 2) n = (stages_rk >= 2) ? stages_rk : -1;
+  else if (order_rk == 3 && (stages_rk == 3 || stages_rk == 4)) n = stages_rk;
+  if (n < 0) return AMRS_ERR_RK;
+  if (n > cap) return AMRS_ERR_SIZE;
+  std::memset(st, 0, sizeof(amrs_stage_prog) * n);
+  if (forms) std::memset(forms, 0, sizeof(DProg) * n);
+  auto op = [&](int i, int j, int kind, int dst, int x, int y, Cf a, Cf b) {
+    amrs_rk_op& o = st[i].ops[j];
+    o.kind = kind; o.dst = dst; o.x = x; o.y = y; o.a = cf_val(a, dt); o.b = cf_val(b, dt);
+    if (forms) {
+      DOp& d = forms[i].ops[j];
+      d.kind = kind; d.dst = dst; d.x = x; d.y = y; d.a = a.c; d.b = b.c; d.fa = a.f; d.fb = b.f;
+    }
+  };
+  auto set = [&](int i, int src, int nops) {
+    st[i].src_state = src; st[i].nops = nops;
+    if (forms) forms[i].nops = nops;
+  };
+  if (order_rk == -2) {  // src/tim/CNS_advance.cpp:51-70
+    set(0, 0, 1); op(0, 0, 0, S2, S1, DS, K(1.0), DT);
+    set(1, 1, 2); op(1, 0, 0, S2, S2, S1, K(0.5), K(0.5)); op(1, 1, 1, S2, DS, 0, Cf{1, 0.5}, K0);
+  } else if (order_rk == 0) {  // :71-75
+    set(0, 0, 1); op(0, 0, 3, S2, DS, 0, K0, K0);
+  } else if (order_rk == 1) {  // :76-80
+    set(0, 0, 1); op(0, 0, 0, S2, S1, DS, K(1.0), DT);
+  } else if (order_rk == 2) {  // :81-114
+    const int m = stages_rk;
+    for (int i = 1; i <= m - 1; ++i) { set(i - 1, i == 1 ? 0 : 1, 1); op(i - 1, 0, 1, S2, DS, 0, Cf{2, double(m - 1)}, K0); }
+    set(m - 1, 1, 2);
+    op(m - 1, 0, 0, S2, S2, DS, K(double(m - 1)), DT);
+    op(m - 1, 1, 0, S2, S1, S2, K(1.0 / m), K(1.0 / m));
+  } else if (stages_rk == 3) {  // :118-139
+    set(0, 0, 1); op(0, 0, 0, S2, S1, DS, K(1.0), DT);
+    set(1, 1, 2); op(1, 0, 2, DS, S2, 0, DT, K0); op(1, 1, 0, S2, S1, DS, K(3.0 / 4), K(1.0 / 4));
+    set(2, 1, 2); op(2, 0, 2, DS, S2, 0, DT, K0); op(2, 1, 0, S2, S1, DS, K(1.0 / 3), K(2.0 / 3));
+  } else {  // :141-166
+    set(0, 0, 1); op(0, 0, 0, S2, S1, DS, K(1.0), Cf{2, 2.0});
+    set(1, 1, 1); op(1, 0, 1, S2, DS, 0, Cf{2, 2.0}, K0);
+    set(2, 1, 2); op(2, 0, 0, S2, S1, S2, K(2.0 / 3), K(1.0 / 3)); op(2, 1, 1, S2, DS, 0, Cf{2, 6.0}, K0);
+    set(3, 1, 1); op(3, 0, 1, S2, DS, 0, Cf{2, 2.0}, K0);
+  }
+  *nstages = n;
+  return AMRS_OK;
+}
+
 // y sides of the domain with boundary code 6 (user-defined walls) and the
 // domain's y extent: the reference's wall treatment in compute_rhs
 // (src/tim/CNS_advance.cpp:226-229, :300-333) for boxes that touch them.
@@ -193,7 +257,17 @@ struct List {
   LevelDomain dom{};
   int* d_owner = nullptr;  // has_bc == 2: owning box of every grown cell's source (-1: valid cell)
   WallCfg wall{};          // code-6 y walls of the list's domain (amrs_boxlist_set_domain)
+  // device-resident time loop (amrs_rk_run_boxlist)
+  RunCtl* d_run = nullptr;
+  RunCtl h_run{};
+  cudaGraphExec_t run_graph = nullptr;
+  int run_key[6] = {0, 0, 0, 0, 0, 0};
+  double* d_tot = nullptr;  // per-block partial sums of amrs_boxlist_totals
+  size_t d_tot_n = 0;
   ~List() {
+    if (run_graph) cudaGraphExecDestroy(run_graph);
+    if (d_run) cudaFree(d_run);
+    if (d_tot) cudaFree(d_tot);
     if (graph) cudaGraphExecDestroy(graph);
     if (dtab) cudaFree(dtab);
     if (dscr) cudaFree(dscr);
@@ -708,44 +782,7 @@ amrs_status amrs_set_domain(amrs_handle* h, const amrs_box* domain, const int32_
 amrs_status amrs_rk_program(int32_t order_rk, int32_t stages_rk, double dt, amrs_stage_prog* st, int32_t cap,
                             int32_t* nstages) {
   if (!st || !nstages) return AMRS_ERR_NULL;
-  auto op = [](int kind, int dst, int x, int y, double a, double b) {
-    amrs_rk_op o; o.kind = kind; o.dst = dst; o.x = x; o.y = y; o.a = a; o.b = b; return o;
-  };
-  auto set = [&](int i, int src, int nops, amrs_rk_op a, amrs_rk_op b = amrs_rk_op{}) {
-    st[i].src_state = src; st[i].nops = nops; st[i].ops[0] = a; st[i].ops[1] = b;
-  };
-  const int S1 = 0, S2 = 1, DS = 2;
-  int n = -1;
-  if (order_rk == -2) n = 2;
-  else if (order_rk == 0 || order_rk == 1) n = 1;
-  else if (order_rk == 2) n = (stages_rk >= 2) ? stages_rk : -1;
-  else if (order_rk == 3 && (stages_rk == 3 || stages_rk == 4)) n = stages_rk;
-  if (n < 0) return AMRS_ERR_RK;
-  if (n > cap) return AMRS_ERR_SIZE;
-  std::memset(st, 0, sizeof(amrs_stage_prog) * n);
-  if (order_rk == -2) {  // src/tim/CNS_advance.cpp:51-70
-    set(0, 0, 1, op(0, S2, S1, DS, 1.0, dt));
-    set(1, 1, 2, op(0, S2, S2, S1, 0.5, 0.5), op(1, S2, DS, 0, 0.5 * dt, 0));
-  } else if (order_rk == 0) {  // :71-75
-    set(0, 0, 1, op(3, S2, DS, 0, 0, 0));
-  } else if (order_rk == 1) {  // :76-80
-    set(0, 0, 1, op(0, S2, S1, DS, 1.0, dt));
-  } else if (order_rk == 2) {  // :81-114
-    const int m = stages_rk;
-    for (int i = 1; i <= m - 1; ++i) set(i - 1, i == 1 ? 0 : 1, 1, op(1, S2, DS, 0, dt / double(m - 1), 0));
-    set(m - 1, 1, 2, op(0, S2, S2, DS, double(m - 1), dt), op(0, S2, S1, S2, 1.0 / m, 1.0 / m));
-  } else if (stages_rk == 3) {  // :118-139
-    set(0, 0, 1, op(0, S2, S1, DS, 1.0, dt));
-    set(1, 1, 2, op(2, DS, S2, 0, dt, 0), op(0, S2, S1, DS, 3.0 / 4, 1.0 / 4));
-    set(2, 1, 2, op(2, DS, S2, 0, dt, 0), op(0, S2, S1, DS, 1.0 / 3, 2.0 / 3));
-  } else {  // :141-166
-    set(0, 0, 1, op(0, S2, S1, DS, 1.0, dt / 2));
-    set(1, 1, 1, op(1, S2, DS, 0, dt / 2, 0));
-    set(2, 1, 2, op(0, S2, S1, S2, 2.0 / 3, 1.0 / 3), op(1, S2, DS, 0, dt / 6, 0));
-    set(3, 1, 1, op(1, S2, DS, 0, dt / 2, 0));
-  }
-  *nstages = n;
-  return AMRS_OK;
+  return rk_build(order_rk, stages_rk, dt, st, cap, nstages, nullptr);
 }
 
 amrs_status amrs_rhs_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3], amrs_array4 state,
@@ -1166,6 +1203,123 @@ amrs_status amrs_rk_step_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t sta
   }
   CK(cudaGraphLaunch(L.graph, st));
   *result_slot = L.graph_result;
+  return AMRS_OK;
+}
+
+amrs_status amrs_rk_run_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t stages_rk, double cfl, double dt,
+                                double time, double stop_time, int32_t max_steps, int32_t s1, int32_t w1, int32_t w2,
+                                void* stream) {
+  if (!bl) return AMRS_ERR_NULL;
+  List& L = bl->L;
+  amrs_handle* h = bl->h;
+  if (s1 < 0 || w1 < 0 || w2 < 0 || s1 >= L.nslots || w1 >= L.nslots || w2 >= L.nslots || s1 == w1 || s1 == w2 ||
+      w1 == w2 || max_steps < 0)
+    return AMRS_ERR_SIZE;
+  const int use_cfl = cfl > 0.0 ? 1 : 0;
+  if (!use_cfl && !(dt > 0.0)) return AMRS_ERR_SIZE;
+  amrs_stage_prog st16[16];
+  DProg forms[16];
+  int32_t ns = 0;
+  if (amrs_status s = rk_build(order_rk, stages_rk, 1.0, st16, 16, &ns, forms)) return s;
+  CK(cudaSetDevice(h->device));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!L.d_run) CK(cudaMalloc(&L.d_run, sizeof(RunCtl)));
+  const int key[6] = {order_rk, stages_rk, s1, w1, w2, use_cfl};
+  if (!L.run_graph || std::memcmp(key, L.run_key, sizeof(key)) != 0) {
+    if (L.run_graph) { CK(cudaStreamSynchronize(st)); cudaGraphExecDestroy(L.run_graph); L.run_graph = nullptr; }
+    // outer graph: one conditional WHILE node whose body is one step
+    cudaGraph_t g = nullptr;
+    CK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle cond;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+    cudaStream_t cs = nullptr;
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+      e = cudaStreamBeginCaptureToGraph(cs, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeThreadLocal);
+    amrs_status rs = AMRS_OK;
+    if (e == cudaSuccess) {
+      // every kernel of the body returns at once while the loop is inactive
+      const BoxTable saved = L.tb;
+      L.tb.active = &L.d_run->active;
+      int cur = s1;
+      const int outs[2] = {w1, w2};
+      int which = 0;
+      for (int i = 0; i < ns && rs == AMRS_OK && e == cudaSuccess; ++i) {
+        const int in = (st16[i].src_state == 0) ? s1 : cur;
+        int out = outs[which];
+        if (out == in) { which ^= 1; out = outs[which]; }
+        if (L.has_bc) e = list_fill(h, L, in, cs);
+        DProg pr = forms[i];
+        pr.dtp = &L.d_run->dt;
+        if (e == cudaSuccess) rs = list_stage(h, L, pr, in, s1, out, 0, cs);
+        cur = out;
+        which ^= 1;
+      }
+      if (e == cudaSuccess && rs == AMRS_OK && cur != s1) e = launch_copy_slot(L.tb, cur, s1, L.tot_valid, h->nsm, cs);
+      if (e == cudaSuccess && rs == AMRS_OK && use_cfl) e = launch_run_estdt(L.tb, s1, L.tot_valid, L.d_run, h->nsm, cs);
+      if (e == cudaSuccess && rs == AMRS_OK) e = launch_run_step_done(L.d_run, cond, cs);
+      L.tb = saved;
+      cudaGraph_t body = nullptr;
+      const cudaError_t e2 = cudaStreamEndCapture(cs, &body);
+      if (e == cudaSuccess) e = e2;
+    }
+    if (cs) cudaStreamDestroy(cs);
+    if (e == cudaSuccess && rs == AMRS_OK) e = cudaGraphInstantiate(&L.run_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (rs) return rs;
+    if (e != cudaSuccess) return cuda_fail(e, "amrs_rk_run_boxlist graph");
+    std::memcpy(L.run_key, key, sizeof(key));
+  }
+  // loop state, initial dt, then the whole run as one launch
+  RunCtl& c = L.h_run;
+  c.time = time; c.dt = use_cfl ? 0.0 : dt; c.stop = stop_time; c.cfl = cfl; c.change_max = 1.1;
+  c.step = 0; c.max_steps = max_steps; c.use_cfl = use_cfl; c.active = 0; c.bits = ~0ull;
+  CK(cudaMemcpyAsync(L.d_run, &c, sizeof(RunCtl), cudaMemcpyHostToDevice, st));
+  if (use_cfl) {
+    // computeInitialDt on the initial state (the list's kernels unguarded here)
+    CK(launch_run_estdt(L.tb, s1, L.tot_valid, L.d_run, h->nsm, st));
+  }
+  CK(launch_run_begin(L.d_run, st));
+  CK(cudaGraphLaunch(L.run_graph, st));
+  return AMRS_OK;
+}
+
+amrs_status amrs_boxlist_run_state(amrs_boxlist* bl, double* time, double* dt, int32_t* steps, void* stream) {
+  if (!bl || !time || !dt || !steps) return AMRS_ERR_NULL;
+  List& L = bl->L;
+  if (!L.d_run) return AMRS_ERR_STATE;
+  CK(cudaSetDevice(bl->h->device));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  RunCtl c{};
+  CK(cudaMemcpyAsync(&c, L.d_run, sizeof(RunCtl), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  *time = c.time;
+  *dt = c.dt;
+  *steps = c.step;
+  return AMRS_OK;
+}
+
+amrs_status amrs_boxlist_totals(amrs_boxlist* bl, int32_t slot, double scale, double* totals, void* stream) {
+  if (!bl || !totals) return AMRS_ERR_NULL;
+  List& L = bl->L;
+  if (slot < 0 || slot >= L.nslots) return AMRS_ERR_SIZE;
+  CK(cudaSetDevice(bl->h->device));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t need = (size_t)totals_blocks(L.tot_valid, bl->h->nsm) * NCONS;
+  if (need > L.d_tot_n) {
+    if (L.d_tot) { CK(cudaStreamSynchronize(st)); cudaFree(L.d_tot); L.d_tot = nullptr; L.d_tot_n = 0; }
+    CK(cudaMalloc(&L.d_tot, need * sizeof(double)));
+    L.d_tot_n = need;
+  }
+  CK(launch_totals(L.tb, slot, L.tot_valid, scale, L.d_tot, totals, bl->h->nsm, st));
   return AMRS_OK;
 }
 

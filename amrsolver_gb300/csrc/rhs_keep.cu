@@ -23,6 +23,7 @@ namespace amrs {
 
 // ------------------------------------------------------------- prims ----
 __global__ void __launch_bounds__(256) prims_kernel(BoxTable tb, int s_in) {
+  if (list_idle(tb)) return;
   const long long total = tb.pcell[tb.n];
   const int g = tb.gq;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < total;
@@ -50,6 +51,7 @@ __global__ void __launch_bounds__(256) prims_kernel(BoxTable tb, int s_in) {
 
 // ------------------------------------------------- viscous cell fluxes ----
 __global__ void __launch_bounds__(256) visc_cell_kernel(BoxTable tb) {
+  if (list_idle(tb)) return;
   const long long total = tb.vcell[tb.n];
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < total;
        c += (long long)gridDim.x * blockDim.x) {
@@ -128,10 +130,12 @@ __device__ __forceinline__ void ld_qs(const double* buf, int idx, int QS, double
 // One work item = one (tx x ty) column tile of one box over a chunk of z.
 template <int ORDER, bool VISC>
 __global__ void __launch_bounds__(F_THREADS, (ORDER == 6) ? 1 : 2)
-keep_face_kernel(BoxTable tb, int s_in, int s_s1, int s_out, DProg prog, int rhs_only, TmaDesc tma,
+keep_face_kernel(BoxTable tb, int s_in, int s_s1, int s_out, DProg prog_in, int rhs_only, TmaDesc tma,
                  int* err) {
   using C = KeepCfg<ORDER>;
   constexpr int H = C::H;
+  if (list_idle(tb)) return;  // uniform over the CTA: before any barrier
+  const DProg prog = resolve_prog(prog_in);
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double* smem = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
   double* qsbuf = smem;                                   // [2][NQ][QS_CAP]

@@ -66,6 +66,7 @@ static int grid_for(long long n, int nsm) {
 // reference's (l, m) order without sharing between faces.
 template <int ORDER>
 __global__ void __launch_bounds__(256) keep_faces_plain_kernel(BoxTable tb, FaceTable ft, long long total) {
+  if (list_idle(tb)) return;
   constexpr int H = ORDER / 2;
   double coef[3];
   if (ORDER == 6) { coef[0] = 6.0 / 4; coef[1] = -6.0 / 20; coef[2] = 2.0 / 60; }
@@ -110,6 +111,7 @@ __global__ void __launch_bounds__(256) keep_faces_plain_kernel(BoxTable tb, Face
 // ------------------------------------------------------------- WENO5 ----
 // Physical Euler fluxes + max eigenvalue: src/rhs/High_resolution.h:83-121.
 __global__ void __launch_bounds__(256) weno_flux_lambda_kernel(BoxTable tb, FaceTable ft, int s_in, long long total) {
+  if (list_idle(tb)) return;
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
        g += (long long)gridDim.x * blockDim.x) {
     const int b = find_box_ll(ft.gpre, tb.n, g);
@@ -214,6 +216,7 @@ __device__ __forceinline__ double weno5js_cd(const double t0, const double t1, c
 // 0.5 (f +- alpha U) enter weno5js_cd doubled as fma(+-alpha, U, f).
 template <bool REF_ORDER>
 __global__ void __launch_bounds__(256) weno_face_kernel(BoxTable tb, FaceTable ft, int s_in, long long total) {
+  if (list_idle(tb)) return;
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
        g += (long long)gridDim.x * blockDim.x) {
     FaceIdx f;
@@ -294,6 +297,7 @@ __device__ __forceinline__ double mc_limiter(double dlft, double drgt) {
 __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, const long long* spre0,
                                                     const long long* spre1, const long long* spre2,
                                                     long long tot0, long long tot1, long long tot2) {
+  if (list_idle(tb)) return;
   const long long total = tot0 + tot1 + tot2;
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
        g += (long long)gridDim.x * blockDim.x) {
@@ -434,6 +438,7 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
 
 // MUSCL face states + Riemann flux (src/rhs/Riemann.h:251-337).
 __global__ void __launch_bounds__(256) riemann_face_kernel(BoxTable tb, FaceTable ft, long long total) {
+  if (list_idle(tb)) return;
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
        g += (long long)gridDim.x * blockDim.x) {
     FaceIdx f;
@@ -491,6 +496,7 @@ __device__ __forceinline__ double discon_sensor(double pp, double pl, double pr)
 // Sensor and spectral radius on the valid box (src/rhs/CNS_hydro_K.h:46-75);
 // the arrays are zeroed beforehand, as the reference zeroes its MultiFabs.
 __global__ void __launch_bounds__(256) jst_sensor_kernel(BoxTable tb, FaceTable ft, long long total) {
+  if (list_idle(tb)) return;
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
        g += (long long)gridDim.x * blockDim.x) {
     const int b = find_box_ll(ft.vpre, tb.n, g);
@@ -518,6 +524,7 @@ __global__ void __launch_bounds__(256) jst_sensor_kernel(BoxTable tb, FaceTable 
 // y and z read component 0 of sensor and lambda, and the z fourth
 // difference uses k-1 three times, as in the reference.
 __global__ void __launch_bounds__(256) jst_face_kernel(BoxTable tb, FaceTable ft, int s_in, long long total) {
+  if (list_idle(tb)) return;
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
        g += (long long)gridDim.x * blockDim.x) {
     FaceIdx f;
@@ -547,6 +554,7 @@ __global__ void __launch_bounds__(256) jst_face_kernel(BoxTable tb, FaceTable ft
 // ---------------------------------------------- viscous face average ----
 // src/rhs/CNS_hydro_K.h:254-261 (mass component adds zero and is skipped).
 __global__ void __launch_bounds__(256) visc_face_add_kernel(BoxTable tb, FaceTable ft, long long total) {
+  if (list_idle(tb)) return;
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
        g += (long long)gridDim.x * blockDim.x) {
     FaceIdx f;
@@ -568,7 +576,9 @@ __global__ void __launch_bounds__(256) visc_face_add_kernel(BoxTable tb, FaceTab
 // --------------------------------------- divergence + stage program ----
 // src/tim/CNS_advance.cpp:384-390, then the BLAS-1 program of the stage.
 __global__ void __launch_bounds__(256) div_stage_kernel(BoxTable tb, FaceTable ft, int s_in, int s_s1, int s_out,
-                                                        DProg prog, int rhs_only, long long total) {
+                                                        DProg prog_in, int rhs_only, long long total) {
+  if (list_idle(tb)) return;
+  const DProg prog = resolve_prog(prog_in);
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
        g += (long long)gridDim.x * blockDim.x) {
     const int b = find_box_ll(ft.vpre, tb.n, g);

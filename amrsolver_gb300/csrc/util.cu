@@ -70,6 +70,7 @@ __global__ void __launch_bounds__(256) halo_kernel(HaloBox hb) {
 // ensemble member or an isolated box), one launch for all boxes.
 __global__ void __launch_bounds__(256) halo_list_kernel(BoxTable tb, const long long* gpre, int slot, int bl0, int bl1,
                                                         int bl2, int bh0, int bh1, int bh2) {
+  if (list_idle(tb)) return;
   const long long total = gpre[tb.n];
   const int g = NGHOST;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < total;
@@ -109,6 +110,7 @@ __global__ void __launch_bounds__(256) halo_list_kernel(BoxTable tb, const long 
 // fill of one box covering the domain.
 __global__ void __launch_bounds__(256) halo_level_kernel(BoxTable tb, const long long* gpre, const int* owner,
                                                          int slot, LevelDomain dom) {
+  if (list_idle(tb)) return;
   const long long total = gpre[tb.n];
   const int g = NGHOST;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < total;
@@ -170,6 +172,7 @@ cudaError_t launch_halo(const HaloBox& hb, cudaStream_t st) {
 // exact minimum whatever the order.
 __global__ void __launch_bounds__(256) estdt_kernel(BoxTable tb, int s_in, long long total,
                                                      unsigned long long* bits) {
+  if (list_idle(tb)) return;  // uniform over the grid
   unsigned long long best = ~0ull;
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
        g += (long long)gridDim.x * blockDim.x) {
@@ -245,6 +248,159 @@ cudaError_t launch_estdt(const BoxTable& tb, int s_in, long long nvalid, double 
   if (blocks < 1) blocks = 1;
   estdt_kernel<<<(int)blocks, 256, 0, st>>>(tb, s_in, nvalid, bits);
   estdt_final<<<1, 1, 0, st>>>(bits, cfl, dt_out);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------- device time loop ----
+// One launch of a captured step graph inside a conditional WHILE node runs
+// CNS::advance steps with the reference's single-level dt control
+// (computeInitialDt / computeNewDt, src/CNS.cpp:282-377) without host syncs.
+__global__ void run_estdt_reset(RunCtl* c) {
+  if (c->active) c->bits = ~0ull;
+}
+
+// After a step: time += dt, step += 1, the next dt (CFL: min(cfl * min
+// dx/(|u|+c), change_max * dt), the last step clamped to stop_time with
+// eps = 0.001 dt as the reference does), then whether to go on.
+__global__ void run_step_done(RunCtl* c, cudaGraphConditionalHandle cond) {
+  if (c->active) {
+    c->time = c->time + c->dt;
+    c->step += 1;
+    if (c->use_cfl) {
+      const unsigned long long b = c->bits;
+      const double est = ((b == ~0ull) ? 1.7976931348623157e308 : __longlong_as_double((long long)b)) * c->cfl;
+      const double grow = c->change_max * c->dt;
+      double dt0 = (grow < est) ? grow : est;  // std::min(est, grow)
+      const double eps = 0.001 * dt0;
+      if (c->stop >= 0.0 && c->time + dt0 > c->stop - eps) dt0 = c->stop - c->time;
+      c->dt = dt0;
+    }
+    c->active = (c->step < c->max_steps && c->time < c->stop) ? 1 : 0;
+  }
+  cudaGraphSetConditional(cond, c->active ? 1u : 0u);
+}
+
+// Initial dt (computeInitialDt: cfl * min dx/(|u|+c)) and whether to start.
+__global__ void run_begin(RunCtl* c) {
+  if (c->use_cfl) {
+    const unsigned long long b = c->bits;
+    c->dt = ((b == ~0ull) ? 1.7976931348623157e308 : __longlong_as_double((long long)b)) * c->cfl;
+  }
+  c->active = (c->step < c->max_steps && c->time < c->stop) ? 1 : 0;
+}
+
+// Valid cells of slot `from` into slot `to` for every box (the step's result
+// back into the S1 slot the next step reads).
+__global__ void __launch_bounds__(256) copy_slot_kernel(BoxTable tb, int from, int to, long long total) {
+  if (list_idle(tb)) return;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    long long acc = 0;
+    int b = 0;
+    for (; b < tb.n; ++b) {
+      const BoxRec& R = tb.box[b];
+      const long long nc = (long long)(R.hi[0] - R.lo[0] + 1) * (R.hi[1] - R.lo[1] + 1) * (R.hi[2] - R.lo[2] + 1);
+      if (g < acc + nc) break;
+      acc += nc;
+    }
+    if (b == tb.n) break;
+    const BoxRec& R = tb.box[b];
+    const int nx = R.hi[0] - R.lo[0] + 1, ny = R.hi[1] - R.lo[1] + 1;
+    const int l = (int)(g - acc);
+    const int i = l % nx + R.lo[0];
+    const int t = l / nx;
+    const int j = t % ny + R.lo[1];
+    const int k = t / ny + R.lo[2];
+    const DArr A = R.slot[from], B = R.slot[to];
+    const long long oa = A.off(i, j, k), ob = B.off(i, j, k);
+#pragma unroll
+    for (int n = 0; n < NCONS; ++n) B.p[ob + n * B.ns] = A.p[oa + n * A.ns];
+  }
+}
+
+// Conserved totals of slot `slot` over the valid cells of every box:
+// per-block sums in a fixed order, then one block sums the partials in
+// block order (deterministic; not the serial sum's rounding).
+__global__ void __launch_bounds__(256) totals_partial_kernel(BoxTable tb, int slot, long long total, double* part) {
+  double acc[NCONS] = {0, 0, 0, 0, 0};
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    long long base = 0;
+    int b = 0;
+    for (; b < tb.n; ++b) {
+      const BoxRec& R = tb.box[b];
+      const long long nc = (long long)(R.hi[0] - R.lo[0] + 1) * (R.hi[1] - R.lo[1] + 1) * (R.hi[2] - R.lo[2] + 1);
+      if (g < base + nc) break;
+      base += nc;
+    }
+    if (b == tb.n) break;
+    const BoxRec& R = tb.box[b];
+    const int nx = R.hi[0] - R.lo[0] + 1, ny = R.hi[1] - R.lo[1] + 1;
+    const int l = (int)(g - base);
+    const DArr S = R.slot[slot];
+    const long long o = S.off(l % nx + R.lo[0], (l / nx) % ny + R.lo[1], l / nx / ny + R.lo[2]);
+#pragma unroll
+    for (int n = 0; n < NCONS; ++n) acc[n] += S.p[o + n * S.ns];
+  }
+  __shared__ double sm[NCONS][256];
+#pragma unroll
+  for (int n = 0; n < NCONS; ++n) sm[n][threadIdx.x] = acc[n];
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+#pragma unroll
+      for (int n = 0; n < NCONS; ++n) sm[n][threadIdx.x] += sm[n][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < NCONS) part[(long long)blockIdx.x * NCONS + threadIdx.x] = sm[threadIdx.x][0];
+}
+
+__global__ void totals_final_kernel(const double* part, int nblocks, double scale, double* out) {
+  if (threadIdx.x < NCONS) {
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += part[(long long)b * NCONS + threadIdx.x];
+    out[threadIdx.x] = s * scale;
+  }
+}
+
+cudaError_t launch_run_estdt(const BoxTable& tb, int s_in, long long nvalid, RunCtl* c, int nsm, cudaStream_t st) {
+  run_estdt_reset<<<1, 1, 0, st>>>(c);
+  long long blocks = (nvalid + 255) / 256;
+  if (blocks > (long long)nsm * 4) blocks = (long long)nsm * 4;
+  if (blocks < 1) blocks = 1;
+  estdt_kernel<<<(int)blocks, 256, 0, st>>>(tb, s_in, nvalid, &c->bits);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_run_step_done(RunCtl* c, cudaGraphConditionalHandle cond, cudaStream_t st) {
+  run_step_done<<<1, 1, 0, st>>>(c, cond);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_run_begin(RunCtl* c, cudaStream_t st) {
+  run_begin<<<1, 1, 0, st>>>(c);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_copy_slot(const BoxTable& tb, int from, int to, long long nvalid, int nsm, cudaStream_t st) {
+  long long blocks = (nvalid + 255) / 256;
+  if (blocks > (long long)nsm * 8) blocks = (long long)nsm * 8;
+  if (blocks < 1) blocks = 1;
+  copy_slot_kernel<<<(int)blocks, 256, 0, st>>>(tb, from, to, nvalid);
+  return cudaGetLastError();
+}
+
+int totals_blocks(long long nvalid, int nsm) {
+  long long blocks = (nvalid + 255) / 256;
+  if (blocks > (long long)nsm * 2) blocks = (long long)nsm * 2;
+  return (int)(blocks < 1 ? 1 : blocks);
+}
+
+cudaError_t launch_totals(const BoxTable& tb, int slot, long long nvalid, double scale, double* part, double* out,
+                          int nsm, cudaStream_t st) {
+  const int nb = totals_blocks(nvalid, nsm);
+  totals_partial_kernel<<<nb, 256, 0, st>>>(tb, slot, nvalid, part);
+  totals_final_kernel<<<1, 32, 0, st>>>(part, nb, scale, out);
   return cudaGetLastError();
 }
 

@@ -243,6 +243,28 @@ amrs_status amrs_rk_stage_boxlist(amrs_boxlist* bl, const amrs_stage_prog* prog,
 amrs_status amrs_rk_step_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t stages_rk, double dt, int32_t s1,
                                  int32_t w1, int32_t w2, int32_t use_graph, void* stream, int32_t* result_slot);
 
+/* The reference's main loop (src/main.cpp:66-75 with CNS::advance and the
+ * single-level dt control of src/CNS.cpp:282-377) as ONE graph launch on the
+ * device, no host synchronisation: steps of (order_rk, stages_rk) from time
+ * `time` while step < max_steps and time < stop_time.  cfl > 0: dt from
+ * cns_estdt (computeInitialDt, then computeNewDt: growth capped at 1.1x, the
+ * last step clamped to stop_time); cfl <= 0: fixed dt.  The state lives in
+ * slot s1 (each step's result is copied back), w1/w2 are work slots; the
+ * stage kernels read dt from device memory.  A conditional WHILE graph node
+ * repeats the step body; its kernels return at once after the last step.
+ * No counterpart in the reference (its loop runs on the host). */
+amrs_status amrs_rk_run_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t stages_rk, double cfl, double dt,
+                                double time, double stop_time, int32_t max_steps, int32_t s1, int32_t w1, int32_t w2,
+                                void* stream);
+/* Time, current dt and step count of the last amrs_rk_run_boxlist
+ * (host-synchronising on `stream`). */
+amrs_status amrs_boxlist_run_state(amrs_boxlist* bl, double* time, double* dt, int32_t* steps, void* stream);
+/* Conserved totals of slot `slot` (CNS::printTotal, src/CNS.cpp:532-541:
+ * sum over the valid cells of every box times `scale`, the domain volume
+ * there) into totals[0..4] (device memory), one reduction on the device in
+ * a fixed order (deterministic; not the rounding of a serial sum). */
+amrs_status amrs_boxlist_totals(amrs_boxlist* bl, int32_t slot, double scale, double* totals, void* stream);
+
 /* ---- adjoint ----------------------------------------------------------- */
 
 /* Vector-Jacobian product of one RHS evaluation of one box (KEEP, WENO5

@@ -213,6 +213,25 @@ class CNS {
     return dt;
   }
 
+  // The reference's main loop for this level (src/main.cpp:66-75): steps
+  // until stop_time or max_step, dt from cfl (computeInitialDt /
+  // computeNewDt) when cfl > 0, else fixed_dt; the whole loop is one graph
+  // launch on the device (amrs_rk_run_boxlist).  Returns the steps taken
+  // (host-synchronising).
+  int run(Real stop_time, int max_step, Real cfl, Real fixed_dt = 0.0) {
+    int work[2], w = 0;
+    for (int i = 0; i < 3; ++i)
+      if (i != cur_) work[w++] = i;
+    check(amrs_rk_run_boxlist(bl_, order_rk_, stages_rk_, cfl, fixed_dt, time_, stop_time, max_step, cur_, work[0],
+                              work[1], stream_),
+          "amrs_rk_run_boxlist");
+    double t = 0.0, dt = 0.0;
+    int32_t steps = 0;
+    check(amrs_boxlist_run_state(bl_, &t, &dt, &steps, stream_), "amrs_boxlist_run_state");
+    time_ = t;
+    return steps;
+  }
+
   // CNS::estTimeStep: cfl * min over the level of dx/(|u|+c) (host-synchronising).
   Real estTimeStep(Real cfl) {
     const int n = (int)grids_.size();

@@ -1,12 +1,13 @@
 // Exercises include/amrs_cns.hpp the way a C++ caller of the reference's CNS
 // class would: compute_rhs on a ghost-filled state, then advance steps.
-//   cns_adapter_main <in.bin> <rhs_out.bin> <state_out.bin> n nsteps dt mu [m]
+//   cns_adapter_main <in.bin> <rhs_out.bin> <state_out.bin> n nsteps dt mu [m [run]]
 // in.bin: ghosted initial state (5, n+6, n+6, n+6) float64, periodic box of
 // edge 2*pi; the level is split into m boxes per direction (cuts at
 // floor(i*n/m), default m = 1); outputs: dSdt of the initial state (valid
 // cells) and the valid state after nsteps SSPRK3 steps.
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "amrs_cns.hpp"
@@ -74,7 +75,12 @@ int main(int argc, char** argv) {
     std::vector<double> Rg((size_t)5 * n * n * n);
     for (int b = 0; b < dSdt.size(); ++b) copy_box(Rg, n, 0, dSdt.fab(b), 0, false, 0);
     R = Rg;
-    for (int s = 0; s < nsteps; ++s) lev.advance(lev.curTime(), dt, 1, 1);
+    if (argc > 9 && std::string(argv[9]) == "run") {
+      // the whole loop as one device launch, fixed dt
+      if (lev.run(1e30, nsteps, 0.0, dt) != nsteps) return 5;
+    } else {
+      for (int s = 0; s < nsteps; ++s) lev.advance(lev.curTime(), dt, 1, 1);
+    }
     amrs::MultiFab& F = lev.get_new_data();
     for (int b = 0; b < F.size(); ++b) copy_box(V, n, 0, F.fab(b), 3, false, 0);
     amrs::check(amrs_sync_check(lev.handle(), nullptr), "sync");

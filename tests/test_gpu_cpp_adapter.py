@@ -15,8 +15,9 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
+@pytest.mark.parametrize("mode", ["advance", "run"])
 @pytest.mark.parametrize("m", [1, 3])
-def test_cpp_adapter_bitexact(orc, tmp_path, m):
+def test_cpp_adapter_bitexact(orc, tmp_path, m, mode):
     assert torch.cuda.is_available()
     lib = B.build()
     exe = str(tmp_path / "cns_adapter")
@@ -28,7 +29,7 @@ def test_cpp_adapter_bitexact(orc, tmp_path, m):
     fin = tmp_path / "in.bin"
     U.tofile(fin)
     subprocess.check_call([exe, str(fin), str(tmp_path / "rhs.bin"), str(tmp_path / "state.bin"), str(n),
-                           str(nsteps), repr(dt), repr(mu), str(m)])
+                           str(nsteps), repr(dt), repr(mu), str(m), mode])
     R = np.fromfile(tmp_path / "rhs.bin").reshape(5, n, n, n)
     S = np.fromfile(tmp_path / "state.bin").reshape(5, n, n, n)
     cl = P.Closures.nondimensional(mu)

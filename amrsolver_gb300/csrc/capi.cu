@@ -264,7 +264,10 @@ struct List {
   int run_key[6] = {0, 0, 0, 0, 0, 0};
   double* d_tot = nullptr;  // per-block partial sums of amrs_boxlist_totals
   size_t d_tot_n = 0;
+  double* d_step_dt = nullptr;  // dt the step graph's stage programs read
+  double h_step_dt = 0.0;
   ~List() {
+    if (d_step_dt) cudaFree(d_step_dt);
     if (run_graph) cudaGraphExecDestroy(run_graph);
     if (d_run) cudaFree(d_run);
     if (d_tot) cudaFree(d_tot);
@@ -1157,13 +1160,15 @@ amrs_status amrs_rk_step_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t sta
       w1 == w2)
     return AMRS_ERR_SIZE;
   amrs_stage_prog progs[16];
+  DProg forms[16];
   int32_t ns = 0;
-  if (amrs_status s = amrs_rk_program(order_rk, stages_rk, dt, progs, 16, &ns)) return s;
+  if (amrs_status s = rk_build(order_rk, stages_rk, dt, progs, 16, &ns, forms)) return s;
   CK(cudaSetDevice(bl->h->device));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // slot rotation: stage input is S1 for src_state 0, else the last output;
-  // outputs alternate between the two work slots.
-  auto record = [&](cudaStream_t s, int* res) -> amrs_status {
+  // outputs alternate between the two work slots.  In a graph the stage
+  // programs read dt from device memory, so one graph serves every dt.
+  auto record = [&](cudaStream_t s, int* res, bool device_dt) -> amrs_status {
     int cur = s1;  // holds S2 values (stage input)
     int outs[2] = {w1, w2};
     int which = 0;
@@ -1172,16 +1177,21 @@ amrs_status amrs_rk_step_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t sta
       int out = outs[which];
       if (out == in) { which ^= 1; out = outs[which]; }
       if (L.has_bc) CK(list_fill(bl->h, L, in, s));
-      if (amrs_status e = list_stage(bl->h, L, to_dprog(&progs[i]), in, s1, out, 0, s)) return e;
+      DProg p = to_dprog(&progs[i]);
+      if (device_dt) { p = forms[i]; p.dtp = L.d_step_dt; }
+      if (amrs_status e = list_stage(bl->h, L, p, in, s1, out, 0, s)) return e;
       cur = out;
       which ^= 1;
     }
     *res = cur;
     return AMRS_OK;
   };
-  if (!use_graph) return record(st, result_slot);
+  if (!use_graph) return record(st, result_slot, false);
+  if (!L.d_step_dt) CK(cudaMalloc(&L.d_step_dt, sizeof(double)));
+  L.h_step_dt = dt;
+  CK(cudaMemcpyAsync(L.d_step_dt, &L.h_step_dt, sizeof(double), cudaMemcpyHostToDevice, st));
   const int key[6] = {order_rk, stages_rk, s1, w1, w2, 1};
-  if (!L.graph || std::memcmp(key, L.graph_key, sizeof(key)) != 0 || L.graph_dt != dt) {
+  if (!L.graph || std::memcmp(key, L.graph_key, sizeof(key)) != 0) {
     if (L.graph) { cudaGraphExecDestroy(L.graph); L.graph = nullptr; }
     cudaStream_t cs;
     CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
@@ -1189,7 +1199,7 @@ amrs_status amrs_rk_step_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t sta
     cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) { cudaStreamDestroy(cs); return cuda_fail(e, "cudaStreamBeginCapture"); }
     int res = -1;
-    amrs_status rs = record(cs, &res);
+    amrs_status rs = record(cs, &res, true);
     e = cudaStreamEndCapture(cs, &g);
     cudaStreamDestroy(cs);
     if (rs) { if (e == cudaSuccess) cudaGraphDestroy(g); return rs; }

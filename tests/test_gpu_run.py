@@ -148,3 +148,21 @@ def test_level_run_and_totals():
     scale[1:4] = scale[1:4].max()
     assert np.all(np.abs(tot1 - tot0) <= 1e-13 * scale), (tot1 - tot0, scale)
     h.sync_check()
+
+
+def test_step_graph_serves_changing_dt():
+    """The step graph reads dt from device memory: one capture, three dts."""
+    U, dx = P.tgv(16, mach=0.2)
+    cl = P.Closures.nondimensional(1.0 / 800.0)
+    sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1)
+    bc = (-1, -1, -1)
+    h, bl, slots = one_box_list(sc, cl, U, dx, bc)
+    lev = cns.CNSLevel(sc, cl, U, dx)
+    s1, w1, w2 = 0, 1, 2
+    for dt in (1e-3, 2.5e-3, 7e-4, 1e-3):
+        r = bl.step(3, 3, dt, s1, w1, w2, use_graph=True)
+        # copy the result back so that the same graph (same slots) is replayed
+        slots[0][s1][:] = slots[0][r]
+        lev.advance(lev.time, dt)
+    h.sync_check()
+    np.testing.assert_array_equal(slots[0][s1][:, NG:-NG, NG:-NG, NG:-NG].cpu().numpy(), lev.valid().cpu().numpy())

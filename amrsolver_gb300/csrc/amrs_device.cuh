@@ -131,25 +131,29 @@ __device__ __forceinline__ void viscous_cell_dy(const double* qc, const double* 
   const double mu = visc(c, qc[QT]);
   const double lambda = cond(c, qc[QT]);
   const double r1_3 = 1.0 / 3.0;
-  const double mu2 = 2.0 * mu;
-  const double tauxx = mu2 * (dudx - r1_3 * div);
-  const double tauxy = mu * (dudy + dvdx);
-  const double tauxz = mu * (dudz + dwdx);
-  const double tauyy = mu2 * (dvdy - r1_3 * div);
-  const double tauyz = mu * (dvdz + dwdy);
-  const double tauzz = mu2 * (dwdz - r1_3 * div);
-  f[0] = -tauxx;
-  f[1] = -tauxy;
-  f[2] = -tauxz;
-  f[3] = -lambda * dTdx - tauxx * ux - tauxy * uy - tauxz * uz;
-  f[4] = -tauxy;
-  f[5] = -tauyy;
-  f[6] = -tauyz;
-  f[7] = -lambda * dTdy - tauxy * ux - tauyy * uy - tauyz * uz;
-  f[8] = -tauxz;
-  f[9] = -tauyz;
-  f[10] = -tauzz;
-  f[11] = -lambda * dTdz - tauxz * ux - tauyz * uy - tauzz * uz;
+  // The fluxes are stored negated (-tau, -lambda dT - tau.u).  Negation is
+  // exact, so (-2mu)*d == -(2mu*d) and a + (-t)*u == a - t*u to the bit:
+  // the negated stresses n.. are formed directly and the sums add them,
+  // with no separate negations.
+  const double nmu = -mu, nmu2 = -2.0 * mu, nlam = -lambda;
+  const double nxx = nmu2 * (dudx - r1_3 * div);
+  const double nxy = nmu * (dudy + dvdx);
+  const double nxz = nmu * (dudz + dwdx);
+  const double nyy = nmu2 * (dvdy - r1_3 * div);
+  const double nyz = nmu * (dvdz + dwdy);
+  const double nzz = nmu2 * (dwdz - r1_3 * div);
+  f[0] = nxx;
+  f[1] = nxy;
+  f[2] = nxz;
+  f[3] = nlam * dTdx + nxx * ux + nxy * uy + nxz * uz;
+  f[4] = nxy;
+  f[5] = nyy;
+  f[6] = nyz;
+  f[7] = nlam * dTdy + nxy * ux + nyy * uy + nyz * uz;
+  f[8] = nxz;
+  f[9] = nyz;
+  f[10] = nzz;
+  f[11] = nlam * dTdz + nxz * ux + nyz * uy + nzz * uz;
 }
 
 __device__ __forceinline__ void viscous_cell(const double* qc, const double* qxm, const double* qxp,

@@ -234,33 +234,68 @@ keep_face_kernel(BoxTable tb, int s_in, int s_s1, int s_out, DProg prog_in, int 
       if (tid == 0) tma_load_plane(tma, b, &mbar[0], qsbuf, x0 - 3 - qlo0, y0 - H - qlo1, k0 - (R.lo[2] - NGHOST), QS * NQ * 8);
     }
 
-    for (int k = k0; k < k1; ++k) {
+    // Per plane k two barriers: A publishes plane k (and closes the faces
+    // of plane k-1), B closes the pair terms of plane k.  Between A and B:
+    // the divergence of plane k-1 (phase 3) and the pair terms of plane k
+    // (phase 1); after B: the faces of plane k (phase 2).  One extra
+    // iteration k = k1 runs the last plane's phase 3.
+    double fznew[5];
+    for (int k = k0; k <= k1; ++k) {
+      const bool plane = k < k1;
       double* qs = qsbuf + buf * NQ * C::QS_CAP;
       // ---- phase 0: plane k of Q into shared memory
-      if (use_tma) {
-        if (!mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) { if (tid == 0) atomicExch(err, 1); }
-        phase_bits ^= (1u << buf);
-        if (tid == 0 && k + 1 < k1) {
-          fence_proxy_async();
-          tma_load_plane(tma, b, &mbar[buf ^ 1], qsbuf + (buf ^ 1) * NQ * C::QS_CAP, x0 - 3 - qlo0, y0 - H - qlo1,
-                         k + 1 - (R.lo[2] - NGHOST), QS * NQ * 8);
-        }
-      } else {
-        const int nel = NQ * QS;
-        for (int e = tid; e < nel; e += F_THREADS) {
-          const int n = e / QS;
-          const int r = e - n * QS;
-          const int yy = r / QP, xx = r - (r / QP) * QP;
-          const int gi = x0 - 3 + xx, gj = y0 - H + yy;
-          double v = 0.0;
-          if (gi >= qlo0 && gi <= qhi0 && gj >= qlo1 && gj <= qhi1) v = Q(gi, gj, k, n);
-          qs[e] = v;
+      if (plane) {
+        if (use_tma) {
+          if (!mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) { if (tid == 0) atomicExch(err, 1); }
+          phase_bits ^= (1u << buf);
+        } else {
+          // buffer buf held plane k-2, whose readers finished before the last barrier A
+          const int nel = NQ * QS;
+          for (int e = tid; e < nel; e += F_THREADS) {
+            const int n = e / QS;
+            const int r = e - n * QS;
+            const int yy = r / QP, xx = r - (r / QP) * QP;
+            const int gi = x0 - 3 + xx, gj = y0 - H + yy;
+            double v = 0.0;
+            if (gi >= qlo0 && gi <= qhi0 && gj >= qlo1 && gj <= qhi1) v = Q(gi, gj, k, n);
+            qs[e] = v;
+          }
         }
       }
-      __syncthreads();
+      __syncthreads();  // A
+      // the next plane into the other buffer: its plane k-1 was last read
+      // by the faces of plane k-1, which every thread finished before A
+      if (plane && use_tma && tid == 0 && k + 1 < k1) {
+        fence_proxy_async();
+        tma_load_plane(tma, b, &mbar[buf ^ 1], qsbuf + (buf ^ 1) * NQ * C::QS_CAP, x0 - 3 - qlo0, y0 - H - qlo1,
+                       k + 1 - (R.lo[2] - NGHOST), QS * NQ * 8);
+      }
+
+      // ---- phase 3 of plane k-1: divergence + stage program for the own cell
+      if (k > k0 && has_col) {
+        const int kc = k - 1;
+        const long long oin = Uin.off(ci, cj, kc), o1 = U1.off(ci, cj, kc), oo = Uo.off(ci, cj, kc);
+#pragma unroll
+        for (int n = 0; n < 5; ++n) {
+          const double* fx = fsx + n * C::F_CAP + cb * (TX + 1) + ca;
+          const double* fy = fsy + n * C::F_CAP + cb * TX + ca;
+          const double ds = dxi0 * (fx[0] - fx[1]) + dxi1 * (fy[0] - fy[TX]) + dxi2 * (fzprev[n] - fznew[n]);
+          if (rhs_only) {
+            Uo.p[oo + n * Uo.ns] = ds;
+          } else {
+            double reg[3];
+            reg[0] = U1.p[o1 + n * U1.ns];
+            reg[1] = Uin.p[oin + n * Uin.ns];
+            reg[2] = ds;
+            apply_prog(prog, reg);
+            Uo.p[oo + n * Uo.ns] = reg[1];
+          }
+          fzprev[n] = fznew[n];
+        }
+      }
+      if (!plane) break;
 
       // ---- phase 1: stored pair terms (x, y) and the z face above plane k
-      double fznew[5];
       if (has_col) {
         double qk[NQ], qtop[NQ];
         ld_qs(qs, (cb + H) * QP + (ca + 3), QS, qk);
@@ -407,29 +442,8 @@ keep_face_kernel(BoxTable tb, int s_in, int s_s1, int s_out, DProg prog_in, int 
           }
         }
       }
-      __syncthreads();
-
-      // ---- phase 3: divergence + stage program for the own cell of plane k
-      if (has_col) {
-        const long long oin = Uin.off(ci, cj, k), o1 = U1.off(ci, cj, k), oo = Uo.off(ci, cj, k);
-#pragma unroll
-        for (int n = 0; n < 5; ++n) {
-          const double* fx = fsx + n * C::F_CAP + cb * (TX + 1) + ca;
-          const double* fy = fsy + n * C::F_CAP + cb * TX + ca;
-          const double ds = dxi0 * (fx[0] - fx[1]) + dxi1 * (fy[0] - fy[TX]) + dxi2 * (fzprev[n] - fznew[n]);
-          if (rhs_only) {
-            Uo.p[oo + n * Uo.ns] = ds;
-          } else {
-            double reg[3];
-            reg[0] = U1.p[o1 + n * U1.ns];
-            reg[1] = Uin.p[oin + n * Uin.ns];
-            reg[2] = ds;
-            apply_prog(prog, reg);
-            Uo.p[oo + n * Uo.ns] = reg[1];
-          }
-          fzprev[n] = fznew[n];
-        }
-      }
+      // phase 3 of this plane (its divergence) runs in the next iteration,
+      // after the barrier that also publishes the next plane
       buf ^= 1;
     }
     // the TMA ring is drained at the last plane; nothing is in flight here

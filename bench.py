@@ -380,6 +380,46 @@ def bench_level(torch, capi, P, n=128, box=32, steps=10, warmup=3):
             "ms_per_step": ms, "cell_updates_per_s": n ** 3 / (ms * 1e-3), "result_slot": r}
 
 
+def bench_sod(torch, capi, P):
+    """Sod tube 256x8x8 (WENO5-LLF, outflow x, periodic y/z) to t = 0.2 at
+    CFL 0.3 with the reference's dt control: the whole run as one device
+    launch (amrs_rk_run_boxlist) against the host-driven loop (one step and
+    one dt reduction read back per step)."""
+    import time as _time
+    from amrsolver_gb300 import cns
+    U, dx = P.sod(256, 8, 8)
+    cl = P.Closures.air_sutherland()
+    sc = P.Scheme(flux_euler=2, rhs_visc=0)
+    bc = (2, -1, -1)
+    stop, cfl = 0.2, 0.3
+    h = capi.Handle(sc, cl)
+    t0 = torch.from_numpy(U).cuda()
+    slots = [[t0.clone(), t0.clone(), t0.clone()]]
+    bl = capi.BoxList(h, [(0, 0, 0)], slots, [1.0 / v for v in dx])
+    bl.set_domain((0, 0, 0), (256, 8, 8), bc, bc)
+    res = {}
+    for rep in range(2):  # the first run captures the graph
+        slots[0][0].copy_(t0)
+        torch.cuda.synchronize()
+        w0 = _time.perf_counter()
+        bl.run(3, 3, stop_time=stop, max_steps=100000, cfl=cfl)
+        t, dt, steps = bl.run_state()
+        res["device_loop_ms"] = (_time.perf_counter() - w0) * 1e3
+    res["steps"] = steps
+    res["final_time"] = t
+    lev = cns.CNSLevel(sc, cl, U, dx, bc_lo=bc, bc_hi=bc)
+    torch.cuda.synchronize()
+    w0 = _time.perf_counter()
+    lev.run(stop, 100000, cfl=cfl)
+    torch.cuda.synchronize()
+    res["host_loop_ms"] = (_time.perf_counter() - w0) * 1e3
+    res["same_state"] = bool(torch.equal(lev.valid(), slots[0][0][:, 3:-3, 3:-3, 3:-3]))
+    res["speedup"] = res["host_loop_ms"] / res["device_loop_ms"]
+    h.sync_check()
+    res["workload"] = "Sod 256x8x8 WENO5-LLF to t=0.2, CFL 0.3 dynamic dt: one graph launch vs host loop (wall clock)"
+    return res
+
+
 def bench_large(torch, capi, P, peak, n=256, steps=20):
     """Periodic 256^3 random-phase turbulence (E(k) ~ k^4 exp(-2 (k/4)^2),
     turbulent Mach 0.6, rho = 1, p = 1/gamma), mu = 1e-4, Pr = 0.71, WENO5-LLF +
@@ -617,6 +657,7 @@ def run_gpu(args, rank, world, local):
             result["ensemble"] = bench_ensemble(torch, capi, P)
             result["adjoint"] = bench_adjoint(torch, P)
             result["level"] = bench_level(torch, capi, P, n=n)
+            result["sod_device_loop"] = bench_sod(torch, capi, P)
         if not args.skip_large:
             result["large"] = bench_large(torch, capi, P, peak)
         if not args.skip_cpu:

@@ -275,7 +275,8 @@ class Handle:
 
     def profile_stage_box(self, prog, Uin, U1, Uout, dxinv, lo=(0, 0, 0), reps=5, stream=None):
         """Per-kernel ms of one stage: (prims [+ WENO point fluxes], viscous
-        cells, Euler face kernel [fused: + divergence + program], total)."""
+        cells, Euler face kernel [fused: + divergence + program; MUSCL:
+        slopes + Riemann faces], total)."""
         nz, ny, nx = (s - 2 * NGHOST for s in Uin.shape[1:])
         g1 = (U1.shape[1] - nz) // 2
         go = (Uout.shape[1] - nz) // 2

@@ -25,7 +25,7 @@ struct FaceRec {
   DArr pf[3];   // WENO physical fluxes over grow(box,3), NCONS comps
   DArr lam;     // WENO / JST spectral radius over grow(box,3), 3 comps
   DArr sen;     // JST sensor over grow(box,3), 3 comps
-  DArr slope[3];  // MUSCL slopes per direction over grow(box,1), NCONS comps
+  DArr slope[3];  // MUSCL face-state terms per direction over grow(box,1), NSLOPE comps
   long long nface[3];  // faces per direction (for flattening)
 };
 struct FaceTable {
@@ -47,6 +47,9 @@ cudaError_t launch_weno_faces(const BoxTable& tb, const FaceTable& ft, int s_in,
                               int nsm, cudaStream_t st);
 cudaError_t launch_riemann(const BoxTable& tb, const FaceTable& ft, const long long* spre_d[3],
                            long long nslope[3], long long nfaces[3], int nsm, cudaStream_t st);
+// WENO5-reconstructed primitive states + the two-shock solver (flux_euler = 3)
+cudaError_t launch_weno_riemann(const BoxTable& tb, const FaceTable& ft, long long nfaces[3], int nsm,
+                                cudaStream_t st);
 cudaError_t launch_jst(const BoxTable& tb, const FaceTable& ft, int s_in, long long ngcells, long long nvalid,
                        long long nfaces[3], int nsm, cudaStream_t st);
 cudaError_t launch_visc_face_add(const BoxTable& tb, const FaceTable& ft, long long nfaces[3], int nsm,

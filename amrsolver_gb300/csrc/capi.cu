@@ -73,7 +73,7 @@ long long grown_cells(const amrs_box& b, int g) {
 }
 
 amrs_status check_scheme(const amrs_scheme& s) {
-  if (s.flux_euler < 0 || s.flux_euler > 2) return AMRS_ERR_SCHEME;
+  if (s.flux_euler < 0 || s.flux_euler > 3) return AMRS_ERR_SCHEME;
   if (s.flux_euler == 1 && !(s.order_keep == 2 || s.order_keep == 4 || s.order_keep == 6)) return AMRS_ERR_SCHEME;
   if (s.art_diss != 0 && s.art_diss != 1) return AMRS_ERR_SCHEME;
   if (s.weno_fast != 0 && s.weno_fast != 1) return AMRS_ERR_SCHEME;
@@ -86,6 +86,7 @@ int prim_ghost(const amrs_scheme& s) {
   if (s.rhs_euler) {
     if (s.flux_euler == 1) g = std::max(g, s.order_keep / 2);
     else if (s.flux_euler == 0) g = std::max(g, 2);  // slopes on grow(bx,1) read +-1
+    else if (s.flux_euler == 3) g = std::max(g, 3);  // five-point stencils of the faces
     if (s.art_diss) g = std::max(g, 1);
   }
   if (s.rhs_visc) g = std::max(g, 2);
@@ -377,7 +378,7 @@ amrs_status list_build(amrs_handle* h, List& L, int n, const amrs_box* boxes, co
     if (need_weno || need_jst) { lam_off[b] = off; off = align_up(off + grown_cells(B, 3) * 3 * 8, 256); }
     if (need_jst) { sen_off[b] = off; off = align_up(off + grown_cells(B, 3) * 3 * 8, 256); }
     if (need_slope)
-      for (int d = 0; d < 3; ++d) { sl_off[b * 3 + d] = off; off = align_up(off + grown_cells(B, 1) * NCONS * 8, 256); }
+      for (int d = 0; d < 3; ++d) { sl_off[b * 3 + d] = off; off = align_up(off + grown_cells(B, 1) * NSLOPE * 8, 256); }
   }
   if (off > L.dscr_bytes) {
     if (L.dscr) { cudaFree(L.dscr); L.dscr = nullptr; L.dscr_bytes = 0; }
@@ -423,7 +424,7 @@ amrs_status list_build(amrs_handle* h, List& L, int n, const amrs_box* boxes, co
       }
       if (need_weno || need_jst) F.lam = mk(lam_off[b], 3, -1, 3);
       if (need_jst) F.sen = mk(sen_off[b], 3, -1, 3);
-      if (need_slope) for (int d = 0; d < 3; ++d) F.slope[d] = mk(sl_off[b * 3 + d], 1, -1, NCONS);
+      if (need_slope) for (int d = 0; d < 3; ++d) F.slope[d] = mk(sl_off[b * 3 + d], 1, -1, NSLOPE);
     }
     const int g = L.gq;
     L.pcell[b + 1] = L.pcell[b] + grown_cells(B, g);
@@ -602,6 +603,7 @@ amrs_status list_stage(amrs_handle* h, List& L, const DProg& prog, int s_in, int
   if (sc.rhs_euler) {
     if (sc.flux_euler == 1) CK(launch_keep_faces_plain(sc.order_keep, L.tb, L.ft, nf, nsm, st));
     else if (sc.flux_euler == 2) CK(launch_weno(L.tb, L.ft, s_in, L.tot_g, nf, sc.weno_fast == 0, nsm, st));
+    else if (sc.flux_euler == 3) CK(launch_weno_riemann(L.tb, L.ft, nf, nsm, st));
     else {
       long long ns[3] = {L.tot_s[0], L.tot_s[1], L.tot_s[2]};
       CK(launch_riemann(L.tb, L.ft, L.d_spre, ns, nf, nsm, st));
@@ -1566,8 +1568,9 @@ amrs_status amrs_profile_stage_box(amrs_handle* h, const amrs_box* bx, const dou
   List& L = *h->one;
   const amrs_scheme& sc = L.sc;
   // the face-array path is profiled for WENO5 (point fluxes timed with the
-  // primitives) and the unshared KEEP baseline
-  const bool plain_ok = sc.rhs_euler && !sc.art_diss && (sc.flux_euler == 1 || sc.flux_euler == 2);
+  // primitives), MUSCL-Riemann (slopes timed with the faces), WENO5-Riemann
+  // and the unshared KEEP baseline
+  const bool plain_ok = sc.rhs_euler && !sc.art_diss && sc.flux_euler >= 0 && sc.flux_euler <= 3;
   if (!L.fused && !plain_ok) { ring_release(h, st); return AMRS_ERR_SCHEME; }
   const DProg p = to_dprog(prog);
   cudaEvent_t ev[5];
@@ -1587,7 +1590,12 @@ amrs_status amrs_profile_stage_box(amrs_handle* h, const amrs_box* bx, const dou
                            h->nsm, st);
     else if (e == cudaSuccess && sc.flux_euler == 2)
       e = launch_weno_faces(L.tb, L.ft, 0, nf, sc.weno_fast == 0, h->nsm, st);
-    else if (e == cudaSuccess)
+    else if (e == cudaSuccess && sc.flux_euler == 3)
+      e = launch_weno_riemann(L.tb, L.ft, nf, h->nsm, st);
+    else if (e == cudaSuccess && sc.flux_euler == 0) {
+      long long ns[3] = {L.tot_s[0], L.tot_s[1], L.tot_s[2]};
+      e = launch_riemann(L.tb, L.ft, L.d_spre, ns, nf, h->nsm, st);
+    } else if (e == cudaSuccess)
       e = launch_keep_faces_plain(sc.order_keep, L.tb, L.ft, nf, h->nsm, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[3], st);
     if (e == cudaSuccess && !L.fused) {

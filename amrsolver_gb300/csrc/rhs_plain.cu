@@ -321,7 +321,8 @@ __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, c
     const long long o = q.off(i, j, k);
     const int QN = QU + d, QT1 = (d == 0) ? QV : QU, QT2 = (d == 2) ? QV : QW;
     auto Q = [&](long long off, int n) { return q.p[off + n * q.ns]; };
-    const double cspeed = sqrt(cl.gamma * cl.Rspec * Q(o, QT)) + (d == 0 ? 2.e-40 : 1.e-40);
+    const double c0 = sqrt(cl.gamma * cl.Rspec * Q(o, QT));
+    const double cspeed = c0 + (d == 0 ? 2.e-40 : 1.e-40);
     double dlft = 0.5 * (Q(o, QPRES) - Q(o - s, QPRES)) / cspeed - 0.5 * Q(o, QRHO) * (Q(o, QN) - Q(o - s, QN));
     double drgt = 0.5 * (Q(o + s, QPRES) - Q(o, QPRES)) / cspeed - 0.5 * Q(o, QRHO) * (Q(o + s, QN) - Q(o, QN));
     const double d0 = mc_limiter(dlft, drgt);
@@ -334,13 +335,26 @@ __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, c
     const double d2 = mc_limiter(dlft, drgt);
     const double d3 = mc_limiter(Q(o, QT1) - Q(o - s, QT1), Q(o + s, QT1) - Q(o, QT1));
     const double d4 = mc_limiter(Q(o, QT2) - Q(o - s, QT2), Q(o + s, QT2) - Q(o, QT2));
+    // The terms of this cell's extrapolations to its two faces
+    // (src/rhs/Riemann.h:251-337), formed once here instead of once per face
+    // side: A = (d0+d2)/c + d1 (density), B = (d2-d0)/rho (normal velocity),
+    // C = (d0+d2)*c (pressure), c the cell's sqrt(gamma R T) + 1e-40.
+    const double csr = c0 + 1.e-40;
+    const double s02 = d0 + d2;
     const DArr S = ft.fr[b].slope[d];
     const long long os = S.off(i, j, k);
-    S.p[os] = d0;
-    S.p[os + S.ns] = d1;
-    S.p[os + 2 * S.ns] = d2;
-    S.p[os + 3 * S.ns] = d3;
-    S.p[os + 4 * S.ns] = d4;
+    S.p[os + SL_A * S.ns] = s02 / csr + d1;
+    S.p[os + SL_B * S.ns] = (d2 - d0) / Q(o, QRHO);
+    S.p[os + SL_C * S.ns] = s02 * csr;
+    S.p[os + SL_T1 * S.ns] = d3;
+    S.p[os + SL_T2 * S.ns] = d4;
+    if (d == 2 && k <= R.hi[2]) {
+      // cns_riemann_z's left state takes its sound speed from q(i,j,k+1)
+      // (src/rhs/Riemann.h:316): for the face above this cell, cell k + 2
+      const double csl = sqrt(cl.gamma * cl.Rspec * Q(o + 2 * s, QT)) + 1.e-40;
+      S.p[os + SL_AL * S.ns] = s02 / csl + d1;
+      S.p[os + SL_CL * S.ns] = s02 * csl;
+    }
   }
 }
 
@@ -405,34 +419,47 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
     utrans2 = 0.5 * (ut2l + ut2r);
   }
   const double wosq = (0.5 * (gamma - 1.) * (pstar + po) + pstar) * ro;
-  const double co = sqrt(gamma * po / ro);
-  const double wo = sqrt(wosq);
   const double dpjmp = pstar - po;
-  const double rstar = ro / (1. - ro * dpjmp / wosq);
-  const double cstar = sqrt(gamma * pstar / rstar);
-  double spout = co - sgnm * uo;
-  double spin = cstar - sgnm * uo;
-  if (pstar >= po) {
-    spin = wo / ro - sgnm * uo;
-    spout = spin;
-  }
-  const double ss = rmax(spout - spin, spout + spin);
-  const double frac = 0.5 * (1. + (spin + spout) / rmax(ss, ccsmall));
+  const double suo = sgnm * uo;
   double rgdnv, ugdnv, pgdnv;
-  if (spout < 0.) {
-    rgdnv = ro; ugdnv = uo; pgdnv = po;
-  } else if (spin >= 0.) {
-    rgdnv = rstar; ugdnv = ustar; pgdnv = pstar;
-  } else {
+  // The reference evaluates every wave speed and the star density before it
+  // selects the state; here each is evaluated on the branch that reads it
+  // (same operations, same values, same selection, NaN included).
+  auto mixed = [&](double spin, double spout, double rstar) {
+    const double ss = rmax(spout - spin, spout + spin);
+    const double frac = 0.5 * (1. + (spin + spout) / rmax(ss, ccsmall));
     rgdnv = frac * rstar + (1. - frac) * ro;
     ugdnv = frac * ustar + (1. - frac) * uo;
     pgdnv = frac * pstar + (1. - frac) * po;
+  };
+  if (pstar >= po) {
+    // shock: spout == spin, so the side state or the star state
+    const double spin = sqrt(wosq) / ro - suo;
+    if (spin < 0.) {
+      rgdnv = ro; ugdnv = uo; pgdnv = po;
+    } else if (spin >= 0.) {
+      rgdnv = ro / (1. - ro * dpjmp / wosq); ugdnv = ustar; pgdnv = pstar;
+    } else {
+      mixed(spin, spin, ro / (1. - ro * dpjmp / wosq));
+    }
+  } else {
+    const double rstar = ro / (1. - ro * dpjmp / wosq);
+    const double spout = sqrt(gamma * po / ro) - suo;
+    const double spin = sqrt(gamma * pstar / rstar) - suo;
+    if (spout < 0.) {
+      rgdnv = ro; ugdnv = uo; pgdnv = po;
+    } else if (spin >= 0.) {
+      rgdnv = rstar; ugdnv = ustar; pgdnv = pstar;
+    } else {
+      mixed(spin, spout, rstar);
+    }
   }
   flxrho = rgdnv * ugdnv;
   flxu = rgdnv * ugdnv * ugdnv + pgdnv;
   flxut = rgdnv * ugdnv * utrans1;
   flxutt = rgdnv * ugdnv * utrans2;
-  flxe = ugdnv * (0.5 * rgdnv * (ugdnv * ugdnv + utrans1 * utrans1 + utrans2 * utrans2) + pgdnv / (gamma - 1.) +
+  // (0.5*r)*k + x == fma(0.5, r*k, x): the halving is exact (normal range)
+  flxe = ugdnv * (fma(0.5, rgdnv * (ugdnv * ugdnv + utrans1 * utrans1 + utrans2 * utrans2), pgdnv / (gamma - 1.)) +
                   pgdnv);
 }
 
@@ -446,35 +473,77 @@ __global__ void __launch_bounds__(256) riemann_face_kernel(BoxTable tb, FaceTabl
     const BoxRec& R = tb.box[f.b];
     const int d = f.d;
     const DArr q = R.q;
-    const DArr dq = ft.fr[f.b].slope[d];
+    const DArr S = ft.fr[f.b].slope[d];
     const DClosures& cl = tb.cls[R.cl];
     const int QN = QU + d, QT1 = (d == 0) ? QV : QU, QT2 = (d == 2) ? QV : QW;
     const int UN = UMX + d, UT1 = (d == 0) ? UMY : UMX, UT2 = (d == 2) ? UMY : UMZ;
     const int im = f.i - (d == 0), jm = f.j - (d == 1), km = f.k - (d == 2);
     const long long oq = q.off(f.i, f.j, f.k), oqm = q.off(im, jm, km);
-    const long long os = dq.off(f.i, f.j, f.k), osm = dq.off(im, jm, km);
+    const long long os = S.off(f.i, f.j, f.k), osm = S.off(im, jm, km);
     auto Q = [&](long long off, int n) { return q.p[off + n * q.ns]; };
-    auto D = [&](long long off, int n) { return dq.p[off + n * dq.ns]; };
-    const double gam = cl.gamma, Rs = cl.Rspec;
-    double cspeed = (d == 2) ? sqrt(gam * Rs * Q(q.off(f.i, f.j, f.k + 1), QT)) + 1.e-40
-                             : sqrt(gam * Rs * Q(oqm, QT)) + 1.e-40;
-    double rl = Q(oqm, QRHO) + 0.5 * ((D(osm, 0) + D(osm, 2)) / cspeed + D(osm, 1));
-    rl = rmax(rl, 1.0e-40);
-    const double ul = Q(oqm, QN) + 0.5 * ((D(osm, 2) - D(osm, 0)) / Q(oqm, QRHO));
-    double pl = Q(oqm, QPRES) + 0.5 * (D(osm, 0) + D(osm, 2)) * cspeed;
-    pl = rmax(pl, 1.0e-40);
-    const double ut1l = Q(oqm, QT1) + 0.5 * D(osm, 3);
-    const double ut2l = Q(oqm, QT2) + 0.5 * D(osm, 4);
-    cspeed = sqrt(gam * Rs * Q(oq, QT)) + 1.e-40;
-    double rr = Q(oq, QRHO) - 0.5 * ((D(os, 0) + D(os, 2)) / cspeed + D(os, 1));
-    rr = rmax(rr, 1.0e-40);
-    const double ur = Q(oq, QN) - 0.5 * ((D(os, 2) - D(os, 0)) / Q(oq, QRHO));
-    double pr = Q(oq, QPRES) - 0.5 * (D(os, 0) + D(os, 2)) * cspeed;
-    pr = rmax(pr, 1.0e-40);
-    const double ut1r = Q(oq, QT1) - 0.5 * D(os, 3);
-    const double ut2r = Q(oq, QT2) - 0.5 * D(os, 4);
+    auto D = [&](long long off, int n) { return S.p[off + n * S.ns]; };
+    const double gam = cl.gamma;
+    // left state from cell i-1, right state from cell i, with the terms
+    // slope_kernel formed (z: the left terms with the quirk's sound speed);
+    // q + 0.5*t == fma(0.5, t, q): the halving is exact (normal range)
+    const int cA = (d == 2) ? SL_AL : SL_A, cC = (d == 2) ? SL_CL : SL_C;
+    const double rl = rmax(fma(0.5, D(osm, cA), Q(oqm, QRHO)), 1.0e-40);
+    const double ul = fma(0.5, D(osm, SL_B), Q(oqm, QN));
+    const double pl = rmax(fma(0.5, D(osm, cC), Q(oqm, QPRES)), 1.0e-40);
+    const double ut1l = fma(0.5, D(osm, SL_T1), Q(oqm, QT1));
+    const double ut2l = fma(0.5, D(osm, SL_T2), Q(oqm, QT2));
+    const double rr = rmax(fma(-0.5, D(os, SL_A), Q(oq, QRHO)), 1.0e-40);
+    const double ur = fma(-0.5, D(os, SL_B), Q(oq, QN));
+    const double pr = rmax(fma(-0.5, D(os, SL_C), Q(oq, QPRES)), 1.0e-40);
+    const double ut1r = fma(-0.5, D(os, SL_T1), Q(oq, QT1));
+    const double ut2r = fma(-0.5, D(os, SL_T2), Q(oq, QT2));
     double frho, fu, fut, futt, fe;
     riemann_prob(gam, 1.0e-40, rl, ul, pl, ut1l, ut2l, rr, ur, pr, ut1r, ut2r, frho, fu, fut, futt, fe);
+    const DArr Fd = ft.fr[f.b].f[d];
+    const long long of = Fd.off(f.i, f.j, f.k);
+    Fd.p[of + URHO * Fd.ns] = frho;
+    Fd.p[of + UN * Fd.ns] = fu;
+    Fd.p[of + UT1 * Fd.ns] = fut;
+    Fd.p[of + UT2 * Fd.ns] = futt;
+    Fd.p[of + UET * Fd.ns] = fe;
+  }
+}
+
+// WENO5-Riemann faces (flux_euler = 3), an extension with no counterpart in
+// the reference (which pairs WENO5 only with the Lax-Friedrichs split and
+// the two-shock solver only with MUSCL): rho, u_n, p, u_t1, u_t2 are
+// reconstructed to the face from each side with weno5js (left state: cells
+// i-3..i+1; right state: the mirror i+2..i-2), rho and p floored at 1e-40
+// as the MUSCL states are (src/rhs/Riemann.h:260-272), and riemann_prob
+// gives the flux.  One thread per face.
+__global__ void __launch_bounds__(256) weno_riemann_face_kernel(BoxTable tb, FaceTable ft, long long total) {
+  if (list_idle(tb)) return;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    FaceIdx f;
+    if (!decode_face(tb, ft, g, f)) continue;
+    const BoxRec& R = tb.box[f.b];
+    const int d = f.d;
+    const DArr q = R.q;
+    const DClosures& cl = tb.cls[R.cl];
+    const int QN = QU + d, QT1 = (d == 0) ? QV : QU, QT2 = (d == 2) ? QV : QW;
+    const int UN = UMX + d, UT1 = (d == 0) ? UMY : UMX, UT2 = (d == 2) ? UMY : UMZ;
+    const long long sq = (d == 0) ? 1 : (d == 1 ? q.js : q.ks);
+    const long long o = q.off(f.i, f.j, f.k);
+    const int comp[5] = {QRHO, QN, QPRES, QT1, QT2};
+    double lft[5], rgt[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) {
+      const double* p = q.p + o + comp[m] * q.ns;
+      double v[6];
+#pragma unroll
+      for (int t = 0; t < 6; ++t) v[t] = p[(t - 3) * sq];
+      lft[m] = weno5js(v[0], v[1], v[2], v[3], v[4]);
+      rgt[m] = weno5js(v[5], v[4], v[3], v[2], v[1]);
+    }
+    double frho, fu, fut, futt, fe;
+    riemann_prob(cl.gamma, 1.0e-40, rmax(lft[0], 1.0e-40), lft[1], rmax(lft[2], 1.0e-40), lft[3], lft[4],
+                 rmax(rgt[0], 1.0e-40), rgt[1], rmax(rgt[2], 1.0e-40), rgt[3], rgt[4], frho, fu, fut, futt, fe);
     const DArr Fd = ft.fr[f.b].f[d];
     const long long of = Fd.off(f.i, f.j, f.k);
     Fd.p[of + URHO * Fd.ns] = frho;
@@ -643,6 +712,13 @@ cudaError_t launch_riemann(const BoxTable& tb, const FaceTable& ft, const long l
                                                   nslope[2]);
   const long long tot = nfaces[0] + nfaces[1] + nfaces[2];
   riemann_face_kernel<<<grid_for(tot, nsm), 256, 0, st>>>(tb, ft, tot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_weno_riemann(const BoxTable& tb, const FaceTable& ft, long long nfaces[3], int nsm,
+                                cudaStream_t st) {
+  const long long tot = nfaces[0] + nfaces[1] + nfaces[2];
+  weno_riemann_face_kernel<<<grid_for(tot, nsm), 256, 0, st>>>(tb, ft, tot);
   return cudaGetLastError();
 }
 

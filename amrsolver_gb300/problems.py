@@ -68,7 +68,9 @@ class Closures:
 
 @dataclasses.dataclass
 class Scheme:
-    """cns.* switches: flux_euler 0 = MUSCL/Riemann, 1 = KEEP, 2 = WENO5-JS LLF.
+    """cns.* switches: flux_euler 0 = MUSCL/Riemann, 1 = KEEP, 2 = WENO5-JS LLF,
+    3 = WENO5-Riemann (an extension: WENO5-reconstructed primitive states fed
+    to the two-shock solver; no reference counterpart).
 
     weno_fast (not a reference switch): 0 (default) evaluates WENO5 in the
     reference's operation order (bit-identical results); 1 forms the weights

@@ -52,6 +52,11 @@ SCHEMES = {
     "weno_fast": (dict(flux_euler=2, rhs_visc=1, weno_fast=1), "weno_visc",
                   "weno_face_kernel<false> (common-denominator weights)", "weno_fast_face_kernel_tgv96.md", 7,
                   "WENO5-LLF + viscous, common-denominator weights"),
+    "muscl": (dict(flux_euler=0, rhs_visc=1), "muscl_visc", "slope_kernel + riemann_face_kernel",
+              "riemann_face_kernel_tgv128.md", 7, "MUSCL-Riemann + viscous"),
+    "weno_riemann": (dict(flux_euler=3, rhs_visc=1), "weno_riemann_visc", "weno_riemann_face_kernel",
+                     "weno_riemann_face_kernel_tgv128.md", 6,
+                     "WENO5-Riemann (extension) + viscous"),
 }
 
 
@@ -147,6 +152,16 @@ def weno_face_flops(scheme_name, n):
     c = json.load(open(OP_COUNTS))["schemes"][scheme_name]["phases"]["euler_faces"]
     per_point = c[3] // 216
     return c[0] * n ** 3 + c[1] * n ** 2 + c[2] * n + c[3] - per_point * (n + 6) ** 3
+
+
+def riemann_face_flops(key, n):
+    """Flops of the Euler faces of one RHS of a Riemann-solver scheme (MUSCL:
+    slopes + faces; WENO5-Riemann: faces): the Euler phase as the oracle
+    counts it on the first RHS of the TGV 128^3 input (the solver's branches
+    make the count data-dependent); other edges scale it by n^3
+    (approximate)."""
+    ent = json.load(open(OP_COUNTS))["data_dependent"][key]
+    return ent["phases"]["euler_faces"] * (n / ent["n"]) ** 3
 
 
 def prog_flops(progs):
@@ -605,6 +620,14 @@ def run_gpu(args, rank, world, local):
         if args.scheme == "keep4":
             face_flops, per = face_kernel_flops(spec[1], n, prog_flops(progs[1:2]))
             algo_bytes_face = n ** 3 * (3 * 40)  # reads U_s, U^n, writes U_{s+1}: 120 B/cell
+        elif args.scheme == "muscl":
+            face_flops = riemann_face_flops(spec[1], n)
+            # reads Q (6 comps) per cell, writes and re-reads 3 x 5 slopes, writes 3 x 5 face values
+            algo_bytes_face = n ** 3 * (48 + 2 * 120) + 3 * (n + 1) * n * n * 40
+        elif args.scheme == "weno_riemann":
+            face_flops = riemann_face_flops(spec[1], n)
+            # reads Q (5 comps) per cell, writes 3 x 5 face values
+            algo_bytes_face = n ** 3 * 40 + 3 * (n + 1) * n * n * 40
         else:
             face_flops = weno_face_flops(spec[1], n)
             # reads U (40), point fluxes (120) and lambda (24) per cell, writes 3 x 5 face values

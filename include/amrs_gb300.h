@@ -65,7 +65,11 @@ typedef struct amrs_closures {
 /* cns.* run-time switches read by CNS::read_params (src/CNS.cpp:85-136).
  * flux_euler: 0 = MUSCL + Riemann (src/rhs/Riemann.h), 1 = KEEP split form
  * (src/rhs/CentralKEEP.h), 2 = WENO5-JS with local Lax-Friedrichs splitting
- * (src/rhs/High_resolution.h).  order_keep: 2, 4 or 6.  art_diss: JST. */
+ * (src/rhs/High_resolution.h); 3 = WENO5-Riemann, an extension with no
+ * reference counterpart: rho, u_n, p and the tangential velocities
+ * reconstructed to each face from both sides with the WENO5-JS stencils,
+ * fed to the reference's two-shock solver (src/rhs/Riemann.h:123-249); no
+ * reverse pass.  order_keep: 2, 4 or 6.  art_diss: JST. */
 typedef struct amrs_scheme {
   int32_t rhs_euler, rhs_visc, flux_euler, order_keep, art_diss;
   /* WENO5 only (no counterpart in the reference's switches).  0: the
@@ -310,7 +314,8 @@ amrs_status amrs_probe_fp64_tflops(amrs_handle* h, double* tflops);
  * kernels on `stream`, averaged over `reps`.  ms[0] primitives (plus the
  * WENO5 point fluxes), ms[1] viscous cell fluxes, ms[2] the Euler face
  * kernel (on the fused KEEP path: faces + viscous averages + divergence +
- * stage program), ms[3] the whole stage.  Host-synchronising. */
+ * stage program; on the MUSCL-Riemann path: slopes + Riemann faces), ms[3]
+ * the whole stage.  Host-synchronising. */
 amrs_status amrs_profile_stage_box(amrs_handle* h, const amrs_box* bx, const double dxinv[3],
                                    const amrs_stage_prog* prog, amrs_array4 stage_in, amrs_array4 s1,
                                    amrs_array4 out, int32_t reps, void* stream, double* ms);

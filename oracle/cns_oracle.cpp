@@ -18,6 +18,9 @@
 // restatement with that build bit for bit, and tests/golden/*.npz hold
 // vectors produced by that build so the pin also holds where the reference
 // sources are absent.
+// WENO5-Riemann (flux_euler = 3) has no reference counterpart: for it this
+// file is the specification, and its parity is unpinned against the
+// reference.
 //
 // Layout of every field (Array4 convention): component-major, i fastest,
 // ghost-inclusive.  A box [lo,hi] with g ghosts is stored as
@@ -187,7 +190,7 @@ struct Closures {
 struct Scheme {
   int rhs_euler;   // cns.rhs_euler
   int rhs_visc;    // cns.rhs_visc
-  int flux_euler;  // 0 = MUSCL + Riemann, 1 = KEEP, 2 = WENO5-JS LLF
+  int flux_euler;  // 0 = MUSCL + Riemann, 1 = KEEP, 2 = WENO5-JS LLF, 3 = WENO5-Riemann (extension)
   int order_keep;  // 2, 4, 6
   int art_diss;    // JST artificial dissipation
 };
@@ -518,6 +521,44 @@ inline void cns_riemann(int i, int j, int k, int d, const Arr<R>& f, const Arr<R
   f(i, j, k, UET) = fe;
 }
 
+// WENO5-Riemann (flux_euler = 3), an extension with no counterpart in the
+// reference: the reference pairs WENO5 only with the local Lax-Friedrichs
+// split (flux_euler = 2) and the two-shock solver only with MUSCL
+// (flux_euler = 0).  Here rho, u_n, p, u_t1, u_t2 are reconstructed to the
+// d-face below (i,j,k) from each side with weno5js (left state: cells
+// i-3..i+1; right state: the mirror i+2..i-2), density and pressure floored
+// at 1e-40 as the MUSCL states are (src/rhs/Riemann.h:260-272), and the
+// states go to riemann_prob.
+template <class R>
+inline void weno_riemann_face(int i, int j, int k, int d, const Arr<R>& f, const Arr<R>& q, const Closures& cl) {
+  const int di = (d == 0), dj = (d == 1), dk = (d == 2);
+  const int QN = QU + d;
+  const int QT1 = (d == 0) ? QV : QU;
+  const int QT2 = (d == 2) ? QV : QW;
+  const int UN = UMX + d;
+  const int UT1 = (d == 0) ? UMY : UMX;
+  const int UT2 = (d == 2) ? UMY : UMZ;
+  const int comp[5] = {QRHO, QN, QPRES, QT1, QT2};
+  R lft[5], rgt[5];
+  for (int m = 0; m < 5; ++m) {
+    R s[5];
+    for (int o = 0; o < 5; ++o) s[o] = q(i + (o - 3) * di, j + (o - 3) * dj, k + (o - 3) * dk, comp[m]);
+    lft[m] = weno5js(s);
+    for (int o = 0; o < 5; ++o) s[o] = q(i + (2 - o) * di, j + (2 - o) * dj, k + (2 - o) * dk, comp[m]);
+    rgt[m] = weno5js(s);
+  }
+  const R rl = rmax(lft[0], R(1.0e-40)), pl = rmax(lft[2], R(1.0e-40));
+  const R rr = rmax(rgt[0], R(1.0e-40)), pr = rmax(rgt[2], R(1.0e-40));
+  R frho, fu, fut, futt, fe;
+  riemann_prob(R(cl.gamma), R(1.0e-40), rl, lft[1], pl, lft[3], lft[4], rr, rgt[1], pr, rgt[3], rgt[4], frho, fu,
+               fut, futt, fe);
+  f(i, j, k, URHO) = frho;
+  f(i, j, k, UN) = fu;
+  f(i, j, k, UT1) = fut;
+  f(i, j, k, UT2) = futt;
+  f(i, j, k, UET) = fe;
+}
+
 // Cell-centred viscous fluxes: src/rhs/CNS_hydro_K.h:108-172.
 template <class R>
 inline void viscous_fluxes(int i, int j, int k, const Arr<R>& q, const Arr<R> pf[3], const double dxinv[3],
@@ -727,6 +768,15 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
           for (int j = lo1; j <= hi1 + (d == 1); ++j)
             for (int i = lo0; i <= hi0 + (d == 0); ++i)
               for (int n = 0; n < NCONS; ++n) F[d](i, j, k, n) = weno_llf_face(i, j, k, n, d, u, PF[d], lam);
+      }
+    } else if (sc.flux_euler == 3) {
+      for (int d = 0; d < 3; ++d) {
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nt) schedule(static)
+#endif
+        for (int k = lo2; k <= hi2 + (d == 2); ++k)
+          for (int j = lo1; j <= hi1 + (d == 1); ++j)
+            for (int i = lo0; i <= hi0 + (d == 0); ++i) weno_riemann_face(i, j, k, d, F[d], q, cl);
       }
     } else {
       // MUSCL + Riemann (src/rhs/Riemann.h:339-408); slope temp on grow(bx,1)

@@ -10,6 +10,12 @@ operation by operation (+, -, * each 1, / and sqrt each 1, no FMA in the
 oracle); comparisons are not flops.  `bench.py` reads the JSON this writes,
 so the roofline needs no oracle at run time.
 
+MUSCL-Riemann and WENO5-Riemann are the exceptions: the two-shock solver's
+branches (weak-wave switch, sign of u*, shock or rarefaction at the face)
+make their counts depend on the data, so they are recorded for the one input
+the bench times: the first RHS of the TGV 128^3 (M = 0.1, mu = 1/1600)
+initial state.
+
     python tests/golden/make_op_counts.py
 """
 import json
@@ -35,6 +41,11 @@ SCHEMES = {
 }
 FIT_N = (6, 8, 10, 12)
 CHECK_N = 14
+# data-dependent counts: (switches, edge, TGV Mach, mu) of the bench input
+DATA_DEPENDENT = {
+    "muscl_visc": (dict(flux_euler=0, rhs_visc=1), 128, 0.1, 1.0 / 1600.0),
+    "weno_riemann_visc": (dict(flux_euler=3, rhs_visc=1), 128, 0.1, 1.0 / 1600.0),
+}
 
 
 def flops(d):
@@ -45,6 +56,13 @@ def counts(orc, scheme, n):
     U, dx = P.tgv(n, mach=0.3)
     cl = P.Closures.nondimensional(1.0 / 400.0)
     per = orc.rhs_counts(P.Scheme(**scheme), cl, U, [1.0 / h for h in dx], per_phase=True)
+    return {ph: flops(v) for ph, v in per.items()}
+
+
+def tgv_counts(orc, scheme, n, mach, mu):
+    U, dx = P.tgv(n, mach=mach)
+    per = orc.rhs_counts(P.Scheme(**scheme), P.Closures.nondimensional(mu), U, [1.0 / h for h in dx],
+                         per_phase=True)
     return {ph: flops(v) for ph, v in per.items()}
 
 
@@ -68,7 +86,10 @@ def main():
     orc = pyoracle.oracle()
     data = {"doc": "per-RHS flops (+,-,*,/,sqrt each 1) of each compute_rhs phase as cubic coefficients "
                    "[n^3, n^2, n, 1] for an n^3 box, from the oracle's op-counting scalar",
-            "schemes": {name: {"switches": sc, "phases": fit(orc, sc)} for name, sc in SCHEMES.items()}}
+            "schemes": {name: {"switches": sc, "phases": fit(orc, sc)} for name, sc in SCHEMES.items()},
+            "data_dependent": {name: {"switches": sc, "n": n, "tgv_mach": mach, "mu": mu,
+                                      "phases": tgv_counts(orc, sc, n, mach, mu)}
+                               for name, (sc, n, mach, mu) in DATA_DEPENDENT.items()}}
     with open(OUT, "w") as f:
         json.dump(data, f, indent=1, sort_keys=True)
     print("wrote", OUT)

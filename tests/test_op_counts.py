@@ -25,3 +25,14 @@ def test_op_count_schemes_cover_bench():
     data = json.load(open(os.path.join(HERE, "golden", "op_counts.json")))
     assert {"keep4_visc", "weno_visc"} <= set(data["schemes"])
     assert P.Scheme(**data["schemes"]["weno_visc"]["switches"]).flux_euler == 2
+
+
+def test_data_dependent_counts_match_oracle(orc):
+    """The Riemann-solver schemes' counts depend on the data; the committed
+    figures are the oracle's counts of the bench input's first RHS."""
+    data = json.load(open(os.path.join(HERE, "golden", "op_counts.json")))
+    assert {"muscl_visc", "weno_riemann_visc"} <= set(data["data_dependent"])
+    for name, ent in data["data_dependent"].items():
+        assert P.Scheme(**ent["switches"]).flux_euler in (0, 3), name
+        got = M.tgv_counts(orc, ent["switches"], ent["n"], ent["tgv_mach"], ent["mu"])
+        assert got == ent["phases"], name

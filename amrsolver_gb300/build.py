@@ -1,10 +1,14 @@
 """Build recipe of the CUDA library (sm_103a only).
 
 Compiles amrsolver_gb300/csrc/*.cu with nvcc in parallel and links
-amrsolver_gb300/_lib/libamrs_gb300.so in the source tree.  The RHS
+amrsolver_gb300/_lib/libamrs_gb300.so in the source tree.  The forward
 translation units are built with -fmad=false: the kernels keep the
 reference's floating-point operation order, and without contraction their
-results are bit-identical to the reference's CPU build.
+results are bit-identical to the reference's CPU build.  The reverse-mode
+units (adjoint*.cu) have no bit-exact counterpart (their bar is agreement
+with forward-mode derivatives to ~1e-11 and with finite differences), so
+they let the compiler contract a*b + c into fused multiply-adds: on this
+FP64-bound path that removes a large share of their FP64 instructions.
 """
 import concurrent.futures as cf
 import glob
@@ -17,8 +21,13 @@ OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libamrs_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr"] + ARCH
+
+
+def _fmad(src):
+    """-fmad=false for the forward kernels, contraction for the reverse mode."""
+    return ["-fmad=true"] if os.path.basename(src).startswith("adjoint") else ["-fmad=false"]
 
 
 def _sources():
@@ -46,7 +55,7 @@ def build(force=False, verbose=False, extra=()):
     for s in _sources():
         o = os.path.join(OUT, os.path.basename(s)[:-3] + ".o")
         objs.append(o)
-        cmds.append([NVCC] + FLAGS + list(extra) + ["-c", s, "-o", o])
+        cmds.append([NVCC] + FLAGS + _fmad(s) + list(extra) + ["-c", s, "-o", o])
 
     def run(c):
         r = subprocess.run(c, capture_output=True, text=True)

@@ -1,8 +1,10 @@
 // Device-side types and point functions of the compressible RHS path.
 //
 // Every function keeps the floating-point operation order of the reference
-// function it cites, and the translation units are compiled with
-// -fmad=false, so results are bit-identical to the reference's CPU build.
+// function it cites, and the forward translation units are compiled with
+// -fmad=false, so results are bit-identical to the reference's CPU build
+// (the reverse-mode units, which recompute linearisation points with these
+// functions, allow contraction).
 // Explicit fma() appears only where one multiplicand is a power of two
 // (exact product), which rounds identically to the separate mul + add.
 #pragma once
@@ -16,6 +18,9 @@ constexpr int URHO = 0, UMX = 1, UMY = 2, UMZ = 3, UET = 4, NCONS = 5;
 constexpr int QRHO = 0, QU = 1, QV = 2, QW = 3, QT = 4, QPRES = 5, QE = 6, NQ = 7;
 constexpr int NGHOST = 3;
 constexpr int NVF = 12;  // viscous cell fluxes: x,y,z directions x (UMX..UET)
+// MUSCL face-state terms per cell and direction (see slope_kernel): the
+// Riemann faces' L/R extrapolations read them instead of the raw slopes
+constexpr int SL_A = 0, SL_B = 1, SL_C = 2, SL_T1 = 3, SL_T2 = 4, SL_AL = 5, SL_CL = 6, NSLOPE = 7;
 
 // Array4-like view (amrex::Array4<Real>).
 struct DArr {

@@ -35,7 +35,8 @@ class CClosures(ctypes.Structure):
 
 class CScheme(ctypes.Structure):
     _fields_ = [("rhs_euler", ctypes.c_int32), ("rhs_visc", ctypes.c_int32), ("flux_euler", ctypes.c_int32),
-                ("order_keep", ctypes.c_int32), ("art_diss", ctypes.c_int32), ("weno_fast", ctypes.c_int32)]
+                ("order_keep", ctypes.c_int32), ("art_diss", ctypes.c_int32), ("weno_fast", ctypes.c_int32),
+                ("riemann_weno", ctypes.c_int32)]
 
 
 class CBox(ctypes.Structure):
@@ -151,7 +152,7 @@ def c_closures(cl):
 
 def c_scheme(sc):
     return CScheme(int(sc.rhs_euler), int(sc.rhs_visc), int(sc.flux_euler), int(sc.order_keep), int(sc.art_diss),
-                   int(getattr(sc, "weno_fast", 0)))
+                   int(getattr(sc, "weno_fast", 0)), int(getattr(sc, "riemann_weno", 0)))
 
 
 def c_box(lo, n):

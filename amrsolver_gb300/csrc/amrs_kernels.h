@@ -47,7 +47,7 @@ cudaError_t launch_weno_faces(const BoxTable& tb, const FaceTable& ft, int s_in,
                               int nsm, cudaStream_t st);
 cudaError_t launch_riemann(const BoxTable& tb, const FaceTable& ft, const long long* spre_d[3],
                            long long nslope[3], long long nfaces[3], int nsm, cudaStream_t st);
-// WENO5-reconstructed primitive states + the two-shock solver (flux_euler = 3)
+// WENO5-reconstructed primitive states + the two-shock solver (riemann_weno = 1)
 cudaError_t launch_weno_riemann(const BoxTable& tb, const FaceTable& ft, long long nfaces[3], int nsm,
                                 cudaStream_t st);
 cudaError_t launch_jst(const BoxTable& tb, const FaceTable& ft, int s_in, long long ngcells, long long nvalid,

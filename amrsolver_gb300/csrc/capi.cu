@@ -72,8 +72,17 @@ long long grown_cells(const amrs_box& b, int g) {
   return (long long)(bn(b, 0) + 2 * g) * (bn(b, 1) + 2 * g) * (bn(b, 2) + 2 * g);
 }
 
+// The library's internal Euler-flux code: 1 KEEP, 2 WENO5 LLF, 0 MUSCL +
+// Riemann, 3 WENO5-Riemann.  The public flux_euler sends every value other
+// than 1 and 2 to the Riemann path, as the reference's compute_rhs does;
+// riemann_weno picks the states there.
+amrs_scheme canonical_scheme(amrs_scheme s) {
+  if (s.flux_euler != 1 && s.flux_euler != 2) s.flux_euler = s.riemann_weno ? 3 : 0;
+  return s;
+}
+
 amrs_status check_scheme(const amrs_scheme& s) {
-  if (s.flux_euler < 0 || s.flux_euler > 3) return AMRS_ERR_SCHEME;
+  if (s.riemann_weno != 0 && s.riemann_weno != 1) return AMRS_ERR_SCHEME;
   if (s.flux_euler == 1 && !(s.order_keep == 2 || s.order_keep == 4 || s.order_keep == 6)) return AMRS_ERR_SCHEME;
   if (s.art_diss != 0 && s.art_diss != 1) return AMRS_ERR_SCHEME;
   if (s.weno_fast != 0 && s.weno_fast != 1) return AMRS_ERR_SCHEME;
@@ -719,7 +728,7 @@ amrs_status amrs_create(amrs_handle** out, const amrs_scheme* scheme, const amrs
   amrs_handle* h = new (std::nothrow) amrs_handle();
   if (!h) return AMRS_ERR_ALLOC;
   h->device = device;
-  h->sc = *scheme;
+  h->sc = canonical_scheme(*scheme);
   h->cl = *closures;
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, device);

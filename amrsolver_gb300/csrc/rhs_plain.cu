@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(256) riemann_face_kernel(BoxTable tb, FaceTabl
   }
 }
 
-// WENO5-Riemann faces (flux_euler = 3), an extension with no counterpart in
+// WENO5-Riemann faces (riemann_weno = 1), an extension with no counterpart in
 // the reference (which pairs WENO5 only with the Lax-Friedrichs split and
 // the two-shock solver only with MUSCL): rho, u_n, p, u_t1, u_t2 are
 // reconstructed to the face from each side with weno5js (left state: cells

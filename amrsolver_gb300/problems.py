@@ -68,9 +68,13 @@ class Closures:
 
 @dataclasses.dataclass
 class Scheme:
-    """cns.* switches: flux_euler 0 = MUSCL/Riemann, 1 = KEEP, 2 = WENO5-JS LLF,
-    3 = WENO5-Riemann (an extension: WENO5-reconstructed primitive states fed
-    to the two-shock solver; no reference counterpart).
+    """cns.* switches: flux_euler 0 = MUSCL/Riemann, 1 = KEEP, 2 = WENO5-JS LLF
+    (any value other than 1 and 2 takes the Riemann path, as in the
+    reference).
+
+    riemann_weno (not a reference switch): on the Riemann path, 0 (default)
+    the reference's MUSCL states, 1 WENO5-Riemann (an extension:
+    WENO5-reconstructed primitive states fed to the two-shock solver).
 
     weno_fast (not a reference switch): 0 (default) evaluates WENO5 in the
     reference's operation order (bit-identical results); 1 forms the weights
@@ -82,6 +86,7 @@ class Scheme:
     order_keep: int = 4
     art_diss: int = 0
     weno_fast: int = 0
+    riemann_weno: int = 0
 
 
 @dataclasses.dataclass

@@ -54,7 +54,7 @@ SCHEMES = {
                   "WENO5-LLF + viscous, common-denominator weights"),
     "muscl": (dict(flux_euler=0, rhs_visc=1), "muscl_visc", "slope_kernel + riemann_face_kernel",
               "riemann_face_kernel_tgv128.md", 7, "MUSCL-Riemann + viscous"),
-    "weno_riemann": (dict(flux_euler=3, rhs_visc=1), "weno_riemann_visc", "weno_riemann_face_kernel",
+    "weno_riemann": (dict(flux_euler=0, riemann_weno=1, rhs_visc=1), "weno_riemann_visc", "weno_riemann_face_kernel",
                      "weno_riemann_face_kernel_tgv128.md", 6,
                      "WENO5-Riemann (extension) + viscous"),
 }

@@ -63,13 +63,11 @@ typedef struct amrs_closures {
 } amrs_closures;
 
 /* cns.* run-time switches read by CNS::read_params (src/CNS.cpp:85-136).
- * flux_euler: 0 = MUSCL + Riemann (src/rhs/Riemann.h), 1 = KEEP split form
- * (src/rhs/CentralKEEP.h), 2 = WENO5-JS with local Lax-Friedrichs splitting
- * (src/rhs/High_resolution.h); 3 = WENO5-Riemann, an extension with no
- * reference counterpart: rho, u_n, p and the tangential velocities
- * reconstructed to each face from both sides with the WENO5-JS stencils,
- * fed to the reference's two-shock solver (src/rhs/Riemann.h:123-249); no
- * reverse pass.  order_keep: 2, 4 or 6.  art_diss: JST. */
+ * flux_euler: 1 = KEEP split form (src/rhs/CentralKEEP.h), 2 = WENO5-JS with
+ * local Lax-Friedrichs splitting (src/rhs/High_resolution.h), any other value
+ * (0 in the reference's inputs) = the Riemann path, as compute_rhs's else
+ * branch (src/tim/CNS_advance.cpp:221-223): MUSCL + two-shock solver
+ * (src/rhs/Riemann.h).  order_keep: 2, 4 or 6.  art_diss: JST. */
 typedef struct amrs_scheme {
   int32_t rhs_euler, rhs_visc, flux_euler, order_keep, art_diss;
   /* WENO5 only (no counterpart in the reference's switches).  0: the
@@ -81,6 +79,12 @@ typedef struct amrs_scheme {
    * differencing amplifies where the RHS is small next to the split fluxes
    * (near-incompressible flow: up to ~1e-9 relative on the mass RHS). */
   int32_t weno_fast;
+  /* Riemann path only (no counterpart in the reference's switches).  0: the
+   * reference's MUSCL characteristic states.  1: WENO5-Riemann, an
+   * extension: rho, u_n, p and the tangential velocities reconstructed to
+   * each face from both sides with the WENO5-JS stencils, fed to the same
+   * two-shock solver (src/rhs/Riemann.h:123-249); no reverse pass. */
+  int32_t riemann_weno;
 } amrs_scheme;
 
 /* Cell-centred index box, inclusive bounds (amrex::Box). */

@@ -18,9 +18,9 @@
 // restatement with that build bit for bit, and tests/golden/*.npz hold
 // vectors produced by that build so the pin also holds where the reference
 // sources are absent.
-// WENO5-Riemann (flux_euler = 3) has no reference counterpart: for it this
-// file is the specification, and its parity is unpinned against the
-// reference.
+// WENO5-Riemann (the riemann_weno extension, flux code 3 here) has no
+// reference counterpart: for it this file is the specification, and its
+// parity is unpinned against the reference.
 //
 // Layout of every field (Array4 convention): component-major, i fastest,
 // ghost-inclusive.  A box [lo,hi] with g ghosts is stored as
@@ -190,7 +190,7 @@ struct Closures {
 struct Scheme {
   int rhs_euler;   // cns.rhs_euler
   int rhs_visc;    // cns.rhs_visc
-  int flux_euler;  // 0 = MUSCL + Riemann, 1 = KEEP, 2 = WENO5-JS LLF, 3 = WENO5-Riemann (extension)
+  int flux_euler;  // 1 = KEEP, 2 = WENO5-JS LLF, 3 = WENO5-Riemann (extension), other = MUSCL + Riemann
   int order_keep;  // 2, 4, 6
   int art_diss;    // JST artificial dissipation
 };
@@ -521,10 +521,10 @@ inline void cns_riemann(int i, int j, int k, int d, const Arr<R>& f, const Arr<R
   f(i, j, k, UET) = fe;
 }
 
-// WENO5-Riemann (flux_euler = 3), an extension with no counterpart in the
-// reference: the reference pairs WENO5 only with the local Lax-Friedrichs
-// split (flux_euler = 2) and the two-shock solver only with MUSCL
-// (flux_euler = 0).  Here rho, u_n, p, u_t1, u_t2 are reconstructed to the
+// WENO5-Riemann (flux code 3: the riemann_weno extension), with no
+// counterpart in the reference: the reference pairs WENO5 only with the
+// local Lax-Friedrichs split (flux_euler = 2) and the two-shock solver only
+// with MUSCL (its Riemann path).  Here rho, u_n, p, u_t1, u_t2 are reconstructed to the
 // d-face below (i,j,k) from each side with weno5js (left state: cells
 // i-3..i+1; right state: the mirror i+2..i-2), density and pressure floored
 // at 1e-40 as the MUSCL states are (src/rhs/Riemann.h:260-272), and the

@@ -38,8 +38,12 @@ def c_closures(cl):
 
 
 def c_scheme(sc):
-    return CScheme(int(sc.rhs_euler), int(sc.rhs_visc), int(sc.flux_euler), int(sc.order_keep),
-                   int(sc.art_diss))
+    # the oracle's flux code: 1 KEEP, 2 WENO5 LLF, 3 WENO5-Riemann (the
+    # riemann_weno extension), anything else MUSCL + Riemann
+    fe = int(sc.flux_euler)
+    if fe not in (1, 2):
+        fe = 3 if int(getattr(sc, "riemann_weno", 0)) else 0
+    return CScheme(int(sc.rhs_euler), int(sc.rhs_visc), fe, int(sc.order_keep), int(sc.art_diss))
 
 
 def _i3(v):

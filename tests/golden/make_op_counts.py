@@ -44,7 +44,7 @@ CHECK_N = 14
 # data-dependent counts: (switches, edge, TGV Mach, mu) of the bench input
 DATA_DEPENDENT = {
     "muscl_visc": (dict(flux_euler=0, rhs_visc=1), 128, 0.1, 1.0 / 1600.0),
-    "weno_riemann_visc": (dict(flux_euler=3, rhs_visc=1), 128, 0.1, 1.0 / 1600.0),
+    "weno_riemann_visc": (dict(flux_euler=0, riemann_weno=1, rhs_visc=1), 128, 0.1, 1.0 / 1600.0),
 }
 
 

@@ -124,6 +124,21 @@ def test_muscl_strong_waves_bitexact(orc, visc):
     np.testing.assert_array_equal(R, ref)
 
 
+def test_other_flux_values_take_the_riemann_path():
+    """compute_rhs sends every flux_euler other than 1 and 2 to the Riemann
+    path (src/tim/CNS_advance.cpp:221-223); the library does the same."""
+    U = P.random_state((10, 9, 8), seed=4, amp=0.2)
+    cl = P.Closures.nondimensional(1.0 / 300.0)
+    R0, _ = gpu_rhs(P.Scheme(flux_euler=0, rhs_visc=1), cl, U, (1.0, 2.0, 3.0))
+    for fe in (-1, 3, 7):
+        R, _ = gpu_rhs(P.Scheme(flux_euler=fe, rhs_visc=1), cl, U, (1.0, 2.0, 3.0))
+        np.testing.assert_array_equal(R, R0)
+    W0, _ = gpu_rhs(P.Scheme(flux_euler=0, riemann_weno=1, rhs_visc=1), cl, U, (1.0, 2.0, 3.0))
+    W, _ = gpu_rhs(P.Scheme(flux_euler=5, riemann_weno=1, rhs_visc=1), cl, U, (1.0, 2.0, 3.0))
+    np.testing.assert_array_equal(W, W0)
+    assert not np.array_equal(W0, R0)
+
+
 def test_tgv_rhs_bitexact_64(orc):
     """TGV 64^3, KEEP4 + viscous: GPU == oracle to the last bit."""
     U, dx = P.tgv(64)

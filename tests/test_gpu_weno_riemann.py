@@ -1,4 +1,4 @@
-"""WENO5-Riemann (flux_euler = 3): WENO5-JS reconstructed primitive states
+"""WENO5-Riemann (riemann_weno = 1): WENO5-JS reconstructed primitive states
 fed to the reference's two-shock Riemann solver.  The reference has no such
 scheme (it pairs WENO5 with the Lax-Friedrichs split only), so parity is
 against the oracle's restatement of the extension (unpinned against the
@@ -34,7 +34,7 @@ def gpu_rhs(scheme, closures, U, dxinv, lo=(0, 0, 0)):
 @pytest.mark.parametrize("visc", [0, 1])
 @pytest.mark.parametrize("n", [(8, 8, 8), (13, 7, 5), (37, 19, 11)])
 def test_weno_riemann_vs_oracle(orc, n, visc):
-    sc = P.Scheme(flux_euler=3, rhs_visc=visc)
+    sc = P.Scheme(flux_euler=0, riemann_weno=1, rhs_visc=visc)
     cl = P.Closures.nondimensional(1.0 / 300.0)
     U = P.random_state(n, seed=sum(n) + 11 * visc, amp=0.3)
     lo = (n[0] % 5 - 2, -n[1], 7)
@@ -52,7 +52,7 @@ def test_weno_riemann_uniform_flow_has_zero_rhs():
     shape = (n[2] + 6, n[1] + 6, n[0] + 6)
     one = np.ones(shape)
     U = P.prims_to_cons(1.3 * one, 0.4 * one, -0.2 * one, 0.7 * one, 0.9 * one, 1.4)
-    R = gpu_rhs(P.Scheme(flux_euler=3, rhs_visc=1), P.Closures.nondimensional(1e-2), U, (3.0, 2.0, 1.0))
+    R = gpu_rhs(P.Scheme(flux_euler=0, riemann_weno=1, rhs_visc=1), P.Closures.nondimensional(1e-2), U, (3.0, 2.0, 1.0))
     assert np.all(R == 0.0)
 
 
@@ -112,11 +112,12 @@ def test_sod_exact_solution_reference_values():
     assert abs(rho[0] - 0.42632) < 1e-5 and abs(rho[1] - 0.26557) < 1e-5
 
 
-def run_sod(flux_euler, nx, stop=0.2, cfl=0.3):
+def run_sod(riemann_weno, nx, stop=0.2, cfl=0.3):
     cl = P.Closures.ideal_gas(gamma=1.4, mw=1.0, Ru=1.0, visc_law=0, cond_law=0)
     U, dx = P.sod(nx, 4, 4)
     bc = (2, -1, -1)
-    lev = cns.CNSLevel(P.Scheme(flux_euler=flux_euler, rhs_visc=0), cl, U, dx, bc_lo=bc, bc_hi=bc)
+    sc = P.Scheme(flux_euler=0, riemann_weno=riemann_weno, rhs_visc=0)
+    lev = cns.CNSLevel(sc, cl, U, dx, bc_lo=bc, bc_hi=bc)
     dt = lev.compute_initial_dt(cfl)
     steps = 0
     while lev.time < stop and steps < 5000:
@@ -134,7 +135,7 @@ def test_weno_riemann_sod_converges_to_exact_solution():
     grid is refined (first order at the discontinuities)."""
     errs = []
     for nx in (64, 128, 256):
-        x, rho, t = run_sod(3, nx)
+        x, rho, t = run_sod(1, nx)
         assert abs(t - 0.2) < 1e-12
         assert np.isfinite(rho).all() and rho.min() > 0.1 and rho.max() < 1.0 + 1e-6
         ex, _, _ = sod_exact(x, t)
@@ -147,11 +148,11 @@ def test_weno_riemann_sod_matches_oracle_run(orc):
     """The whole Sod run (64 cells, dynamic dt, to t = 0.2) against the
     oracle's loop: same step count, same final time, states within 1e-10."""
     nx, stop, cfl = 64, 0.2, 0.3
-    x, rho, t = run_sod(3, nx)
+    x, rho, t = run_sod(1, nx)
     cl = P.Closures.ideal_gas(gamma=1.4, mw=1.0, Ru=1.0, visc_law=0, cond_law=0)
     U, dx = P.sod(nx, 4, 4)
     bc = (2, -1, -1)
-    sc = P.Scheme(flux_euler=3, rhs_visc=0)
+    sc = P.Scheme(flux_euler=0, riemann_weno=1, rhs_visc=0)
     S, tt = U, 0.0
     odt = orc.est_timestep(cl, S, dx, cfl)
     while tt < stop:
@@ -166,7 +167,7 @@ def test_weno_riemann_sod_matches_oracle_run(orc):
 
 
 def test_weno_riemann_vjp_is_rejected():
-    h = capi.Handle(P.Scheme(flux_euler=3, rhs_visc=1), P.Closures.nondimensional(1e-2))
+    h = capi.Handle(P.Scheme(flux_euler=0, riemann_weno=1, rhs_visc=1), P.Closures.nondimensional(1e-2))
     U = P.random_state((8, 8, 8), seed=3)
     Ud = torch.from_numpy(U).cuda()
     with pytest.raises(capi.AmrsError):

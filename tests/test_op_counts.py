@@ -33,6 +33,6 @@ def test_data_dependent_counts_match_oracle(orc):
     data = json.load(open(os.path.join(HERE, "golden", "op_counts.json")))
     assert {"muscl_visc", "weno_riemann_visc"} <= set(data["data_dependent"])
     for name, ent in data["data_dependent"].items():
-        assert P.Scheme(**ent["switches"]).flux_euler in (0, 3), name
+        assert P.Scheme(**ent["switches"]).flux_euler not in (1, 2), name  # the Riemann path
         got = M.tgv_counts(orc, ent["switches"], ent["n"], ent["tgv_mach"], ent["mu"])
         assert got == ent["phases"], name

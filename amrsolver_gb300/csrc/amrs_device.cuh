@@ -86,27 +86,30 @@ __device__ __forceinline__ void keep_pair(const double* q1, const double* q2, do
   constexpr int QN = QU + D;
   const double rhoS = q1[QRHO] + q2[QRHO];
   const double unS = q1[QN] + q2[QN];
-  // t8 = 0.125*rhoS*unS is the common factor of every fghCubic term.  The
-  // reference's fgQuad massflx = 0.25*rhoS*unS equals 2*t8 and its
-  // ke = 0.5*(u1u2+v1v2+w1w2) equals s3/2, both exactly (binary scalings
-  // commute with rounding), so coef*massflx == (2*coef)*t8 and
-  // massflx*ke == t8*s3 to the bit, with three FP64 operations fewer.
-  const double t8 = 0.1250 * rhoS * unS;
+  // Binary scalings commute with rounding (normal range), so every power of
+  // two in the reference's expressions moves into the pair's constant
+  // coefficient, to the bit:
+  //   fghCubic: 0.125*rhoS*unS*h == 0.125*(P*h), P = rhoS*unS;
+  //   fgQuad massflx 0.25*rhoS*unS == 0.25*P, and massflx*ke with
+  //   ke = 0.5*(u1u2+v1v2+w1w2) == 0.125*(P*s3);
+  //   fDiv 0.5*(p1+p2) and fgDiv 0.5*(p1*un2+p2*un1) added to an eighth:
+  //   x/8 + s/2 == (x + 4s)/8 == fma(4, s, x)/8.
+  // So coef*(...) == (coef/8)*(...) with the eighths taken out, and no
+  // FP64 instruction is spent on a power-of-two scaling.
+  const double c8 = 0.125 * coef, c4 = 0.25 * coef;
+  const double P = rhoS * unS;
   const double s3 = q1[QU] * q2[QU] + q1[QV] * q2[QV] + q1[QW] * q2[QW];
-  const double cx = t8 * (q1[QU] + q2[QU]);
-  const double cy = t8 * (q1[QV] + q2[QV]);
-  const double cz = t8 * (q1[QW] + q2[QW]);
-  const double ce = t8 * (q1[QE] + q2[QE]);
-  // fDiv = 0.5*(p1+p2) and fgDiv = 0.5*(p1*un2 + p2*un1) enter sums; the
-  // products by 0.5 are exact, so fma(0.5, s, x) rounds exactly like
-  // x + 0.5*s evaluated in two steps (one FP64 instruction fewer each).
+  const double cx = P * (q1[QU] + q2[QU]);
+  const double cy = P * (q1[QV] + q2[QV]);
+  const double cz = P * (q1[QW] + q2[QW]);
+  const double ce = P * (q1[QE] + q2[QE]);
   const double psum = q1[QPRES] + q2[QPRES];
   const double pu = q1[QPRES] * q2[QN] + q2[QPRES] * q1[QN];
-  T[URHO] = (2.0 * coef) * t8;
-  T[UMX] = coef * (D == 0 ? fma(0.5, psum, cx) : cx);
-  T[UMY] = coef * (D == 1 ? fma(0.5, psum, cy) : cy);
-  T[UMZ] = coef * (D == 2 ? fma(0.5, psum, cz) : cz);
-  T[UET] = coef * fma(0.5, pu, t8 * s3 + ce);
+  T[URHO] = c4 * P;
+  T[UMX] = c8 * (D == 0 ? fma(4.0, psum, cx) : cx);
+  T[UMY] = c8 * (D == 1 ? fma(4.0, psum, cy) : cy);
+  T[UMZ] = c8 * (D == 2 ? fma(4.0, psum, cz) : cz);
+  T[UET] = c8 * fma(4.0, pu, P * s3 + ce);
 }
 
 // Cell-centred viscous fluxes (src/rhs/CNS_hydro_K.h:108-172) from the

@@ -62,14 +62,16 @@ bool covers(const amrs_array4& a, const amrs_box& b, int g, int ncomp) {
   return true;
 }
 
-bool box_ok(const amrs_box& b) {
-  for (int d = 0; d < 3; ++d)
-    if (b.hi[d] < b.lo[d]) return false;
-  return true;
-}
 int bn(const amrs_box& b, int d) { return b.hi[d] - b.lo[d] + 1; }
 long long grown_cells(const amrs_box& b, int g) {
   return (long long)(bn(b, 0) + 2 * g) * (bn(b, 1) + 2 * g) * (bn(b, 2) + 2 * g);
+}
+// Non-empty, and small enough that a box's cells with 3 ghosts fit the
+// kernels' 32-bit per-box cell index (about 1290^3 cells, ~86 GB per state).
+bool box_ok(const amrs_box& b) {
+  for (int d = 0; d < 3; ++d)
+    if (b.hi[d] < b.lo[d] || (long long)b.hi[d] - b.lo[d] >= (1 << 20)) return false;
+  return grown_cells(b, NGHOST) < (1LL << 31);
 }
 
 // The library's internal Euler-flux code: 1 KEEP, 2 WENO5 LLF, 0 MUSCL +

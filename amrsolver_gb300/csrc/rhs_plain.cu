@@ -158,9 +158,11 @@ __device__ __forceinline__ double weno5js(const double s0, const double s1, cons
   const double g = s1 - s3;
   const double d = fma(-2.0, s3, s2) + s4;         // s2 - 2 s3 + s4
   const double f = fma(-4.0, s3, 3.0 * s2) + s4;   // 3 s2 - 4 s3 + s4
-  const double beta0 = (13.0 / 12.0) * a * a + 0.25 * b * b;
-  const double beta1 = (13.0 / 12.0) * c * c + 0.25 * g * g * g * g;
-  const double beta2 = (13.0 / 12.0) * d * d + 0.25 * f * f;
+  // 0.25*b*b == 0.25*(b*b) and 0.25*g*g*g*g == 0.25*(((g*g)*g)*g): the
+  // quarter scales exactly, so x + 0.25*y is one fma(0.25, y, x) (normal range)
+  const double beta0 = fma(0.25, b * b, (13.0 / 12.0) * a * a);
+  const double beta1 = fma(0.25, g * g * g * g, (13.0 / 12.0) * c * c);
+  const double beta2 = fma(0.25, f * f, (13.0 / 12.0) * d * d);
   const double e0 = eps + beta0, e1 = eps + beta1, e2 = eps + beta2;
   const double alpha0 = 0.1 / (e0 * e0);
   const double alpha1 = 0.6 / (e1 * e1);

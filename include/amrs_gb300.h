@@ -30,7 +30,7 @@ extern "C" {
 typedef enum amrs_status {
   AMRS_OK = 0,
   AMRS_ERR_NULL = 1,        /* a required pointer is NULL */
-  AMRS_ERR_BOX = 2,         /* empty box or box outside its array */
+  AMRS_ERR_BOX = 2,         /* empty box, box outside its array, or 2^31+ cells with ghosts */
   AMRS_ERR_BC = 3,          /* unsupported or inconsistent boundary codes */
   AMRS_ERR_SCHEME = 4,      /* unsupported scheme switches */
   AMRS_ERR_RK = 5,          /* order_rk/stages_rk combination the reference rejects */

@@ -85,7 +85,7 @@ SCHEMES = [dict(flux_euler=1, order_keep=o, rhs_visc=v) for o in (2, 4, 6) for v
 
 
 @pytest.mark.parametrize("skw", SCHEMES, ids=lambda d: "-".join("%s%s" % kv for kv in d.items()))
-@pytest.mark.parametrize("n", [(8, 8, 8), (13, 7, 5), (37, 19, 11), (3, 4, 40)])
+@pytest.mark.parametrize("n", [(8, 8, 8), (13, 7, 5), (37, 19, 11), (3, 4, 40), (1, 1, 1), (1, 6, 2), (2, 1, 9)])
 def test_rhs_vs_oracle_random(orc, skw, n):
     sc = P.Scheme(**skw)
     cl = P.Closures.nondimensional(1.0 / 300.0)
@@ -186,6 +186,22 @@ def test_conservation_periodic():
     R, _ = gpu_rhs(P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1), cl, U, [1.0 / h for h in dx])
     scale = np.abs(R).reshape(5, -1).max(axis=1) + 1.0
     assert np.all(np.abs(R.reshape(5, -1).sum(axis=1)) <= 1e-9 * scale * R[0].size)
+
+
+def test_oversized_box_is_rejected():
+    """A box whose cells with ghosts reach 2^31 is refused before anything
+    runs (the arrays passed cover only a 4^3 box, so a missed check would
+    still stop at the layout check)."""
+    import ctypes
+    h = capi.Handle(P.Scheme(), P.Closures.nondimensional(1e-3))
+    U = torch.zeros((5, 10, 10, 10), dtype=torch.float64, device="cuda")
+    out = torch.zeros((5, 4, 4, 4), dtype=torch.float64, device="cuda")
+    L = capi.load()
+    big = capi.c_box((0, 0, 0), (1400, 1400, 1400))
+    st = L.amrs_rhs_box(h.h, ctypes.byref(big), capi.d3((1.0, 1.0, 1.0)), capi.array4(U, (0, 0, 0), 3),
+                        capi.array4(out, (0, 0, 0), 0), None)
+    assert st == 2  # AMRS_ERR_BOX
+    h.sync_check()
 
 
 def test_bad_inputs_fail_loudly():

@@ -106,6 +106,7 @@ SIGNATURES = {
                                    ctypes.POINTER(ctypes.c_int32), Array4, Array4, Array4, Array4, _P, _P]),
     "amrs_sync_check": (_S, [_P, _P]),
     "amrs_probe_fp64_tflops": (_S, [_P, ctypes.POINTER(ctypes.c_double)]),
+    "amrs_debug_wait_timeout": (_S, [_P, ctypes.c_int32, _P]),
     "amrs_profile_stage_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double),
                                     ctypes.POINTER(StageProg), Array4, Array4, Array4, ctypes.c_int32, _P,
                                     ctypes.POINTER(ctypes.c_double)]),
@@ -292,6 +293,11 @@ class Handle:
         v = ctypes.c_double()
         check(self._L.amrs_probe_fp64_tflops(self.h, ctypes.byref(v)), "amrs_probe_fp64_tflops")
         return v.value
+
+    def debug_wait_timeout(self, polls=4096, stream=None):
+        """Run the bounded-wait failure path once (amrs_debug_wait_timeout);
+        the next sync_check raises AmrsError (AMRS_ERR_TIMEOUT)."""
+        check(self._L.amrs_debug_wait_timeout(self.h, int(polls), _stream_ptr(stream)), "amrs_debug_wait_timeout")
 
 
 def fill_halo_box(U, bc_lo, bc_hi, lo=(0, 0, 0), stream=None):

@@ -109,6 +109,8 @@ struct LevelDomain {
 cudaError_t launch_halo_level(const BoxTable& tb, const long long* gpre, const int* owner, long long total, int slot,
                               const LevelDomain& dom, int nsm, cudaStream_t st);
 cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t st);
+// One bounded mbarrier wait that nothing completes; raises *err.
+cudaError_t launch_wait_timeout_probe(int* err, long long polls, cudaStream_t st);
 cudaError_t launch_estdt(const BoxTable& tb, int s_in, long long nvalid, double cfl, unsigned long long* bits,
                          double* dt_out, int nsm, cudaStream_t st);
 

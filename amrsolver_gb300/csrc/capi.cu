@@ -1533,6 +1533,15 @@ amrs_status amrs_sync_check(amrs_handle* h, void* stream) {
   return AMRS_OK;
 }
 
+// Exercises the timeout path of the bounded device waits (see the header).
+amrs_status amrs_debug_wait_timeout(amrs_handle* h, int32_t polls, void* stream) {
+  if (!h) return AMRS_ERR_NULL;
+  if (polls < 1 || polls > (1 << 20)) return AMRS_ERR_SIZE;
+  CK(cudaSetDevice(h->device));
+  CK(launch_wait_timeout_probe(h->derr, polls, static_cast<cudaStream_t>(stream)));
+  return AMRS_OK;
+}
+
 // Measured FP64 FMA throughput of the handle's device in TFLOP/s (an FMA
 // counts 2 flops): 2 CTAs of 256 threads per SM, eight DFMA chains each,
 // timed with CUDA events after one warm-up launch.  Host-synchronising.

@@ -36,10 +36,11 @@ __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// Returns false if the phase did not complete within the spin limit.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+// Returns false if the phase did not complete within `limit` polls.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity,
+                                          long long limit = MBAR_SPIN_LIMIT) {
   const uint32_t a = smem_u32(bar);
-  for (long long it = 0; it < MBAR_SPIN_LIMIT; ++it) {
+  for (long long it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"

@@ -1,5 +1,6 @@
 // Ghost fill and time-step reduction kernels.
 #include "amrs_kernels.h"
+#include "tma.cuh"
 
 namespace amrs {
 
@@ -419,6 +420,23 @@ __global__ void __launch_bounds__(256) fp64_probe_kernel(double* out, int iters,
 
 cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t st) {
   fp64_probe_kernel<<<blocks, 256, 0, st>>>(out, iters, 0.999);
+  return cudaGetLastError();
+}
+
+// ----------------------------------------------------- timeout probe ----
+// The error path of the bounded waits, without a hang: one thread waits on
+// an mbarrier that nothing arrives at, with the same bounded wait the face
+// kernel uses (at most `polls` polls), gives up, raises the error flag and
+// returns.
+__global__ void wait_timeout_probe_kernel(int* err, long long polls) {
+  __shared__ unsigned long long bar;
+  mbar_init(&bar, 1);
+  fence_mbar_init();
+  if (!mbar_wait(&bar, 0u, polls)) atomicExch(err, 1);
+}
+
+cudaError_t launch_wait_timeout_probe(int* err, long long polls, cudaStream_t st) {
+  wait_timeout_probe_kernel<<<1, 1, 0, st>>>(err, polls);
   return cudaGetLastError();
 }
 

@@ -310,6 +310,13 @@ amrs_status amrs_rk_stage_vjp_box(amrs_handle* h, const amrs_box* bx, const doub
  * bounded device-side wait raises when it gives up (AMRS_ERR_TIMEOUT).
  * Host-synchronising. */
 amrs_status amrs_sync_check(amrs_handle* h, void* stream);
+/* Test of the failure path of the bounded device waits: launches one thread
+ * that waits on an mbarrier nothing arrives at, with the face kernel's
+ * bounded wait limited to `polls` polls (1..2^20), after which it raises the
+ * handle's error flag and returns; the next amrs_sync_check reports
+ * AMRS_ERR_TIMEOUT (and clears the flag), and the context stays usable.
+ * Asynchronous on `stream`. */
+amrs_status amrs_debug_wait_timeout(amrs_handle* h, int32_t polls, void* stream);
 /* FP64 FMA throughput of the device (TFLOP/s, FMA = 2 flops), measured
  * by a DFMA-chain kernel: the roofline denominator of this FP64-bound path.
  * Host-synchronising. */

@@ -204,6 +204,27 @@ def test_oversized_box_is_rejected():
     h.sync_check()
 
 
+def test_bounded_wait_timeout_reports_and_context_survives():
+    """A device wait that runs out (an mbarrier nothing arrives at, bounded
+    to a few thousand polls) raises the handle's error flag: sync_check
+    reports AMRS_ERR_TIMEOUT once, clears it, and the next RHS is correct."""
+    U = P.random_state((6, 5, 4), seed=9, amp=0.2)
+    sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1)
+    cl = P.Closures.nondimensional(1.0 / 300.0)
+    h = capi.Handle(sc, cl)
+    h.debug_wait_timeout(4096)
+    with pytest.raises(capi.AmrsError, match="(?i)time"):
+        h.sync_check()
+    h.sync_check()  # cleared
+    out = torch.empty((5, 4, 5, 6), dtype=torch.float64, device="cuda")
+    h.rhs_box(torch.from_numpy(U).cuda(), (1.0, 1.0, 1.0), out)
+    h.sync_check()
+    R, _ = gpu_rhs(sc, cl, U, (1.0, 1.0, 1.0))
+    np.testing.assert_array_equal(out.cpu().numpy(), R)
+    with pytest.raises(capi.AmrsError):
+        h.debug_wait_timeout(0)
+
+
 def test_bad_inputs_fail_loudly():
     h = capi.Handle(P.Scheme(), P.Closures.nondimensional(1e-3))
     U = torch.zeros((5, 10, 10, 10), dtype=torch.float64, device="cuda")

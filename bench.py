@@ -72,6 +72,24 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world, device):
+    """The largest per-rank value over all ranks (the slowest replica's step
+    time); `device` is where the process group's backend reduces ("cuda" for
+    NCCL, "cpu" for gloo)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(cells_per_rank, world, ms_max):
+    """Whole-job cell-updates/s of `world` replicas that each advanced
+    `cells_per_rank` cells in a step of `ms_max` ms (the slowest rank)."""
+    return world * cells_per_rank / (ms_max * 1e-3)
+
+
 class ClockSampler:
     """nvidia-smi samples (200 ms) during the timed region."""
 
@@ -563,12 +581,8 @@ def run_gpu(args, rank, world, local):
     ms = e0.elapsed_time(e1) / args.steps
     clk = clocks.stop()
     lev.h.sync_check()
-    ms_all = ms
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_all = float(t.item())
-    value = world * n ** 3 / (ms_all * 1e-3)
+    ms_all = max_over_ranks(ms, world, "cuda")
+    value = replica_throughput(n ** 3, world, ms_all)
 
     # ---- end to end through the public API with host buffers: every step
     # copies its input state from pinned host memory and reads its result
@@ -607,7 +621,7 @@ def run_gpu(args, rank, world, local):
     e1.record(s_in)
     torch.cuda.synchronize()
     lev2.h.sync_check()
-    ms_e2e = e0.elapsed_time(e1) / args.steps
+    ms_e2e = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, "cuda")
     nbytes = pin_in.numel() * 8
     del lev2, levs
 
@@ -669,7 +683,7 @@ def run_gpu(args, rank, world, local):
                        "l2": "inputs larger than L2 (3 ghosted states + scratch, %.2f GB of states alone)"
                        % (3 * U.nbytes / 1e9), "parallelism": "replicas" if world > 1 else "single GPU",
                        "tma": lev.h.tma_enabled()},
-            "e2e": {"value": world * n ** 3 / (ms_e2e * 1e-3), "unit": UNIT, "h2d_bytes_per_step": nbytes,
+            "e2e": {"value": replica_throughput(n ** 3, world, ms_e2e), "unit": UNIT, "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes},
             "roofline": roofline,
             "gpu_launches": args.steps * 3 * spec[4],

@@ -107,6 +107,8 @@ SIGNATURES = {
     "amrs_sync_check": (_S, [_P, _P]),
     "amrs_probe_fp64_tflops": (_S, [_P, ctypes.POINTER(ctypes.c_double)]),
     "amrs_debug_wait_timeout": (_S, [_P, ctypes.c_int32, _P]),
+    "amrs_average_down": (_S, [ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_int32), Array4, Array4, ctypes.c_int32,
+                               ctypes.c_int32, _P]),
     "amrs_profile_stage_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double),
                                     ctypes.POINTER(StageProg), Array4, Array4, Array4, ctypes.c_int32, _P,
                                     ctypes.POINTER(ctypes.c_double)]),
@@ -306,6 +308,19 @@ def fill_halo_box(U, bc_lo, bc_hi, lo=(0, 0, 0), stream=None):
     bx = c_box(lo, (nx, ny, nz))
     check(L.amrs_fill_halo_box(ctypes.byref(bx), i3(bc_lo), i3(bc_hi), array4(U, lo, NGHOST), _stream_ptr(stream)),
           "amrs_fill_halo_box")
+
+
+def average_down(fine, crse, crse_lo, ratio, fine_g=0, crse_g=0, scomp=0, ncomp=None, stream=None):
+    """amrs_average_down: the valid cells of `crse` (box at `crse_lo`, `crse_g`
+    ghost layers in the tensor) become the means of their fine cells in
+    `fine` (valid box at crse_lo * ratio, `fine_g` ghost layers)."""
+    L = load()
+    nz, ny, nx = (s - 2 * crse_g for s in crse.shape[1:])
+    bx = c_box(crse_lo, (nx, ny, nz))
+    flo = tuple(int(a) * int(r) for a, r in zip(crse_lo, ratio))
+    nc = crse.shape[0] - scomp if ncomp is None else ncomp
+    check(L.amrs_average_down(ctypes.byref(bx), i3(ratio), array4(fine, flo, fine_g), array4(crse, crse_lo, crse_g),
+                              int(scomp), int(nc), _stream_ptr(stream)), "amrs_average_down")
 
 
 class BoxList:

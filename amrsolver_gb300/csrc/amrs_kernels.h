@@ -109,6 +109,9 @@ struct LevelDomain {
 cudaError_t launch_halo_level(const BoxTable& tb, const long long* gpre, const int* owner, long long total, int slot,
                               const LevelDomain& dom, int nsm, cudaStream_t st);
 cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t st);
+// amrex::average_down of cell-centred data (coarse box lo, extents n, ratio r).
+cudaError_t launch_avgdown(const DArr& fine, const DArr& crse, const int lo[3], const int n[3], const int r[3],
+                           int scomp, int ncomp, double volfrac, int nsm, cudaStream_t st);
 // One bounded mbarrier wait that nothing completes; raises *err.
 cudaError_t launch_wait_timeout_probe(int* err, long long polls, cudaStream_t st);
 cudaError_t launch_estdt(const BoxTable& tb, int s_in, long long nvalid, double cfl, unsigned long long* bits,

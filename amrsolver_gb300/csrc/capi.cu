@@ -857,6 +857,32 @@ amrs_status amrs_fill_halo_box(const amrs_box* domain, const int32_t bc_lo[3], c
   return AMRS_OK;
 }
 
+amrs_status amrs_average_down(const amrs_box* crse_box, const int32_t ratio[3], amrs_array4 fine, amrs_array4 crse,
+                               int32_t scomp, int32_t ncomp, void* stream) {
+  if (!crse_box || !ratio) return AMRS_ERR_NULL;
+  if (!box_ok(*crse_box)) return AMRS_ERR_BOX;
+  if (scomp < 0 || ncomp < 1) return AMRS_ERR_LAYOUT;
+  amrs_box fb;
+  int r[3], lo[3], n[3];
+  for (int d = 0; d < 3; ++d) {
+    if (ratio[d] < 1 || ratio[d] > 16) return AMRS_ERR_SIZE;
+    r[d] = ratio[d];
+    lo[d] = crse_box->lo[d];
+    n[d] = bn(*crse_box, d);
+    fb.lo[d] = crse_box->lo[d] * ratio[d];
+    fb.hi[d] = (crse_box->hi[d] + 1) * ratio[d] - 1;
+  }
+  if (!box_ok(fb)) return AMRS_ERR_BOX;
+  if (!covers(fine, fb, 0, scomp + ncomp) || !covers(crse, *crse_box, 0, scomp + ncomp)) return AMRS_ERR_LAYOUT;
+  if (fine.p == crse.p) return AMRS_ERR_LAYOUT;
+  int dev = 0, nsm = 1;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  CK(launch_avgdown(to_darr(fine), to_darr(crse), lo, n, r, scomp, ncomp, 1.0 / (double)(r[0] * r[1] * r[2]), nsm,
+                    static_cast<cudaStream_t>(stream)));
+  return AMRS_OK;
+}
+
 amrs_status amrs_est_timestep_box(amrs_handle* h, const amrs_box* bx, const double dx[3], double cfl,
                                   amrs_array4 state, double* dt_device, void* stream) {
   if (!h || !bx || !dx || !dt_device) return AMRS_ERR_NULL;

@@ -15,6 +15,7 @@
 // (2-deep ring, filled by TMA when the layout allows) and evaluates every
 // KEEP pair term once: a pair (a+l, a) feeds l faces, so it is stored in
 // shared memory (x, y) or carried in registers (z) and reused.
+#include <atomic>
 #include "amrs_boxes.cuh"
 #include "amrs_kernels.h"
 #include "tma.cuh"
@@ -455,12 +456,17 @@ template <int ORDER, bool VISC>
 static cudaError_t launch_face_t(const BoxTable& tb, int s_in, int s_s1, int s_out, const DProg& prog, int rhs_only,
                                  const TmaDesc& tma, int* err, int grid, cudaStream_t st) {
   const int smem = keep_smem_bytes<ORDER>();
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(keep_face_kernel<ORDER, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         smem);
+  // the shared-memory opt-in is a per-device function attribute: set it once
+  // for each device this process launches on (devices 0..63 tracked)
+  static std::atomic<unsigned long long> attr_set{0ull};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (dev >= 64 || !(attr_set.load() & bit)) {
+    e = cudaFuncSetAttribute(keep_face_kernel<ORDER, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    attr_set = true;
+    attr_set.fetch_or(bit);
   }
   keep_face_kernel<ORDER, VISC><<<grid, F_THREADS, smem, st>>>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err);
   return cudaGetLastError();

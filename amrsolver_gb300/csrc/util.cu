@@ -423,6 +423,41 @@ cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t s
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------ average_down ----
+// amrex::average_down of cell-centred data on a Cartesian grid (called by
+// CNS::avgDown, src/CNS.cpp:513-530): each coarse cell of the box becomes
+// the mean of its rx*ry*rz fine cells, summed from zero with the fine k
+// offset outermost and i innermost and scaled by 1/(rx*ry*rz), the order of
+// AMReX's amrex_avgdown.  One thread per coarse cell, all components.
+__global__ void __launch_bounds__(256) avgdown_kernel(DArr fine, DArr crse, int lo0, int lo1, int lo2, int nx,
+                                                      int ny, long long total, int rx, int ry, int rz, int scomp,
+                                                      int ncomp, double volfrac) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(g % nx) + lo0;
+    const long long t = g / nx;
+    const int j = (int)(t % ny) + lo1, k = (int)(t / ny) + lo2;
+    for (int n = scomp; n < scomp + ncomp; ++n) {
+      double c = 0.0;
+      for (int kr = 0; kr < rz; ++kr)
+        for (int jr = 0; jr < ry; ++jr)
+          for (int ir = 0; ir < rx; ++ir) c += fine(i * rx + ir, j * ry + jr, k * rz + kr, n);
+      crse(i, j, k, n) = volfrac * c;
+    }
+  }
+}
+
+cudaError_t launch_avgdown(const DArr& fine, const DArr& crse, const int lo[3], const int n[3], const int r[3],
+                           int scomp, int ncomp, double volfrac, int nsm, cudaStream_t st) {
+  const long long total = (long long)n[0] * n[1] * n[2];
+  if (total <= 0) return cudaSuccess;
+  long long blocks = (total + 255) / 256;
+  if (blocks > 8LL * nsm) blocks = 8LL * nsm;
+  avgdown_kernel<<<(int)blocks, 256, 0, st>>>(fine, crse, lo[0], lo[1], lo[2], n[0], n[1], total, r[0], r[1], r[2],
+                                               scomp, ncomp, volfrac);
+  return cudaGetLastError();
+}
+
 // ----------------------------------------------------- timeout probe ----
 // The error path of the bounded waits, without a hang: one thread waits on
 // an mbarrier that nothing arrives at, with the same bounded wait the face

@@ -310,6 +310,16 @@ amrs_status amrs_rk_stage_vjp_box(amrs_handle* h, const amrs_box* bx, const doub
  * bounded device-side wait raises when it gives up (AMRS_ERR_TIMEOUT).
  * Host-synchronising. */
 amrs_status amrs_sync_check(amrs_handle* h, void* stream);
+/* amrex::average_down for cell-centred data on a Cartesian grid, the call
+ * CNS::avgDown makes after a fine level's step (src/CNS.cpp:513-530): every
+ * cell of `crse_box` (coarse index space) becomes the mean of its
+ * ratio[0]*ratio[1]*ratio[2] fine cells, summed from zero with the fine k
+ * offset outermost and i innermost, then scaled by 1/(rx*ry*rz) (AMReX's
+ * amrex_avgdown order), for components scomp..scomp+ncomp-1.  `fine` must
+ * cover the refined box, `crse` the coarse box; ratios 1..16.  Asynchronous
+ * on `stream`, on the current device. */
+amrs_status amrs_average_down(const amrs_box* crse_box, const int32_t ratio[3], amrs_array4 fine, amrs_array4 crse,
+                              int32_t scomp, int32_t ncomp, void* stream);
 /* Test of the failure path of the bounded device waits: launches one thread
  * that waits on an mbarrier nothing arrives at, with the face kernel's
  * bounded wait limited to `polls` polls (1..2^20), after which it raises the

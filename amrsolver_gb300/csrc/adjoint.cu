@@ -17,6 +17,7 @@
 // Non-smooth points follow the branch the forward pass takes (max(1e-40,rho)
 // passes the derivative only when rho > 1e-40).  Sums are deterministic:
 // every output element is written by exactly one thread.
+#include "adjoint_common.cuh"
 #include "amrs_kernels.h"
 
 namespace amrs {
@@ -28,7 +29,6 @@ struct AdjRec {
   DArr vg;      // viscous cotangents over grow(box,1): centre u,v,w,T (0..3), gradients (4..15)
   int visc;     // vg holds data (the viscous reverse pass ran)
 };
-constexpr int NQA = 6;  // rho, u, v, w, T, p (e = cv*T folded into T)
 
 __device__ __forceinline__ double vget(const DArr& v, const BoxRec& R, int i, int j, int k, int n) {
   if (i < R.lo[0] || i > R.hi[0] || j < R.lo[1] || j > R.hi[1] || k < R.lo[2] || k > R.hi[2]) return 0.0;
@@ -303,28 +303,10 @@ __global__ void __launch_bounds__(256) adj_gather_kernel(BoxTable tb, AdjRec ar,
       }
     }
     // cons2prim VJP (src/rhs/CNS_hydro_K.h:15-34)
-    const DArr Q = R.q;
-    const long long oq = Q.off(i, j, k);
-    const double rho = Q.p[oq + QRHO * Q.ns], u = Q.p[oq + QU * Q.ns], v = Q.p[oq + QV * Q.ns],
-                 w = Q.p[oq + QW * Q.ns], T = Q.p[oq + QT * Q.ns];
-    double rb = qb[QRHO], ub = qb[QU], vb = qb[QV], wb = qb[QW];
-    double pb = qb[QPRES] + qb[QT] / (rho * cl.Rspec);
-    rb += -qb[QT] * T / rho;
-    const double eib = (cl.gamma - 1.0) * pb;  // d/d rhoei
-    const double keb = -eib;                   // d/d rhoke
-    rb += 0.5 * (u * u + v * v + w * w) * keb;
-    ub += rho * u * keb;
-    vb += rho * v * keb;
-    wb += rho * w * keb;
-    const double rinv = 1.0 / rho;
-    rb += -(ub * u + vb * v + wb * w) * rinv;
-    const DArr U = R.slot[0];
-    const double rho_raw = U(i, j, k, URHO);
-    Ub.p[ou] = (rho_raw > 1e-40) ? rb : 0.0;
-    Ub.p[ou + Ub.ns] = ub * rinv;
-    Ub.p[ou + 2 * Ub.ns] = vb * rinv;
-    Ub.p[ou + 3 * Ub.ns] = wb * rinv;
-    Ub.p[ou + 4 * Ub.ns] = eib;
+    double ub5[5];
+    cons2prim_vjp(R, cl, i, j, k, qb, ub5);
+#pragma unroll
+    for (int n = 0; n < 5; ++n) Ub.p[ou + n * Ub.ns] = ub5[n];
   }
 }
 

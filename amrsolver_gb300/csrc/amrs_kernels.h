@@ -45,6 +45,9 @@ cudaError_t launch_weno_point(const BoxTable& tb, const FaceTable& ft, int s_in,
 // the WENO face kernel alone (point fluxes already current)
 cudaError_t launch_weno_faces(const BoxTable& tb, const FaceTable& ft, int s_in, long long nfaces[3], bool ref_order,
                               int nsm, cudaStream_t st);
+// MUSCL slopes and face-state terms alone (the reverse pass recomputes them)
+cudaError_t launch_slopes(const BoxTable& tb, const FaceTable& ft, const long long* spre_d[3], long long nslope[3],
+                          int nsm, cudaStream_t st);
 cudaError_t launch_riemann(const BoxTable& tb, const FaceTable& ft, const long long* spre_d[3],
                            long long nslope[3], long long nfaces[3], int nsm, cudaStream_t st);
 // WENO5-reconstructed primitive states + the two-shock solver (riemann_weno = 1)
@@ -77,6 +80,10 @@ struct AdjRecHost {
 // order 0: viscous part and cons2prim reverse only (no KEEP pairs)
 cudaError_t launch_rhs_vjp(int order, const BoxTable& tb, const AdjRecHost& ah, double* pbar, int nsm,
                            cudaStream_t st);
+// MUSCL-Riemann Euler part of the RHS VJP, added to ubar (adjoint_muscl.cu)
+size_t muscl_vjp_buffer_bytes(const int n[3]);
+cudaError_t launch_muscl_vjp(const BoxTable& tb, const FaceRec& fr, const DArr& vbar, const DArr& ubar, double* buf,
+                             const int n[3], int nsm, cudaStream_t st);
 // WENO5 Euler part of the RHS VJP, added to ubar (adjoint_weno.cu)
 size_t weno_vjp_buffer_bytes(const int n[3]);
 cudaError_t launch_weno_vjp(const BoxTable& tb, const FaceRec& fr, const DArr& vbar, const DArr& ubar, double* buf,

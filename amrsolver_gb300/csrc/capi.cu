@@ -1382,17 +1382,19 @@ namespace {
 struct AdjScratch {
   AdjRecHost ah;
   DArr vbar_tmp, ubar_tmp;
-  double* wbuf = nullptr;  // WENO per-face cotangent slots
+  double* wbuf = nullptr;  // WENO / MUSCL per-face and per-cell cotangent slots
   int order = 0;           // KEEP order of the pair pass (0: none)
 };
 
-// Schemes with a reverse pass: KEEP (+ viscous), WENO5 LLF (+ viscous), viscous only.
+// Schemes with a reverse pass: KEEP, WENO5 LLF, MUSCL-Riemann (each + viscous),
+// viscous only.  (Internal flux codes: 0 MUSCL, 3 WENO5-Riemann.)
 bool vjp_scheme(const amrs_scheme& s) {
   if (s.art_diss) return false;
   if (!s.rhs_euler) return s.rhs_visc != 0;
-  return s.flux_euler == 1 || s.flux_euler == 2;
+  return s.flux_euler == 1 || s.flux_euler == 2 || s.flux_euler == 0;
 }
 bool weno_scheme(const amrs_scheme& s) { return s.rhs_euler && s.flux_euler == 2; }
+bool muscl_scheme(const amrs_scheme& s) { return s.rhs_euler && s.flux_euler == 0; }
 
 amrs_status adj_prepare(amrs_handle* h, const amrs_box& B, AdjScratch& S, cudaStream_t st) {
   S.order = fused_path(h->sc) ? h->sc.order_keep : 0;
@@ -1404,7 +1406,9 @@ amrs_status adj_prepare(amrs_handle* h, const amrs_box& B, AdjScratch& S, cudaSt
   const size_t o_vg = off; off = align_up(off + cells(1) * 16 * 8, 256);
   const size_t o_v = off; off = align_up(off + cells(0) * 5 * 8, 256);
   const size_t o_u = off; off = align_up(off + cells(3) * 5 * 8, 256);
-  const size_t o_w = off; off = align_up(off + (weno_scheme(h->sc) ? weno_vjp_buffer_bytes(nb) : 0), 256);
+  const size_t euler_bytes = weno_scheme(h->sc) ? weno_vjp_buffer_bytes(nb)
+                            : (muscl_scheme(h->sc) ? muscl_vjp_buffer_bytes(nb) : 0);
+  const size_t o_w = off; off = align_up(off + euler_bytes, 256);
   if (off > h->adj_bytes) {
     if (h->adj) { CK(cudaStreamSynchronize(st)); cudaFree(h->adj); h->adj = nullptr; h->adj_bytes = 0; }
     CK(cudaMalloc(&h->adj, off));
@@ -1426,14 +1430,14 @@ amrs_status adj_prepare(amrs_handle* h, const amrs_box& B, AdjScratch& S, cudaSt
   S.ubar_tmp = mk(o_u, 3);
   for (int d = 0; d < 3; ++d) S.ah.n[d] = bn(B, d);
   S.ah.visc = h->sc.rhs_visc != 0;
-  S.wbuf = reinterpret_cast<double*>(P + o_w);
+  S.wbuf = reinterpret_cast<double*>(P + o_w);  // WENO or MUSCL per-face / per-cell slots
   if (H > 0) CK(cudaMemsetAsync(P + o_pair, 0, cells(3) * 12 * 8 * 3 * H, st));
   return AMRS_OK;
 }
 
 // Reverse pass of one RHS of the list's single box (state in slot 0):
 // primitives, then the KEEP-pair / viscous / cons2prim reverse kernels,
-// then the WENO5 Euler part.
+// then the WENO5 or MUSCL-Riemann Euler part.
 cudaError_t rhs_vjp_launch(amrs_handle* h, List& L, const amrs_box& B, AdjScratch& S, double* param_bar,
                            cudaStream_t st) {
   cudaError_t e = launch_prims(L.tb, 0, L.tot_p, h->nsm, st);
@@ -1442,6 +1446,12 @@ cudaError_t rhs_vjp_launch(amrs_handle* h, List& L, const amrs_box& B, AdjScratc
     const int nb[3] = {bn(B, 0), bn(B, 1), bn(B, 2)};
     e = launch_weno_point(L.tb, L.ft, 0, L.tot_g, h->nsm, st);
     if (e == cudaSuccess) e = launch_weno_vjp(L.tb, L.hface[0], S.ah.vbar, S.ah.ubar, S.wbuf, nb, h->nsm, st);
+  }
+  if (e == cudaSuccess && muscl_scheme(h->sc)) {
+    const int nb[3] = {bn(B, 0), bn(B, 1), bn(B, 2)};
+    long long ns[3] = {L.tot_s[0], L.tot_s[1], L.tot_s[2]};
+    e = launch_slopes(L.tb, L.ft, L.d_spre, ns, h->nsm, st);
+    if (e == cudaSuccess) e = launch_muscl_vjp(L.tb, L.hface[0], S.ah.vbar, S.ah.ubar, S.wbuf, nb, h->nsm, st);
   }
   return e;
 }

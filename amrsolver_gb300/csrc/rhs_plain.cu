@@ -707,6 +707,14 @@ cudaError_t launch_weno(const BoxTable& tb, const FaceTable& ft, int s_in, long 
   return cudaGetLastError();
 }
 
+cudaError_t launch_slopes(const BoxTable& tb, const FaceTable& ft, const long long* spre_d[3], long long nslope[3],
+                          int nsm, cudaStream_t st) {
+  const long long ts = nslope[0] + nslope[1] + nslope[2];
+  slope_kernel<<<grid_for(ts, nsm), 256, 0, st>>>(tb, ft, spre_d[0], spre_d[1], spre_d[2], nslope[0], nslope[1],
+                                                  nslope[2]);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_riemann(const BoxTable& tb, const FaceTable& ft, const long long* spre_d[3], long long nslope[3],
                            long long nfaces[3], int nsm, cudaStream_t st) {
   const long long ts = nslope[0] + nslope[1] + nslope[2];

@@ -276,9 +276,9 @@ amrs_status amrs_boxlist_totals(amrs_boxlist* bl, int32_t slot, double scale, do
 /* ---- adjoint ----------------------------------------------------------- */
 
 /* Vector-Jacobian product of one RHS evaluation of one box (KEEP, WENO5
- * LLF or no Euler flux, each with or without viscous fluxes; JST and MUSCL
- * Riemann return AMRS_ERR_SCHEME; no counterpart in the reference, whose
- * lib/autodiff is absent):
+ * LLF, MUSCL-Riemann or no Euler flux, each with or without viscous fluxes;
+ * JST and WENO5-Riemann return AMRS_ERR_SCHEME; no counterpart in the
+ * reference, whose lib/autodiff is absent):
  * given the ghost-filled state and a cotangent `vbar` on the valid cells,
  * writes ubar = (d dSdt/d state)^T vbar into `ubar` over the ghosted box
  * (ghost entries hold the sensitivities to ghost values).  `ubar` is

@@ -138,9 +138,9 @@ def test_weno_step_vjp_dot_product(orc):
     assert abs(lhs - rhs) <= 1e-11 * (abs(lhs) + np.linalg.norm(g) * np.linalg.norm(JW)), (lhs, rhs)
 
 
-def test_riemann_vjp_is_rejected():
+def test_jst_vjp_is_rejected():
     cl = P.Closures.nondimensional(1e-2)
-    h = capi.Handle(P.Scheme(flux_euler=0, rhs_visc=1), cl)
+    h = capi.Handle(P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1, art_diss=1), cl)
     U, dx = turbulent_state(8, seed=1)
     ubar = torch.empty_like(dev(U))
     with pytest.raises(capi.AmrsError):

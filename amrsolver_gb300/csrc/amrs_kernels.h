@@ -84,6 +84,10 @@ cudaError_t launch_rhs_vjp(int order, const BoxTable& tb, const AdjRecHost& ah, 
 size_t muscl_vjp_buffer_bytes(const int n[3]);
 cudaError_t launch_muscl_vjp(const BoxTable& tb, const FaceRec& fr, const DArr& vbar, const DArr& ubar, double* buf,
                              const int n[3], int nsm, cudaStream_t st);
+// WENO5-Riemann Euler part of the RHS VJP, added to ubar (adjoint_weno_riemann.cu)
+size_t weno_riemann_vjp_buffer_bytes(const int n[3]);
+cudaError_t launch_weno_riemann_vjp(const BoxTable& tb, const DArr& vbar, const DArr& ubar, double* buf,
+                                    const int n[3], int nsm, cudaStream_t st);
 // WENO5 Euler part of the RHS VJP, added to ubar (adjoint_weno.cu)
 size_t weno_vjp_buffer_bytes(const int n[3]);
 cudaError_t launch_weno_vjp(const BoxTable& tb, const FaceRec& fr, const DArr& vbar, const DArr& ubar, double* buf,

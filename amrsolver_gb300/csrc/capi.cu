@@ -1386,15 +1386,17 @@ struct AdjScratch {
   int order = 0;           // KEEP order of the pair pass (0: none)
 };
 
-// Schemes with a reverse pass: KEEP, WENO5 LLF, MUSCL-Riemann (each + viscous),
-// viscous only.  (Internal flux codes: 0 MUSCL, 3 WENO5-Riemann.)
+// Schemes with a reverse pass: KEEP, WENO5 LLF, MUSCL-Riemann, WENO5-Riemann
+// (each + viscous), viscous only.  (Internal flux codes: 0 MUSCL, 3
+// WENO5-Riemann.)
 bool vjp_scheme(const amrs_scheme& s) {
   if (s.art_diss) return false;
   if (!s.rhs_euler) return s.rhs_visc != 0;
-  return s.flux_euler == 1 || s.flux_euler == 2 || s.flux_euler == 0;
+  return s.flux_euler >= 0 && s.flux_euler <= 3;
 }
 bool weno_scheme(const amrs_scheme& s) { return s.rhs_euler && s.flux_euler == 2; }
 bool muscl_scheme(const amrs_scheme& s) { return s.rhs_euler && s.flux_euler == 0; }
+bool weno_riemann_scheme(const amrs_scheme& s) { return s.rhs_euler && s.flux_euler == 3; }
 
 amrs_status adj_prepare(amrs_handle* h, const amrs_box& B, AdjScratch& S, cudaStream_t st) {
   S.order = fused_path(h->sc) ? h->sc.order_keep : 0;
@@ -1406,8 +1408,10 @@ amrs_status adj_prepare(amrs_handle* h, const amrs_box& B, AdjScratch& S, cudaSt
   const size_t o_vg = off; off = align_up(off + cells(1) * 16 * 8, 256);
   const size_t o_v = off; off = align_up(off + cells(0) * 5 * 8, 256);
   const size_t o_u = off; off = align_up(off + cells(3) * 5 * 8, 256);
-  const size_t euler_bytes = weno_scheme(h->sc) ? weno_vjp_buffer_bytes(nb)
-                            : (muscl_scheme(h->sc) ? muscl_vjp_buffer_bytes(nb) : 0);
+  const size_t euler_bytes = weno_scheme(h->sc)         ? weno_vjp_buffer_bytes(nb)
+                            : muscl_scheme(h->sc)        ? muscl_vjp_buffer_bytes(nb)
+                            : weno_riemann_scheme(h->sc) ? weno_riemann_vjp_buffer_bytes(nb)
+                                                         : 0;
   const size_t o_w = off; off = align_up(off + euler_bytes, 256);
   if (off > h->adj_bytes) {
     if (h->adj) { CK(cudaStreamSynchronize(st)); cudaFree(h->adj); h->adj = nullptr; h->adj_bytes = 0; }
@@ -1437,7 +1441,7 @@ amrs_status adj_prepare(amrs_handle* h, const amrs_box& B, AdjScratch& S, cudaSt
 
 // Reverse pass of one RHS of the list's single box (state in slot 0):
 // primitives, then the KEEP-pair / viscous / cons2prim reverse kernels,
-// then the WENO5 or MUSCL-Riemann Euler part.
+// then the WENO5, MUSCL-Riemann or WENO5-Riemann Euler part.
 cudaError_t rhs_vjp_launch(amrs_handle* h, List& L, const amrs_box& B, AdjScratch& S, double* param_bar,
                            cudaStream_t st) {
   cudaError_t e = launch_prims(L.tb, 0, L.tot_p, h->nsm, st);
@@ -1452,6 +1456,10 @@ cudaError_t rhs_vjp_launch(amrs_handle* h, List& L, const amrs_box& B, AdjScratc
     long long ns[3] = {L.tot_s[0], L.tot_s[1], L.tot_s[2]};
     e = launch_slopes(L.tb, L.ft, L.d_spre, ns, h->nsm, st);
     if (e == cudaSuccess) e = launch_muscl_vjp(L.tb, L.hface[0], S.ah.vbar, S.ah.ubar, S.wbuf, nb, h->nsm, st);
+  }
+  if (e == cudaSuccess && weno_riemann_scheme(h->sc)) {
+    const int nb[3] = {bn(B, 0), bn(B, 1), bn(B, 2)};
+    e = launch_weno_riemann_vjp(L.tb, S.ah.vbar, S.ah.ubar, S.wbuf, nb, h->nsm, st);
   }
   return e;
 }

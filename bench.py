@@ -334,13 +334,13 @@ def bench_ensemble(torch, capi, P, nmembers=64, n=48, steps=3, warmup=2):
             % (nmembers, n), "cells": cells, "ms_per_step": ms, "cell_updates_per_s": cells / (ms * 1e-3)}
 
 
-def bench_adjoint(torch, P, steps=3):
+def bench_adjoint(torch, P, steps=3, scheme=None, label="KEEP4 + viscous"):
     """TGV 64^3, M=0.1, Re=400: one SSPRK3 step forward (keeping the stage
     inputs the adjoint needs) vs the step's VJP (three stage VJPs)."""
     from amrsolver_gb300 import adjoint, cns
     n = 64
     U, dx = P.tgv(n, mach=0.1)
-    sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1)
+    sc = P.Scheme(**(scheme or dict(flux_euler=1, order_keep=4, rhs_visc=1)))
     lev = cns.CNSLevel(sc, P.Closures.nondimensional(1.0 / 400.0), U, dx)
     dt = 1e-3
     S1 = lev.S.clone()
@@ -370,7 +370,7 @@ def bench_adjoint(torch, P, steps=3):
     torch.cuda.synchronize()
     adj = e0.elapsed_time(e1) / steps
     lev.h.sync_check()
-    return {"workload": "TGV 64^3 M=0.1 Re=400, one SSPRK3 step", "forward_ms": fwd,
+    return {"workload": "TGV 64^3 M=0.1 Re=400, %s, one SSPRK3 step" % label, "forward_ms": fwd,
             "forward_keeping_stages_ms": fwd_save, "adjoint_ms": adj, "adjoint_over_forward": adj / fwd}
 
 
@@ -693,6 +693,10 @@ def run_gpu(args, rank, world, local):
             result["batched"] = bench_batched(torch, capi, P)
             result["ensemble"] = bench_ensemble(torch, capi, P)
             result["adjoint"] = bench_adjoint(torch, P)
+            result["adjoint_muscl"] = bench_adjoint(torch, P, scheme=dict(flux_euler=0, rhs_visc=1),
+                                                    label="MUSCL-Riemann + viscous")
+            result["adjoint_weno_riemann"] = bench_adjoint(
+                torch, P, scheme=dict(flux_euler=0, riemann_weno=1, rhs_visc=1), label="WENO5-Riemann + viscous")
             result["level"] = bench_level(torch, capi, P, n=n)
             result["sod_device_loop"] = bench_sod(torch, capi, P)
         if not args.skip_large:

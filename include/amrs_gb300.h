@@ -83,7 +83,7 @@ typedef struct amrs_scheme {
    * reference's MUSCL characteristic states.  1: WENO5-Riemann, an
    * extension: rho, u_n, p and the tangential velocities reconstructed to
    * each face from both sides with the WENO5-JS stencils, fed to the same
-   * two-shock solver (src/rhs/Riemann.h:123-249); no reverse pass. */
+   * two-shock solver (src/rhs/Riemann.h:123-249). */
   int32_t riemann_weno;
 } amrs_scheme;
 
@@ -276,8 +276,8 @@ amrs_status amrs_boxlist_totals(amrs_boxlist* bl, int32_t slot, double scale, do
 /* ---- adjoint ----------------------------------------------------------- */
 
 /* Vector-Jacobian product of one RHS evaluation of one box (KEEP, WENO5
- * LLF, MUSCL-Riemann or no Euler flux, each with or without viscous fluxes;
- * JST and WENO5-Riemann return AMRS_ERR_SCHEME; no counterpart in the
+ * LLF, MUSCL-Riemann, WENO5-Riemann or no Euler flux, each with or without
+ * viscous fluxes; JST returns AMRS_ERR_SCHEME; no counterpart in the
  * reference, whose lib/autodiff is absent):
  * given the ghost-filled state and a cotangent `vbar` on the valid cells,
  * writes ubar = (d dSdt/d state)^T vbar into `ubar` over the ghosted box

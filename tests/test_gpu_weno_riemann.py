@@ -166,10 +166,24 @@ def test_weno_riemann_sod_matches_oracle_run(orc):
     assert G.relmax(rho[None], P.valid(S)[0, 2, 2, :][None]) <= 1e-10
 
 
-def test_weno_riemann_vjp_is_rejected():
-    h = capi.Handle(P.Scheme(flux_euler=0, riemann_weno=1, rhs_visc=1), P.Closures.nondimensional(1e-2))
-    U = P.random_state((8, 8, 8), seed=3)
+@pytest.mark.parametrize("visc", [0, 1])
+def test_weno_riemann_rhs_vjp_dot_product(orc, visc):
+    """<v, J w> from the oracle's dual-number JVP against <J^T v, w> from the
+    GPU reverse pass (same branches, so equal to rounding)."""
+    from tests.test_gpu_adjoint import scaled_direction
+    sc = P.Scheme(flux_euler=0, riemann_weno=1, rhs_visc=visc)
+    cl = P.Closures.nondimensional(1.0 / 300.0)
+    n = (11, 9, 8)
+    U = P.random_state(n, seed=61 + visc, amp=0.25)
+    dxinv = (1.7, 2.9, 0.8)
+    v = np.random.default_rng(62 + visc).standard_normal((5, n[2], n[1], n[0]))
+    W = scaled_direction(U, 63 + visc)
+    _, JW = orc.rhs_jvp(sc, cl, U, W, dxinv, nthreads=4)
+    h = capi.Handle(sc, cl)
     Ud = torch.from_numpy(U).cuda()
-    with pytest.raises(capi.AmrsError):
-        h.rhs_vjp_box(Ud, torch.zeros((5, 8, 8, 8), dtype=torch.float64, device="cuda"), torch.empty_like(Ud),
-                      [1.0, 1.0, 1.0])
+    ubar = torch.empty_like(Ud)
+    h.rhs_vjp_box(Ud, torch.from_numpy(v).cuda(), ubar, dxinv)
+    h.sync_check()
+    lhs = float(np.sum(v * JW))
+    rhs = float(np.sum(ubar.cpu().numpy() * W))
+    assert abs(lhs - rhs) <= 1e-11 * (abs(lhs) + np.linalg.norm(v) * np.linalg.norm(JW)), (lhs, rhs)

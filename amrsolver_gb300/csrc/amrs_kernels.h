@@ -53,6 +53,8 @@ cudaError_t launch_riemann(const BoxTable& tb, const FaceTable& ft, const long l
 // WENO5-reconstructed primitive states + the two-shock solver (riemann_weno = 1)
 cudaError_t launch_weno_riemann(const BoxTable& tb, const FaceTable& ft, long long nfaces[3], int nsm,
                                 cudaStream_t st);
+// JST sensor and spectral radius alone (the reverse pass recomputes them)
+cudaError_t launch_jst_sensor(const BoxTable& tb, const FaceTable& ft, long long nvalid, int nsm, cudaStream_t st);
 cudaError_t launch_jst(const BoxTable& tb, const FaceTable& ft, int s_in, long long ngcells, long long nvalid,
                        long long nfaces[3], int nsm, cudaStream_t st);
 cudaError_t launch_visc_face_add(const BoxTable& tb, const FaceTable& ft, long long nfaces[3], int nsm,
@@ -84,6 +86,10 @@ cudaError_t launch_rhs_vjp(int order, const BoxTable& tb, const AdjRecHost& ah, 
 size_t muscl_vjp_buffer_bytes(const int n[3]);
 cudaError_t launch_muscl_vjp(const BoxTable& tb, const FaceRec& fr, const DArr& vbar, const DArr& ubar, double* buf,
                              const int n[3], int nsm, cudaStream_t st);
+// JST part of the RHS VJP, added to ubar (adjoint_jst.cu)
+size_t jst_vjp_buffer_bytes(const int n[3]);
+cudaError_t launch_jst_vjp(const BoxTable& tb, const FaceRec& fr, const DArr& vbar, const DArr& ubar, double* buf,
+                           const int n[3], int nsm, cudaStream_t st);
 // WENO5-Riemann Euler part of the RHS VJP, added to ubar (adjoint_weno_riemann.cu)
 size_t weno_riemann_vjp_buffer_bytes(const int n[3]);
 cudaError_t launch_weno_riemann_vjp(const BoxTable& tb, const DArr& vbar, const DArr& ubar, double* buf,

@@ -1383,23 +1383,26 @@ struct AdjScratch {
   AdjRecHost ah;
   DArr vbar_tmp, ubar_tmp;
   double* wbuf = nullptr;  // WENO / MUSCL per-face and per-cell cotangent slots
+  double* jbuf = nullptr;  // JST per-face and per-cell cotangent slots
   int order = 0;           // KEEP order of the pair pass (0: none)
 };
 
 // Schemes with a reverse pass: KEEP, WENO5 LLF, MUSCL-Riemann, WENO5-Riemann
-// (each + viscous), viscous only.  (Internal flux codes: 0 MUSCL, 3
-// WENO5-Riemann.)
+// (each with or without JST and viscous fluxes), viscous only.  (Internal
+// flux codes: 0 MUSCL, 3 WENO5-Riemann.)
 bool vjp_scheme(const amrs_scheme& s) {
-  if (s.art_diss) return false;
   if (!s.rhs_euler) return s.rhs_visc != 0;
   return s.flux_euler >= 0 && s.flux_euler <= 3;
 }
+bool jst_scheme(const amrs_scheme& s) { return s.rhs_euler && s.art_diss == 1; }
 bool weno_scheme(const amrs_scheme& s) { return s.rhs_euler && s.flux_euler == 2; }
 bool muscl_scheme(const amrs_scheme& s) { return s.rhs_euler && s.flux_euler == 0; }
 bool weno_riemann_scheme(const amrs_scheme& s) { return s.rhs_euler && s.flux_euler == 3; }
 
 amrs_status adj_prepare(amrs_handle* h, const amrs_box& B, AdjScratch& S, cudaStream_t st) {
-  S.order = fused_path(h->sc) ? h->sc.order_keep : 0;
+  // the KEEP pair pass runs whether the forward used the fused kernel or
+  // (with JST) the face-array path: both compute the same fluxes
+  S.order = (h->sc.rhs_euler && h->sc.flux_euler == 1) ? h->sc.order_keep : 0;
   const int H = S.order / 2;
   const int nb[3] = {bn(B, 0), bn(B, 1), bn(B, 2)};
   auto cells = [&](int g) { return (size_t)grown_cells(B, g); };
@@ -1413,6 +1416,7 @@ amrs_status adj_prepare(amrs_handle* h, const amrs_box& B, AdjScratch& S, cudaSt
                             : weno_riemann_scheme(h->sc) ? weno_riemann_vjp_buffer_bytes(nb)
                                                          : 0;
   const size_t o_w = off; off = align_up(off + euler_bytes, 256);
+  const size_t o_j = off; off = align_up(off + (jst_scheme(h->sc) ? jst_vjp_buffer_bytes(nb) : 0), 256);
   if (off > h->adj_bytes) {
     if (h->adj) { CK(cudaStreamSynchronize(st)); cudaFree(h->adj); h->adj = nullptr; h->adj_bytes = 0; }
     CK(cudaMalloc(&h->adj, off));
@@ -1434,7 +1438,8 @@ amrs_status adj_prepare(amrs_handle* h, const amrs_box& B, AdjScratch& S, cudaSt
   S.ubar_tmp = mk(o_u, 3);
   for (int d = 0; d < 3; ++d) S.ah.n[d] = bn(B, d);
   S.ah.visc = h->sc.rhs_visc != 0;
-  S.wbuf = reinterpret_cast<double*>(P + o_w);  // WENO or MUSCL per-face / per-cell slots
+  S.wbuf = reinterpret_cast<double*>(P + o_w);
+  S.jbuf = reinterpret_cast<double*>(P + o_j);  // WENO or MUSCL per-face / per-cell slots
   if (H > 0) CK(cudaMemsetAsync(P + o_pair, 0, cells(3) * 12 * 8 * 3 * H, st));
   return AMRS_OK;
 }
@@ -1460,6 +1465,16 @@ cudaError_t rhs_vjp_launch(amrs_handle* h, List& L, const amrs_box& B, AdjScratc
   if (e == cudaSuccess && weno_riemann_scheme(h->sc)) {
     const int nb[3] = {bn(B, 0), bn(B, 1), bn(B, 2)};
     e = launch_weno_riemann_vjp(L.tb, S.ah.vbar, S.ah.ubar, S.wbuf, nb, h->nsm, st);
+  }
+  if (e == cudaSuccess && jst_scheme(h->sc)) {
+    // after the Euler part: the WENO5 pass reads lambda from the array the
+    // JST sensor pass overwrites
+    const int nb[3] = {bn(B, 0), bn(B, 1), bn(B, 2)};
+    const FaceRec& F = L.hface[0];
+    e = cudaMemsetAsync(F.sen.p, 0, (size_t)F.sen.ns * 3 * 8, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(F.lam.p, 0, (size_t)F.lam.ns * 3 * 8, st);
+    if (e == cudaSuccess) e = launch_jst_sensor(L.tb, L.ft, L.tot_valid, h->nsm, st);
+    if (e == cudaSuccess) e = launch_jst_vjp(L.tb, F, S.ah.vbar, S.ah.ubar, S.jbuf, nb, h->nsm, st);
   }
   return e;
 }

@@ -732,6 +732,11 @@ cudaError_t launch_weno_riemann(const BoxTable& tb, const FaceTable& ft, long lo
   return cudaGetLastError();
 }
 
+cudaError_t launch_jst_sensor(const BoxTable& tb, const FaceTable& ft, long long nvalid, int nsm, cudaStream_t st) {
+  jst_sensor_kernel<<<grid_for(nvalid, nsm), 256, 0, st>>>(tb, ft, nvalid);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_jst(const BoxTable& tb, const FaceTable& ft, int s_in, long long ngcells, long long nvalid,
                        long long nfaces[3], int nsm, cudaStream_t st) {
   (void)ngcells;

@@ -277,8 +277,8 @@ amrs_status amrs_boxlist_totals(amrs_boxlist* bl, int32_t slot, double scale, do
 
 /* Vector-Jacobian product of one RHS evaluation of one box (KEEP, WENO5
  * LLF, MUSCL-Riemann, WENO5-Riemann or no Euler flux, each with or without
- * viscous fluxes; JST returns AMRS_ERR_SCHEME; no counterpart in the
- * reference, whose lib/autodiff is absent):
+ * JST dissipation and viscous fluxes; no counterpart in the reference,
+ * whose lib/autodiff is absent):
  * given the ghost-filled state and a cotangent `vbar` on the valid cells,
  * writes ubar = (d dSdt/d state)^T vbar into `ubar` over the ghosted box
  * (ghost entries hold the sensitivities to ghost values).  `ubar` is

@@ -136,12 +136,3 @@ def test_weno_step_vjp_dot_product(orc):
     lhs = float(np.sum(g * JW))
     rhs = float(np.sum(grad.cpu().numpy() * P.valid(W)))
     assert abs(lhs - rhs) <= 1e-11 * (abs(lhs) + np.linalg.norm(g) * np.linalg.norm(JW)), (lhs, rhs)
-
-
-def test_jst_vjp_is_rejected():
-    cl = P.Closures.nondimensional(1e-2)
-    h = capi.Handle(P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1, art_diss=1), cl)
-    U, dx = turbulent_state(8, seed=1)
-    ubar = torch.empty_like(dev(U))
-    with pytest.raises(capi.AmrsError):
-        h.rhs_vjp_box(dev(U), dev(np.zeros((5, 8, 8, 8))), ubar, [1.0 / v for v in dx])

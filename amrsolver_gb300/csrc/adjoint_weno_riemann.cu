@@ -93,7 +93,8 @@ __global__ void __launch_bounds__(256) wr_vjp_face_kernel(BoxTable tb, DArr vbar
   }
 }
 
-// Cells lo-3 .. hi+2 along d, the valid range across.
+// Cells lo-3 .. hi+3 along d (the stencils of faces lo .. hi+1), the valid
+// range across.
 __global__ void __launch_bounds__(256) wr_vjp_gather_kernel(BoxTable tb, DArr ubar, RBuf rb, int d, int m0, int m1,
                                                             long long total) {
   const BoxRec& R = tb.box[0];
@@ -156,7 +157,7 @@ cudaError_t launch_weno_riemann_vjp(const BoxTable& tb, const DArr& vbar, const 
     rb.ny = n[1] + (d == 1);
     rb.nf = (long long)rb.nx * rb.ny * (n[2] + (d == 2));
     wr_vjp_face_kernel<<<grid_r(rb.nf, nsm), 256, 0, st>>>(tb, vbar, rb, d, rb.nf);
-    const int m0 = n[0] + (d == 0 ? 5 : 0), m1 = n[1] + (d == 1 ? 5 : 0), m2 = n[2] + (d == 2 ? 5 : 0);
+    const int m0 = n[0] + (d == 0 ? 6 : 0), m1 = n[1] + (d == 1 ? 6 : 0), m2 = n[2] + (d == 2 ? 6 : 0);
     const long long tot = (long long)m0 * m1 * m2;
     wr_vjp_gather_kernel<<<grid_r(tot, nsm), 256, 0, st>>>(tb, ubar, rb, d, m0, m1, tot);
   }

@@ -114,13 +114,19 @@ __global__ void __launch_bounds__(256) adj_pair_kernel(BoxTable tb, AdjRec ar, l
     const int jj = (int)(t % e1), kk = (int)(t / e1);
     const int i = R.lo[0] + ii - (d == 0) * l, j = R.lo[1] + jj - (d == 1) * l, k = R.lo[2] + kk - (d == 2) * l;
     const int di = d == 0, dj = d == 1, dk = d == 2;
-    // pair (a = (i,j,k), a + l e_d); faces a+1 .. a+l
-    double a[5];
+    // pair (a = (i,j,k), a + l e_d); faces a+1 .. a+l.  Next to a code-6 y
+    // wall the reduced y faces take only the l = 1 pair, with coefficient 1
+    // (Flux_2nd_Order_KEEP, src/rhs/CentralKEEP.h:232-287).
+    double a[5] = {0, 0, 0, 0, 0};
+    for (int m = 1; m <= l; ++m) {
+      double w = coef[l - 1];
+      if (d == 1 && R.walls) {
+        const int jf = j + m;
+        if (jf <= R.red_lo || (jf >= R.red_hi && jf <= R.hi[1])) w = (l == 1) ? 1.0 : 0.0;
+      }
+      if (w == 0.0) continue;
 #pragma unroll
-    for (int n = 0; n < 5; ++n) {
-      double s = 0.0;
-      for (int m = 1; m <= l; ++m) s += fbar(ar.vbar, R, d, i + m * di, j + m * dj, k + m * dk, n);
-      a[n] = coef[l - 1] * s;
+      for (int n = 0; n < 5; ++n) a[n] += w * fbar(ar.vbar, R, d, i + m * di, j + m * dj, k + m * dk, n);
     }
     double q1[NQ], q2[NQ], b1[NQA], b2[NQA];
     const long long o2 = R.q.off(i, j, k), o1 = R.q.off(i + l * di, j + l * dj, k + l * dk);
@@ -170,8 +176,14 @@ __global__ void __launch_bounds__(256) adj_visc_kernel(BoxTable tb, AdjRec ar, l
     const double u = q(o, QU), v = q(o, QV), w = q(o, QW), T = q(o, QT);
     const double dudx = (q(o + sx, QU) - q(o - sx, QU)) * hx, dvdx = (q(o + sx, QV) - q(o - sx, QV)) * hx;
     const double dwdx = (q(o + sx, QW) - q(o - sx, QW)) * hx, dTdx = (q(o + sx, QT) - q(o - sx, QT)) * hx;
-    const double dudy = (q(o + sy, QU) - q(o - sy, QU)) * hy, dvdy = (q(o + sy, QV) - q(o - sy, QV)) * hy;
-    const double dwdy = (q(o + sy, QW) - q(o - sy, QW)) * hy, dTdy = (q(o + sy, QT) - q(o - sy, QT)) * hy;
+    // y derivatives: central, or one-sided on the ghost row beyond a code-6
+    // wall (ViscousWallFluxes, src/rhs/CNS_hydro_K.h:177-251)
+    auto ddy = [&](int n) {
+      if (R.walls && j == R.wrow_lo) return (4.0 * q(o + sy, n) - q(o + 2 * sy, n) - 3.0 * q(o, n)) * hy;
+      if (R.walls && j == R.wrow_hi) return (-4.0 * q(o - sy, n) + 3.0 * q(o, n) + q(o - 2 * sy, n)) * hy;
+      return (q(o + sy, n) - q(o - sy, n)) * hy;
+    };
+    const double dudy = ddy(QU), dvdy = ddy(QV), dwdy = ddy(QW), dTdy = ddy(QT);
     const double dudz = (q(o + sz, QU) - q(o - sz, QU)) * hz, dvdz = (q(o + sz, QV) - q(o - sz, QV)) * hz;
     const double dwdz = (q(o + sz, QW) - q(o - sz, QW)) * hz, dTdz = (q(o + sz, QT) - q(o - sz, QT)) * hz;
     const double div = dudx + dvdy + dwdz;
@@ -291,15 +303,22 @@ __global__ void __launch_bounds__(256) adj_gather_kernel(BoxTable tb, AdjRec ar,
     for (int d = 0; d < 3; ++d) {
       const int di = d == 0, dj = d == 1, dk = d == 2;
       const double h = 0.5 * R.dxinv[d];
-      // gradient at e = c - e_d reads q(c) with +h; at e = c + e_d with -h
+      // the gradient at e = c + s e_d reads q(c) with weight wt: central
+      // differences give +h at s = -1 and -h at s = +1; the one-sided y
+      // derivative of a wall's ghost row e reads e, e+1, e+2 (lower wall)
+      // with -3h, 4h, -h, or e, e-1, e-2 (upper wall) with 3h, -4h, h
 #pragma unroll
-      for (int s = -1; s <= 1; s += 2) {
+      for (int s = -2; s <= 2; ++s) {
         const int a = i + s * di, b = j + s * dj, c = k + s * dk;
         if (!inside1(a, b, c)) continue;
+        double wt = 0.0;
+        if (d == 1 && R.walls && b == R.wrow_lo) wt = (s == 0) ? -3.0 * h : (s == -1 ? 4.0 * h : (s == -2 ? -h : 0.0));
+        else if (d == 1 && R.walls && b == R.wrow_hi) wt = (s == 0) ? 3.0 * h : (s == 1 ? -4.0 * h : (s == 2 ? h : 0.0));
+        else wt = (s == -1) ? h : (s == 1 ? -h : 0.0);
+        if (wt == 0.0) continue;
         const long long o = G.off(a, b, c);
-        const double sg = (s < 0) ? h : -h;
 #pragma unroll
-        for (int n = 0; n < 4; ++n) qb[QU + n] += sg * G.p[o + (4 + 4 * d + n) * G.ns];
+        for (int n = 0; n < 4; ++n) qb[QU + n] += wt * G.p[o + (4 + 4 * d + n) * G.ns];
       }
     }
     // cons2prim VJP (src/rhs/CNS_hydro_K.h:15-34)

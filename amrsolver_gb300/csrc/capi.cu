@@ -1487,7 +1487,7 @@ amrs_status amrs_rhs_vjp_box(amrs_handle* h, const amrs_box* bx, const double dx
                              amrs_array4 vbar, amrs_array4 ubar, double* param_bar, void* stream) {
   if (!h || !bx || !dxinv) return AMRS_ERR_NULL;
   if (!box_ok(*bx)) return AMRS_ERR_BOX;
-  if (!vjp_scheme(h->sc) || h->wall.lo || h->wall.hi) return AMRS_ERR_SCHEME;
+  if (!vjp_scheme(h->sc)) return AMRS_ERR_SCHEME;
   if (!covers(state, *bx, NGHOST, NCONS) || !covers(vbar, *bx, 0, NCONS) || !covers(ubar, *bx, NGHOST, NCONS))
     return AMRS_ERR_LAYOUT;
   std::lock_guard<std::mutex> lk(h->mu);

@@ -130,7 +130,10 @@ amrs_status amrs_set_closures(amrs_handle* h, const amrs_closures* closures);
  * ghost row use one-sided y derivatives (ViscousWallFluxes,
  * src/rhs/CNS_hydro_K.h:177-251).  Ghost cells beyond code-1/6 sides are the
  * caller's (the problem's bcnormal fills them); the library's fills leave
- * them untouched.  The VJP entry points reject a handle with walls. */
+ * them untouched.  amrs_rhs_vjp_box applies the same wall treatment in
+ * reverse; amrs_rk_stage_vjp_box rejects a handle with walls (the ghost
+ * values beyond a code-6 side come from the caller's bcnormal, whose
+ * derivative the library does not have). */
 amrs_status amrs_set_domain(amrs_handle* h, const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3]);
 const char* amrs_status_string(amrs_status s);
 /* Last CUDA error string recorded by the library (thread-local). */

@@ -1142,6 +1142,22 @@ int orc_compute_rhs_walls(const OrcScheme* s, const OrcClosures* c, const int* l
   return 0;
 }
 
+// The same on a box of a domain with code-6 y walls (walls4 as for
+// orc_compute_rhs_walls).
+int orc_compute_rhs_jvp_walls(const OrcScheme* s, const OrcClosures* c, const int* lo, const int* hi,
+                              const double* dxinv, const double* U, const double* W, double* R, double* JW,
+                              int nthreads, const int* walls4) {
+  if (!s || !c || !lo || !hi || !dxinv || !U || !W || !R || !JW || !walls4) return 1;
+  Box b = to_box(lo, hi);
+  const long long ng = ghosted(b) * NCONS, nv = b.cells() * NCONS;
+  std::vector<Dual> ud(ng), rd(nv);
+  for (long long t = 0; t < ng; ++t) ud[t] = Dual(U[t], W[t]);
+  Walls w{walls4[0], walls4[1], walls4[2], walls4[3]};
+  compute_rhs_box<Dual>(to_sc(s), to_cl(c), b, dxinv, ud.data(), rd.data(), nthreads, &w);
+  for (long long t = 0; t < nv; ++t) { R[t] = rd[t].v; JW[t] = rd[t].d; }
+  return 0;
+}
+
 // Jacobian-vector product: R = dS/dt(U), JW = d(dS/dt)/dU . W (dual numbers).
 int orc_compute_rhs_jvp(const OrcScheme* s, const OrcClosures* c, const int* lo, const int* hi,
                         const double* dxinv, const double* U, const double* W, double* R, double* JW,

@@ -87,6 +87,9 @@ class Oracle:
             L.orc_compute_rhs_jvp.argtypes = [ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ip, ip,
                                               dp, dp, dp, dp, dp, ctypes.c_int]
             L.orc_compute_rhs_jvp.restype = ctypes.c_int
+            L.orc_compute_rhs_jvp_walls.argtypes = [ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ip, ip,
+                                                    dp, dp, dp, dp, dp, ctypes.c_int, ip]
+            L.orc_compute_rhs_jvp_walls.restype = ctypes.c_int
             L.orc_compute_rhs_count.argtypes = [ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ip,
                                                 ip, dp, dp, ctypes.POINTER(ctypes.c_longlong)]
             L.orc_compute_rhs_count.restype = ctypes.c_int
@@ -113,7 +116,7 @@ class Oracle:
             raise RuntimeError("orc_compute_rhs failed: %d" % rc)
         return out
 
-    def rhs_jvp(self, scheme, closures, U, W, dxinv, lo=(0, 0, 0), nthreads=1):
+    def rhs_jvp(self, scheme, closures, U, W, dxinv, lo=(0, 0, 0), nthreads=1, walls=None):
         U = np.ascontiguousarray(U, dtype=np.float64)
         W = np.ascontiguousarray(W, dtype=np.float64)
         nz, ny, nx = (s - 2 * NG for s in U.shape[1:])
@@ -121,6 +124,13 @@ class Oracle:
         R = np.empty((NCONS, nz, ny, nx))
         JW = np.empty((NCONS, nz, ny, nx))
         sc, cl = c_scheme(scheme), c_closures(closures)
+        if walls is not None:
+            w4 = (ctypes.c_int * 4)(*[int(v) for v in walls])
+            rc = self.lib.orc_compute_rhs_jvp_walls(ctypes.byref(sc), ctypes.byref(cl), _i3(lo), _i3(hi),
+                                                    _d3(dxinv), _ptr(U), _ptr(W), _ptr(R), _ptr(JW), int(nthreads), w4)
+            if rc:
+                raise RuntimeError("orc_compute_rhs_jvp_walls failed: %d" % rc)
+            return R, JW
         rc = self.lib.orc_compute_rhs_jvp(ctypes.byref(sc), ctypes.byref(cl), _i3(lo), _i3(hi), _d3(dxinv),
                                           _ptr(U), _ptr(W), _ptr(R), _ptr(JW), int(nthreads))
         if rc:

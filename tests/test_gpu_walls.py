@@ -132,12 +132,37 @@ def test_level_between_walls_matches_one_box():
     np.testing.assert_array_equal(out, ref)
 
 
-def test_vjp_rejects_walls():
-    cl = P.Closures.nondimensional(1e-2)
-    h = capi.Handle(P.Scheme(), cl)
-    h.set_domain((0, 0, 0), (8, 8, 8), (-1, 6, -1), (-1, 6, -1))
-    U = P.random_state((8, 8, 8), seed=1)
+@pytest.mark.parametrize("walls", [(1, 1), (1, 0)])
+@pytest.mark.parametrize("skw", [dict(flux_euler=1, order_keep=4, rhs_visc=1), dict(flux_euler=1, order_keep=6, rhs_visc=0),
+                                 dict(flux_euler=2, rhs_visc=1)], ids=["keep4-visc", "keep6", "weno-visc"])
+def test_vjp_on_walls_every_entry(orc, skw, walls):
+    """The RHS VJP next to code-6 walls (reduced KEEP faces, one-sided
+    viscous y derivatives on the wall's ghost row), every entry of J^T v
+    against the oracle's dual-number JVP with the same walls."""
+    n = (4, 7, 3)
+    lo = (1, -2, 0)
+    U = P.random_state(n, seed=51 + walls[1], amp=0.15)
+    dxinv = (4.0, 7.0, 3.0)
+    cl = P.Closures.nondimensional(1.0 / 300.0)
+    sc = P.Scheme(**skw)
+    h = capi.Handle(sc, cl)
+    bl = (-1, 6 if walls[0] else 2, -1)
+    bh = (-1, 6 if walls[1] else 2, -1)
+    h.set_domain(lo, n, bl, bh)
+    v = np.random.default_rng(52).standard_normal((5, n[2], n[1], n[0]))
     Ud = torch.from_numpy(U).cuda()
-    with pytest.raises(capi.AmrsError):
-        h.rhs_vjp_box(Ud, torch.zeros((5, 8, 8, 8), dtype=torch.float64, device="cuda"), torch.empty_like(Ud),
-                      (8.0, 8.0, 8.0))
+    ub = torch.empty_like(Ud)
+    h.rhs_vjp_box(Ud, torch.from_numpy(v).cuda(), ub, dxinv, lo=lo)
+    h.sync_check()
+    ub = ub.cpu().numpy()
+    wl = (walls[0], walls[1], lo[1], lo[1] + n[1] - 1)
+    G = np.zeros_like(U)
+    W = np.zeros_like(U)
+    for idx in np.ndindex(U.shape):
+        W[idx] = 1.0
+        _, JW = orc.rhs_jvp(sc, cl, U, W, dxinv, lo=lo, walls=wl)
+        G[idx] = np.sum(v * JW)
+        W[idx] = 0.0
+    scale = np.abs(G).max()
+    bad = np.argwhere(np.abs(G - ub) > 1e-10 * scale)
+    assert len(bad) == 0, [(tuple(int(x) for x in b), G[tuple(b)], ub[tuple(b)]) for b in bad[:10]]

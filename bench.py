@@ -14,7 +14,9 @@ Also reported on the same JSON line:
   batched   512 uneven boxes, one SSPRK3 step: one persistent launch per
             kernel kind captured in a CUDA graph vs per-box launches;
   ensemble  64 periodic TGV members of 48^3 with per-member closures;
-  adjoint   TGV 64^3: VJP of one SSPRK3 step against the forward step;
+  adjoint   TGV 64^3: VJP of one SSPRK3 step against the forward step
+            (adjoint_muscl, adjoint_weno_riemann: the same for those
+            schemes; --vjp-only prints every scheme's line alone);
   large     256^3 random-phase turbulence, WENO5-LLF + viscous: 20 SSPRK3
             steps and the adjoint of the final step, with the roofline
             fraction of the whole step;
@@ -372,6 +374,27 @@ def bench_adjoint(torch, P, steps=3, scheme=None, label="KEEP4 + viscous"):
     lev.h.sync_check()
     return {"workload": "TGV 64^3 M=0.1 Re=400, %s, one SSPRK3 step" % label, "forward_ms": fwd,
             "forward_keeping_stages_ms": fwd_save, "adjoint_ms": adj, "adjoint_over_forward": adj / fwd}
+
+
+VJP_SCHEMES = (("KEEP4 + viscous", dict(flux_euler=1, order_keep=4, rhs_visc=1)),
+               ("WENO5-LLF + viscous", dict(flux_euler=2, rhs_visc=1)),
+               ("MUSCL-Riemann + viscous", dict(flux_euler=0, rhs_visc=1)),
+               ("WENO5-Riemann + viscous", dict(flux_euler=0, riemann_weno=1, rhs_visc=1)),
+               ("KEEP4 + JST + viscous", dict(flux_euler=1, order_keep=4, rhs_visc=1, art_diss=1)))
+
+
+def run_vjp_only():
+    """Adjoint-step vs forward-step time of every scheme with a reverse pass
+    (bench_adjoint's TGV 64^3 case), one JSON line on rank 0."""
+    import torch
+    from amrsolver_gb300 import capi
+    from amrsolver_gb300 import problems as P
+    capi.load(build_if_missing=True)
+    res = {"metric": "adjoint/forward time per SSPRK3 step", "schemes": {}}
+    for label, skw in VJP_SCHEMES:
+        res["schemes"][label] = bench_adjoint(torch, P, steps=2, scheme=skw, label=label)
+    print(json.dumps(res), flush=True)
+    return 0
 
 
 def bench_level(torch, capi, P, n=128, box=32, steps=10, warmup=3):
@@ -732,7 +755,12 @@ def main():
                     help="scheme of the TGV line (keep4 is the headline; weno* for profiling the WENO path)")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=128, help="TGV box edge (128 for the headline; smaller for profiling)")
+    ap.add_argument("--vjp-only", action="store_true",
+                    help="only the adjoint-step timings (TGV 64^3) of every scheme with a reverse pass, one JSON "
+                         "line; used to profile the reverse kernels")
     args = ap.parse_args()
+    if args.vjp_only:
+        return run_vjp_only()
     rank, world, local = dist_env()
     if world > 1:
         import torch

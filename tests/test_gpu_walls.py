@@ -166,3 +166,17 @@ def test_vjp_on_walls_every_entry(orc, skw, walls):
     scale = np.abs(G).max()
     bad = np.argwhere(np.abs(G - ub) > 1e-10 * scale)
     assert len(bad) == 0, [(tuple(int(x) for x in b), G[tuple(b)], ub[tuple(b)]) for b in bad[:10]]
+
+
+def test_stage_vjp_rejects_walls():
+    """The RK-stage VJP folds ghost cotangents back through the ghost fill;
+    beyond a code-6 side the ghosts come from the caller's bcnormal, so a
+    handle with walls is refused there (the RHS VJP above accepts it)."""
+    cl = P.Closures.nondimensional(1e-2)
+    h = capi.Handle(P.Scheme(), cl)
+    h.set_domain((0, 0, 0), (8, 8, 8), (-1, 6, -1), (-1, 6, -1))
+    U = torch.from_numpy(P.random_state((8, 8, 8), seed=1)).cuda()
+    z = torch.zeros((5, 8, 8, 8), dtype=torch.float64, device="cuda")
+    prog = capi.rk_program(3, 3, 1e-3)[0]
+    with pytest.raises(capi.AmrsError):
+        h.rk_stage_vjp_box(prog, (-1, 6, -1), (-1, 6, -1), U, z, z.clone(), z.clone(), (8.0, 8.0, 8.0))

@@ -376,6 +376,58 @@ def bench_adjoint(torch, P, steps=3, scheme=None, label="KEEP4 + viscous"):
             "forward_keeping_stages_ms": fwd_save, "adjoint_ms": adj, "adjoint_over_forward": adj / fwd}
 
 
+def bench_checkpointed(torch, P, n=64, nsteps=200, every=20, dt=2e-3):
+    """The adjoint configuration at full size: TGV 64^3, M = 0.1, Re = 400,
+    d KE(after 200 SSPRK3 steps)/d(V0, mu) with a checkpoint every 20 steps:
+    the forward run's time, the checkpointed adjoint run's time (forward with
+    checkpoints + recomputed segments + step VJPs) and the gradient against
+    central differences of two more forward runs each."""
+    from amrsolver_gb300 import adjoint, cns
+    sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1)
+    mu0 = 1.0 / 400.0
+    U, dx = P.tgv(n, mach=0.1, amp=1.0)
+    cl = P.Closures.nondimensional(mu0)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def run(amp, mu):
+        Ua, _ = P.tgv(n, mach=0.1, amp=amp)
+        lv = cns.CNSLevel(sc, P.Closures.nondimensional(mu), Ua, dx)
+        for _ in range(nsteps):
+            lv.advance(lv.time, dt)
+        return float(adjoint.kinetic_energy(lv.valid()))
+
+    run(1.0, mu0)
+    lev = cns.CNSLevel(sc, cl, U, dx)
+    e0, e1 = ev(), ev()
+    e0.record()
+    for _ in range(nsteps):
+        lev.advance(lev.time, dt)
+    e1.record()
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1)
+    lev = cns.CNSLevel(sc, cl, U, dx)
+    adj = adjoint.CheckpointedAdjoint(lev, every=every)
+    e0.record()
+    ubar0, pbar, _ = adj.run(torch.from_numpy(P.valid(U).copy()).cuda(), nsteps, dt, adjoint.kinetic_energy_grad)
+    e1.record()
+    torch.cuda.synchronize()
+    adj_ms = e0.elapsed_time(e1)
+    h = 1e-3
+    dU = (P.valid(P.tgv(n, mach=0.1, amp=1.0 + h)[0]) - P.valid(P.tgv(n, mach=0.1, amp=1.0 - h)[0])) / (2 * h)
+    g_v0 = float(np.sum(ubar0.cpu().numpy() * dU))
+    pb = pbar.cpu().numpy()
+    g_mu = float(pb[0] + cl.cp / 0.71 * pb[1])
+    eps = 1e-6
+    fd_v0 = (run(1.0 + eps, mu0) - run(1.0 - eps, mu0)) / (2 * eps)
+    fd_mu = (run(1.0, mu0 * (1 + eps)) - run(1.0, mu0 * (1 - eps))) / (2 * eps * mu0)
+    lev.h.sync_check()
+    return {"workload": "TGV %d^3 M=0.1 Re=400, KEEP4 + viscous, d KE(after %d SSPRK3 steps)/d(V0, mu), "
+                        "checkpoint every %d steps" % (n, nsteps, every),
+            "forward_run_ms": fwd_ms, "checkpointed_adjoint_run_ms": adj_ms, "adjoint_over_forward": adj_ms / fwd_ms,
+            "dKE_dV0": g_v0, "dKE_dV0_rel_err_vs_fd": abs(g_v0 - fd_v0) / abs(fd_v0),
+            "dKE_dmu": g_mu, "dKE_dmu_rel_err_vs_fd": abs(g_mu - fd_mu) / abs(fd_mu)}
+
+
 VJP_SCHEMES = (("KEEP4 + viscous", dict(flux_euler=1, order_keep=4, rhs_visc=1)),
                ("WENO5-LLF + viscous", dict(flux_euler=2, rhs_visc=1)),
                ("MUSCL-Riemann + viscous", dict(flux_euler=0, rhs_visc=1)),
@@ -718,6 +770,7 @@ def run_gpu(args, rank, world, local):
             result["adjoint"] = bench_adjoint(torch, P)
             result["adjoint_muscl"] = bench_adjoint(torch, P, scheme=dict(flux_euler=0, rhs_visc=1),
                                                     label="MUSCL-Riemann + viscous")
+            result["adjoint_checkpointed"] = bench_checkpointed(torch, P)
             result["adjoint_weno_riemann"] = bench_adjoint(
                 torch, P, scheme=dict(flux_euler=0, riemann_weno=1, rhs_visc=1), label="WENO5-Riemann + viscous")
             result["level"] = bench_level(torch, capi, P, n=n)

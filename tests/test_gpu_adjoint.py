@@ -196,3 +196,37 @@ def test_checkpointed_gradient_vs_fd():
     fd_mu = (run(1.0, mu0 * (1 + eps)) - run(1.0, mu0 * (1 - eps))) / (2 * eps * mu0)
     assert abs(g_v0 - fd_v0) <= 1e-6 * abs(fd_v0), (g_v0, fd_v0)
     assert abs(g_mu - fd_mu) <= 1e-6 * abs(fd_mu), (g_mu, fd_mu)
+
+
+def test_checkpointed_gradient_vs_fd_tgv64_200_steps():
+    """The adjoint configuration at full size: TGV 64^3, M = 0.1, Re = 400,
+    d KE(after 200 SSPRK3 steps) / d(V0, mu) with a checkpoint every 20
+    steps, against central differences of the whole forward run."""
+    n, nsteps, dt, every = 64, 200, 2e-3, 20
+    mach, re = 0.1, 400.0
+    sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1)
+
+    def run(amp, mu):
+        U, dx = P.tgv(n, mach=mach, amp=amp)
+        lev = cns.CNSLevel(sc, P.Closures.nondimensional(mu), U, dx)
+        for _ in range(nsteps):
+            lev.advance(lev.time, dt)
+        return float(adjoint.kinetic_energy(lev.valid()))
+
+    mu0 = 1.0 / re
+    U, dx = P.tgv(n, mach=mach, amp=1.0)
+    cl = P.Closures.nondimensional(mu0)
+    lev = cns.CNSLevel(sc, cl, U, dx)
+    adj = adjoint.CheckpointedAdjoint(lev, every=every)
+    ubar0, pbar, _ = adj.run(dev(P.valid(U).copy()), nsteps, dt, adjoint.kinetic_energy_grad)
+    e = 1e-3
+    dU = (P.valid(P.tgv(n, mach=mach, amp=1.0 + e)[0]) - P.valid(P.tgv(n, mach=mach, amp=1.0 - e)[0])) / (2 * e)
+    g_v0 = float(np.sum(ubar0.cpu().numpy() * dU))
+    pb = pbar.cpu().numpy()
+    g_mu = float(pb[0] + cl.cp / 0.71 * pb[1])
+    eps = 1e-6
+    fd_v0 = (run(1.0 + eps, mu0) - run(1.0 - eps, mu0)) / (2 * eps)
+    fd_mu = (run(1.0, mu0 * (1 + eps)) - run(1.0, mu0 * (1 - eps))) / (2 * eps * mu0)
+    lev.h.sync_check()
+    assert abs(g_v0 - fd_v0) <= 1e-6 * abs(fd_v0), (g_v0, fd_v0)
+    assert abs(g_mu - fd_mu) <= 1e-6 * abs(fd_mu), (g_mu, fd_mu)

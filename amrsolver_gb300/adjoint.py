@@ -107,7 +107,10 @@ def _step_vjp(level, stages, dt, wbar, param_bar=None):
 
 class CheckpointedAdjoint:
     """Reverse-mode sensitivity of a scalar of the final state after N steps,
-    storing every k-th state (k = `every`) and recomputing in between."""
+    storing every k-th state (k = `every`) and recomputing in between.  The
+    last segment's stage inputs are kept from the forward pass, so it is not
+    recomputed; with every >= N nothing is (all stage inputs are kept: three
+    ghosted states per step, e.g. 8 GB for 200 steps of a 64^3 box)."""
 
     def __init__(self, level, every=20):
         self.level = level
@@ -122,10 +125,14 @@ class CheckpointedAdjoint:
         ckpt = {}
         S = torch.zeros(lev.shape, dtype=torch.float64, device=lev.dev)
         S[:, g:-g, g:-g, g:-g] = U0v
+        last = ((nsteps - 1) // self.every) * self.every  # start of the last segment
+        kept = []
         for n in range(nsteps):
             if n % self.every == 0:
                 ckpt[n] = _valid(S).clone()
-            _, out = _forward_step(lev, S, dt)
+            stages, out = _forward_step(lev, S, dt)
+            if n >= last:
+                kept.append(stages)
             S = out
         final = _valid(S).clone()
         wbar = objective_grad(final)
@@ -133,14 +140,17 @@ class CheckpointedAdjoint:
         seg_starts = sorted(ckpt)
         for a in reversed(seg_starts):
             b = min(a + self.every, nsteps)
-            # recompute the segment, keeping each step's stage inputs
-            S = torch.zeros(lev.shape, dtype=torch.float64, device=lev.dev)
-            S[:, g:-g, g:-g, g:-g] = ckpt[a]
-            saved = []
-            for n in range(a, b):
-                stages, out = _forward_step(lev, S, dt)
-                saved.append(stages)
-                S = out
+            if a == last:
+                saved = kept
+            else:
+                # recompute the segment, keeping each step's stage inputs
+                S = torch.zeros(lev.shape, dtype=torch.float64, device=lev.dev)
+                S[:, g:-g, g:-g, g:-g] = ckpt[a]
+                saved = []
+                for n in range(a, b):
+                    stages, out = _forward_step(lev, S, dt)
+                    saved.append(stages)
+                    S = out
             for n in range(b - 1, a - 1, -1):
                 wbar, _ = _step_vjp(lev, saved[n - a], dt, wbar, param_bar=pbar)
         return wbar, pbar, final

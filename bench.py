@@ -19,7 +19,8 @@ Also reported on the same JSON line:
             schemes; --vjp-only prints every scheme's line alone);
   large     256^3 random-phase turbulence, WENO5-LLF + viscous: 20 SSPRK3
             steps and the adjoint of the final step, with the roofline
-            fraction of the whole step;
+            fraction of the whole step; KEEP4 + viscous and the WENO5 ->
+            Riemann extension + viscous timed on the same state;
   cpu_baseline  the CPU oracle on the host cores (bounded sample).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
@@ -544,7 +545,9 @@ def bench_large(torch, capi, P, peak, n=256, steps=20):
     viscous, SSPRK3 at a fixed dt (CFL 0.3 of the initial state): 20 steps,
     then the adjoint of the final step (cotangent: gradient of the mean
     kinetic energy).  Both WENO5 weight evaluations: the reference's
-    operation order (bit-identical) and the common-denominator form."""
+    operation order (bit-identical) and the common-denominator form.  On the
+    same state: KEEP4 + viscous (the headline scheme, whole-step FP64
+    fraction) and the WENO5 -> Riemann extension + viscous."""
     import gc
     from amrsolver_gb300 import adjoint, cns
     U, dx = P.random_turbulence(n, mach_t=0.6)
@@ -646,6 +649,32 @@ def bench_large(torch, capi, P, peak, n=256, steps=20):
     kach = kflops / (kms * 1e-3) / 1e12
     res["keep4_visc"] = {"ms_per_step": kms, "cell_updates_per_s": n ** 3 / (kms * 1e-3), "steps": ksteps,
                          "achieved_tflops_algorithmic": kach, "frac_of_measured_fp64_peak": kach / peak}
+    del lev
+    gc.collect()
+    torch.cuda.empty_cache()
+    # the WENO5 -> two-shock Riemann extension (riemann_weno = 1) + viscous
+    # on the same state; its operation count depends on the data (the
+    # solver's branches), so only time and rates are reported
+    lev = cns.CNSLevel(P.Scheme(flux_euler=0, riemann_weno=1, rhs_visc=1), cl, U, dx)
+    tot0 = lev.totals()
+    lev.advance(lev.time, res["dt"])
+    torch.cuda.synchronize()
+    e0, e1 = ev(), ev()
+    wsteps = 5
+    e0.record()
+    for _ in range(wsteps):
+        lev.advance(lev.time, res["dt"])
+    e1.record()
+    torch.cuda.synchronize()
+    lev.h.sync_check()
+    wms = e0.elapsed_time(e1) / wsteps
+    tot1 = lev.totals()
+    scale = (lev.valid().abs().reshape(5, -1).sum(dim=1) * (2 * math.pi) ** 3).cpu().numpy()
+    res["weno_riemann_visc"] = {
+        "ms_per_step": wms, "cell_updates_per_s": n ** 3 / (wms * 1e-3), "steps": wsteps,
+        "conserved_totals_max_rel_change": max(abs(float(a) - float(b)) / float(c)
+                                               for a, b, c in zip(tot0, tot1, scale)),
+        "finite": bool(torch.isfinite(lev.valid()).all())}
     del lev
     gc.collect()
     torch.cuda.empty_cache()

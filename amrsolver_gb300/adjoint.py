@@ -93,9 +93,19 @@ def _step_vjp(level, stages, dt, wbar, param_bar=None):
         p, inp = stages[s]
         if outbar[s] is None:
             outbar[s] = torch.zeros_like(wbar)
-        inbar = torch.zeros_like(wbar)
-        level.h.rk_stage_vjp_box(p, level.bc_lo, level.bc_hi, inp, outbar[s], s1bar, inbar, level.dxinv, level.lo,
-                                 param_bar=param_bar)
+        if level.has_ext_dir():
+            # ghosts beyond ext_dir sides came from bcnormal after the
+            # library's fill: reverse bcnormal first, then the library's fill
+            ug = torch.empty_like(inp)
+            level.h.rk_stage_vjp_box_ghosted(p, inp, outbar[s], s1bar, ug, level.dxinv, level.lo,
+                                             param_bar=param_bar)
+            ug = level.bcnormal_vjp(inp, ug)
+            capi.fill_halo_box_adjoint(ug, level.bc_lo, level.bc_hi, level.lo)
+            inbar = _valid(ug).contiguous()
+        else:
+            inbar = torch.zeros_like(wbar)
+            level.h.rk_stage_vjp_box(p, level.bc_lo, level.bc_hi, inp, outbar[s], s1bar, inbar, level.dxinv,
+                                     level.lo, param_bar=param_bar)
         if p.src_state == 0:
             s1bar += inbar
         else:

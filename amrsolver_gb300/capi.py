@@ -104,6 +104,8 @@ SIGNATURES = {
     "amrs_rk_stage_vjp_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double),
                                    ctypes.POINTER(StageProg), ctypes.POINTER(ctypes.c_int32),
                                    ctypes.POINTER(ctypes.c_int32), Array4, Array4, Array4, Array4, _P, _P]),
+    "amrs_rk_stage_vjp_box_ghosted": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(StageProg), Array4, Array4, Array4, Array4, _P, _P]),
     "amrs_sync_check": (_S, [_P, _P]),
     "amrs_probe_fp64_tflops": (_S, [_P, ctypes.POINTER(ctypes.c_double)]),
     "amrs_debug_wait_timeout": (_S, [_P, ctypes.c_int32, _P]),
@@ -277,6 +279,20 @@ class Handle:
                                             array4(s1bar, lo, g(s1bar)), array4(inbar, lo, g(inbar)), pb,
                                             _stream_ptr(stream)), "amrs_rk_stage_vjp_box")
 
+    def rk_stage_vjp_box_ghosted(self, prog, Uin, wbar, s1bar, ubar, dxinv, lo=(0, 0, 0), param_bar=None,
+                                 stream=None):
+        """Stage VJP without the ghost fold: ubar (ghosted) is overwritten with
+        the cotangent of the ghost-filled stage input, s1bar gets the S1
+        cotangent added (domains with ext_dir sides; the caller folds)."""
+        nz, ny, nx = (s - 2 * NGHOST for s in Uin.shape[1:])
+        bx = c_box(lo, (nx, ny, nz))
+        g = lambda t: (t.shape[1] - nz) // 2
+        pb = ctypes.c_void_p(param_bar.data_ptr()) if param_bar is not None else None
+        check(self._L.amrs_rk_stage_vjp_box_ghosted(self.h, ctypes.byref(bx), d3(dxinv), ctypes.byref(prog),
+                                                    array4(Uin, lo, NGHOST), array4(wbar, lo, g(wbar)),
+                                                    array4(s1bar, lo, g(s1bar)), array4(ubar, lo, NGHOST), pb,
+                                                    _stream_ptr(stream)), "amrs_rk_stage_vjp_box_ghosted")
+
     def profile_stage_box(self, prog, Uin, U1, Uout, dxinv, lo=(0, 0, 0), reps=5, stream=None):
         """Per-kernel ms of one stage: (prims [+ WENO point fluxes], viscous
         cells, Euler face kernel [fused: + divergence + program; MUSCL:
@@ -308,6 +324,17 @@ def fill_halo_box(U, bc_lo, bc_hi, lo=(0, 0, 0), stream=None):
     bx = c_box(lo, (nx, ny, nz))
     check(L.amrs_fill_halo_box(ctypes.byref(bx), i3(bc_lo), i3(bc_hi), array4(U, lo, NGHOST), _stream_ptr(stream)),
           "amrs_fill_halo_box")
+
+
+def fill_halo_box_adjoint(ubar, bc_lo, bc_hi, lo=(0, 0, 0), stream=None):
+    """Adjoint of fill_halo_box, in place on the ghosted cotangent `ubar`:
+    valid cells receive the cotangents of the ghosts filled from them
+    (ghosts beyond ext_dir sides, codes 1 and 6, are left in place)."""
+    L = load()
+    nz, ny, nx = (s - 2 * NGHOST for s in ubar.shape[1:])
+    bx = c_box(lo, (nx, ny, nz))
+    check(L.amrs_fill_halo_box_adjoint(ctypes.byref(bx), i3(bc_lo), i3(bc_hi), array4(ubar, lo, NGHOST),
+                                       _stream_ptr(stream)), "amrs_fill_halo_box_adjoint")
 
 
 def average_down(fine, crse, crse_lo, ratio, fine_g=0, crse_g=0, scomp=0, ncomp=None, stream=None):

@@ -21,8 +21,15 @@ class CNSLevel:
     """One single-box level: state S1 (U^n) plus two work buffers, all ghosted."""
 
     def __init__(self, scheme, closures, U0, dx, bc_lo=(-1, -1, -1), bc_hi=(-1, -1, -1), lo=(0, 0, 0),
-                 order_rk=3, stages_rk=3, device=0):
+                 order_rk=3, stages_rk=3, device=0, bcnormal=None):
+        """`bcnormal(t)`, if given, fills the ghost cells beyond the ext_dir
+        sides (codes 1, 6) of the ghosted state tensor `t` in place after the
+        library's fill, as the problem's bcnormal does in cns_bcfill
+        (src/set/bcs.cpp:30-100); written with torch operations, it is
+        differentiated by torch autograd in the adjoint.  Without it those
+        ghost cells keep the values of U0."""
         self.scheme, self.closures = scheme, closures
+        self.bcnormal = bcnormal
         self.h = capi.Handle(scheme, closures, device)
         self.dev = torch.device("cuda", device)
         self.dx = tuple(float(v) for v in dx)
@@ -57,8 +64,28 @@ class CNSLevel:
 
     # ------------------------------------------------------------ calls --
     def fill_patch(self, t, stream=None):
-        """Ghost fill of `t` in place (single-level FillPatch)."""
+        """Ghost fill of `t` in place (single-level FillPatch): periodic
+        images and physical BCs, then the ext_dir ghosts by `bcnormal`."""
         capi.fill_halo_box(t, self.bc_lo, self.bc_hi, self.lo, stream)
+        if self.bcnormal is not None:
+            self.bcnormal(t)
+
+    def has_ext_dir(self):
+        return any(b in (1, 6) for b in self.bc_lo + self.bc_hi)
+
+    def bcnormal_vjp(self, t, gbar):
+        """Reverse of `bcnormal` on the ghost-filled `t`: the cotangents of the
+        ghost cells it wrote (in the ghosted `gbar`) go to the cells it read.
+        Returns the folded ghosted cotangent.  Without a bcnormal the ext_dir
+        ghosts are constants and their cotangents are simply not used."""
+        if self.bcnormal is None:
+            return gbar
+        with torch.enable_grad():
+            x = t.detach().clone().requires_grad_(True)
+            y = x.clone()
+            self.bcnormal(y)
+            (gx,) = torch.autograd.grad(y, x, grad_outputs=gbar)
+        return gx
 
     def compute_rhs(self, S, dSdt, stream=None):
         """CNS::compute_rhs for the box: S ghost-filled, dSdt valid-only."""

@@ -1518,8 +1518,9 @@ amrs_status amrs_fill_halo_box_adjoint(const amrs_box* domain, const int32_t bc_
     if ((bc_lo[d] == -1) != (bc_hi[d] == -1)) return AMRS_ERR_BC;
     for (int s = 0; s < 2; ++s) {
       const int p = s ? bc_hi[d] : bc_lo[d];
-      if (p == 1 || p == 6 || p < -1 || p > 6) return AMRS_ERR_BC;
+      if (p < -1 || p > 6) return AMRS_ERR_BC;  // 1, 6: ext_dir, left in place
     }
+    if (bn(*domain, d) < NGHOST && bc_lo[d] != -1 && bc_lo[d] != 2) return AMRS_ERR_BOX;
     hb.lo[d] = domain->lo[d]; hb.hi[d] = domain->hi[d]; hb.bc_lo[d] = bc_lo[d]; hb.bc_hi[d] = bc_hi[d];
   }
   int nsm = 0;
@@ -1537,6 +1538,10 @@ amrs_status amrs_rk_stage_vjp_box(amrs_handle* h, const amrs_box* bx, const doub
   if (!h || !bx || !dxinv || !prog || !bc_lo || !bc_hi) return AMRS_ERR_NULL;
   if (!box_ok(*bx)) return AMRS_ERR_BOX;
   if (!vjp_scheme(h->sc) || h->wall.lo || h->wall.hi) return AMRS_ERR_SCHEME;
+  // ghosts beyond ext_dir sides come from the caller's bcnormal: their
+  // cotangents cannot be folded here (amrs_rk_stage_vjp_box_ghosted)
+  for (int d = 0; d < 3; ++d)
+    if (bc_lo[d] == 1 || bc_lo[d] == 6 || bc_hi[d] == 1 || bc_hi[d] == 6) return AMRS_ERR_BC;
   if (!covers(stage_in, *bx, NGHOST, NCONS) || !covers(wbar, *bx, 0, NCONS) || !covers(s1bar, *bx, 0, NCONS) ||
       !covers(inbar, *bx, 0, NCONS))
     return AMRS_ERR_LAYOUT;
@@ -1574,6 +1579,46 @@ amrs_status amrs_rk_stage_vjp_box(amrs_handle* h, const amrs_box* bx, const doub
   ident.nops = 0;
   DArr dummy = S.vbar_tmp;
   CK(launch_adj_prog(R, to_dprog(&ident), S.ubar_tmp, dummy, to_darr(inbar), dummy, 1, h->nsm, st));
+  return AMRS_OK;
+}
+
+amrs_status amrs_rk_stage_vjp_box_ghosted(amrs_handle* h, const amrs_box* bx, const double dxinv[3],
+                                          const amrs_stage_prog* prog, amrs_array4 stage_in, amrs_array4 wbar,
+                                          amrs_array4 s1bar, amrs_array4 ubar, double* param_bar, void* stream) {
+  if (!h || !bx || !dxinv || !prog) return AMRS_ERR_NULL;
+  if (!box_ok(*bx)) return AMRS_ERR_BOX;
+  if (!vjp_scheme(h->sc)) return AMRS_ERR_SCHEME;
+  if (!covers(stage_in, *bx, NGHOST, NCONS) || !covers(wbar, *bx, 0, NCONS) || !covers(s1bar, *bx, 0, NCONS) ||
+      !covers(ubar, *bx, NGHOST, NCONS))
+    return AMRS_ERR_LAYOUT;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> lk(h->mu);
+  CK(cudaSetDevice(h->device));
+  amrs_array4 slots[3] = {stage_in, stage_in, stage_in};
+  if (amrs_status s = one_box(h, bx, dxinv, slots, 3, st)) return s;
+  AdjScratch S;
+  if (amrs_status s = adj_prepare(h, *bx, S, st)) { ring_release(h, st); return s; }
+  const BoxRec R = h->one->hbox[0];
+  cudaError_t e = cudaMemsetAsync(S.ubar_tmp.p, 0, (size_t)S.ubar_tmp.ns * NCONS * sizeof(double), st);
+  // 1. reverse of the BLAS-1 program: S1 cotangent added to s1bar, the stage
+  //    input's direct cotangent parked in ubar_tmp, dSdt's in vbar_tmp
+  if (e == cudaSuccess)
+    e = launch_adj_prog(R, to_dprog(prog), to_darr(wbar), to_darr(s1bar), S.ubar_tmp, S.vbar_tmp, 1, h->nsm, st);
+  // 2. RHS VJP of the ghost-filled stage input, written into the caller's ubar
+  if (e == cudaSuccess) {
+    S.ah.vbar = S.vbar_tmp;
+    S.ah.ubar = to_darr(ubar);
+    e = rhs_vjp_launch(h, *h->one, *bx, S, param_bar, st);
+  }
+  // 3. ubar(valid) += the parked direct cotangent (the empty program routes
+  //    its input into the stage-input slot; vbar_tmp takes the zeros)
+  if (e == cudaSuccess) {
+    amrs_stage_prog ident{};
+    ident.nops = 0;
+    e = launch_adj_prog(R, to_dprog(&ident), S.ubar_tmp, S.vbar_tmp, to_darr(ubar), S.vbar_tmp, 1, h->nsm, st);
+  }
+  ring_release(h, st);
+  if (e != cudaSuccess) return cuda_fail(e, "amrs_rk_stage_vjp_box_ghosted");
   return AMRS_OK;
 }
 

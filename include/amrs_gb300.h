@@ -133,7 +133,8 @@ amrs_status amrs_set_closures(amrs_handle* h, const amrs_closures* closures);
  * them untouched.  amrs_rhs_vjp_box applies the same wall treatment in
  * reverse; amrs_rk_stage_vjp_box rejects a handle with walls (the ghost
  * values beyond a code-6 side come from the caller's bcnormal, whose
- * derivative the library does not have). */
+ * derivative the library does not have): such domains use
+ * amrs_rk_stage_vjp_box_ghosted. */
 amrs_status amrs_set_domain(amrs_handle* h, const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3]);
 const char* amrs_status_string(amrs_status s);
 /* Last CUDA error string recorded by the library (thread-local). */
@@ -185,7 +186,8 @@ amrs_status amrs_rk_stage_box(amrs_handle* h, const amrs_box* bx, const double d
 /* Ghost fill of a box that is the whole single-box domain: periodic images
  * and the physical BC types of src/set/CNS_setup.cpp:18-31 for cns.lo_bc /
  * cns.hi_bc codes (-1 periodic, 2 outflow/foextrap, 3/4 symmetry and slip
- * wall, 5 no-slip wall).  Codes 1 and 6 (problem bcnormal) are rejected. */
+ * wall, 5 no-slip wall).  Ghost cells beyond codes 1 and 6 (ext_dir: the
+ * problem's bcnormal fills them) are left as the caller stored them. */
 amrs_status amrs_fill_halo_box(const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3],
                                amrs_array4 state, void* stream);
 
@@ -292,7 +294,10 @@ amrs_status amrs_rhs_vjp_box(amrs_handle* h, const amrs_box* bx, const double dx
                              amrs_array4 vbar, amrs_array4 ubar, double* param_bar, void* stream);
 
 /* Adjoint of amrs_fill_halo_box: every valid cell of `ubar` (ghosted, in
- * place) receives the cotangents of the ghost cells filled from it. */
+ * place) receives the cotangents of the ghost cells filled from it.  Ghost
+ * cells beyond ext_dir sides (codes 1, 6) are not filled by the library, so
+ * their cotangents are left where they are: a caller whose bcnormal filled
+ * them folds them back through its own derivative first. */
 amrs_status amrs_fill_halo_box_adjoint(const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3],
                                        amrs_array4 ubar, void* stream);
 
@@ -306,6 +311,17 @@ amrs_status amrs_rk_stage_vjp_box(amrs_handle* h, const amrs_box* bx, const doub
                                   const amrs_stage_prog* prog, const int32_t bc_lo[3], const int32_t bc_hi[3],
                                   amrs_array4 stage_in, amrs_array4 wbar, amrs_array4 s1bar, amrs_array4 inbar,
                                   double* param_bar, void* stream);
+/* The same stage VJP without the ghost fold, for domains with ext_dir sides
+ * (codes 1, 6; code-6 y walls included): OVERWRITES the ghosted `ubar`
+ * (grow(box,3)) with the cotangent of the ghost-filled stage input and ADDS
+ * the cotangent of S1 to `s1bar`.  The caller then folds the ghost
+ * cotangents beyond its ext_dir sides through its bcnormal's derivative,
+ * calls amrs_fill_halo_box_adjoint for the library-filled ghosts, and takes
+ * the valid cells as the stage input's cotangent (AMReX's order reversed:
+ * the forward fills periodic/foextrap/reflect ghosts first, then bcnormal). */
+amrs_status amrs_rk_stage_vjp_box_ghosted(amrs_handle* h, const amrs_box* bx, const double dxinv[3],
+                                          const amrs_stage_prog* prog, amrs_array4 stage_in, amrs_array4 wbar,
+                                          amrs_array4 s1bar, amrs_array4 ubar, double* param_bar, void* stream);
 
 /* ---- diagnostics ---------------------------------------------------- */
 

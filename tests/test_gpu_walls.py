@@ -171,7 +171,8 @@ def test_vjp_on_walls_every_entry(orc, skw, walls):
 def test_stage_vjp_rejects_walls():
     """The RK-stage VJP folds ghost cotangents back through the ghost fill;
     beyond a code-6 side the ghosts come from the caller's bcnormal, so a
-    handle with walls is refused there (the RHS VJP above accepts it)."""
+    handle with walls is refused there (the RHS VJP above accepts it, and
+    the ghosted stage VJP of test_gpu_adjoint_walls.py covers RK stages)."""
     cl = P.Closures.nondimensional(1e-2)
     h = capi.Handle(P.Scheme(), cl)
     h.set_domain((0, 0, 0), (8, 8, 8), (-1, 6, -1), (-1, 6, -1))

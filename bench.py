@@ -21,7 +21,8 @@ Also reported on the same JSON line:
             steps and the adjoint of the final step, with the roofline
             fraction of the whole step; KEEP4 + viscous and the WENO5 ->
             Riemann extension + viscous timed on the same state;
-  cpu_baseline  the CPU oracle on the host cores (bounded sample).
+  cpu_baseline  the CPU oracle on all host cores and on one thread (bounded
+                samples).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -230,7 +231,9 @@ def run_reference(args, rank, world):
 
 # --------------------------------------------------------------- GPU arm --
 def cpu_baseline_sample():
-    """Bounded CPU sample: TGV 64^3 SSPRK3 steps with the oracle, all cores."""
+    """Bounded CPU samples: TGV 64^3 SSPRK3 steps with the oracle on all
+    cores (OpenMP over k-planes), and on one thread (the reference's CPU
+    path has no OpenMP in compute_rhs)."""
     from oracle import pyoracle
     from amrsolver_gb300 import problems as P
     orc = pyoracle.oracle()
@@ -240,17 +243,24 @@ def cpu_baseline_sample():
     cl = P.Closures.nondimensional(1.0 / 1600.0)
     sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1)
     dxinv = [1.0 / h for h in dx]
-    S = orc.advance(sc, cl, U, dxinv, (-1, -1, -1), (-1, -1, -1), 1e-3, nthreads=cores)
-    steps = 0
-    t0 = time.perf_counter()
-    while True:
-        S = orc.advance(sc, cl, S, dxinv, (-1, -1, -1), (-1, -1, -1), 1e-3, nthreads=cores)
-        steps += 1
-        if time.perf_counter() - t0 > 8.0 or steps >= 40:
-            break
-    el = time.perf_counter() - t0
+
+    def sample(threads, seconds, max_steps):
+        S = orc.advance(sc, cl, U, dxinv, (-1, -1, -1), (-1, -1, -1), 1e-3, nthreads=threads)
+        steps = 0
+        t0 = time.perf_counter()
+        while True:
+            S = orc.advance(sc, cl, S, dxinv, (-1, -1, -1), (-1, -1, -1), 1e-3, nthreads=threads)
+            steps += 1
+            if time.perf_counter() - t0 > seconds or steps >= max_steps:
+                break
+        return steps, time.perf_counter() - t0
+
+    steps, el = sample(cores, 8.0, 40)
+    steps1, el1 = sample(1, 6.0, 20)
     return {"value": n ** 3 * steps / el, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "TGV 64^3 KEEP4+viscous, %d SSPRK3 steps, %d OpenMP threads" % (steps, cores)}
+            "sample": "TGV 64^3 KEEP4+viscous, %d SSPRK3 steps, %d OpenMP threads" % (steps, cores),
+            "single_thread": {"value": n ** 3 * steps1 / el1, "unit": UNIT, "cores": 1,
+                              "sample": "TGV 64^3 KEEP4+viscous, %d SSPRK3 steps, one thread" % steps1}}
 
 
 def bench_batched(torch, capi, P, nboxes=512, steps=3, warmup=2):

@@ -1538,47 +1538,60 @@ amrs_status amrs_rk_stage_vjp_box(amrs_handle* h, const amrs_box* bx, const doub
   if (!h || !bx || !dxinv || !prog || !bc_lo || !bc_hi) return AMRS_ERR_NULL;
   if (!box_ok(*bx)) return AMRS_ERR_BOX;
   if (!vjp_scheme(h->sc) || h->wall.lo || h->wall.hi) return AMRS_ERR_SCHEME;
-  // ghosts beyond ext_dir sides come from the caller's bcnormal: their
-  // cotangents cannot be folded here (amrs_rk_stage_vjp_box_ghosted)
-  for (int d = 0; d < 3; ++d)
-    if (bc_lo[d] == 1 || bc_lo[d] == 6 || bc_hi[d] == 1 || bc_hi[d] == 6) return AMRS_ERR_BC;
+  // the fold's BC checks up front, so that nothing is queued for a call
+  // that fails; ghosts beyond ext_dir sides come from the caller's
+  // bcnormal: their cotangents cannot be folded here
+  // (amrs_rk_stage_vjp_box_ghosted)
+  for (int d = 0; d < 3; ++d) {
+    if ((bc_lo[d] == -1) != (bc_hi[d] == -1)) return AMRS_ERR_BC;
+    for (int sd = 0; sd < 2; ++sd) {
+      const int p = sd ? bc_hi[d] : bc_lo[d];
+      if (p < -1 || p > 6 || p == 1 || p == 6) return AMRS_ERR_BC;
+    }
+    if (bn(*bx, d) < NGHOST && bc_lo[d] != -1 && bc_lo[d] != 2) return AMRS_ERR_BOX;
+  }
   if (!covers(stage_in, *bx, NGHOST, NCONS) || !covers(wbar, *bx, 0, NCONS) || !covers(s1bar, *bx, 0, NCONS) ||
       !covers(inbar, *bx, 0, NCONS))
     return AMRS_ERR_LAYOUT;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // the handle's scratch (ubar_tmp) is used until the last launch: hold the
+  // handle for the whole call
+  std::lock_guard<std::mutex> lk(h->mu);
+  CK(cudaSetDevice(h->device));
+  amrs_array4 slots[3] = {stage_in, stage_in, stage_in};
+  if (amrs_status s = one_box(h, bx, dxinv, slots, 3, st)) return s;
   AdjScratch S;
-  BoxRec R{};
-  {
-    std::lock_guard<std::mutex> lk(h->mu);
-    CK(cudaSetDevice(h->device));
-    amrs_array4 slots[3] = {stage_in, stage_in, stage_in};
-    if (amrs_status s = one_box(h, bx, dxinv, slots, 3, st)) return s;
-    if (amrs_status s = adj_prepare(h, *bx, S, st)) { ring_release(h, st); return s; }
-    R = h->one->hbox[0];
-    // 1. reverse of the BLAS-1 program: cotangents of S1, of the stage input
-    //    (register S2) and of dSdt
-    CK(launch_adj_prog(R, to_dprog(prog), to_darr(wbar), to_darr(s1bar), to_darr(inbar), S.vbar_tmp, 1, h->nsm, st));
-    // 2. RHS VJP of the ghost-filled stage input
+  if (amrs_status s = adj_prepare(h, *bx, S, st)) { ring_release(h, st); return s; }
+  const BoxRec R = h->one->hbox[0];
+  // 1. reverse of the BLAS-1 program: cotangents of S1, of the stage input
+  //    (register S2) and of dSdt
+  cudaError_t e = launch_adj_prog(R, to_dprog(prog), to_darr(wbar), to_darr(s1bar), to_darr(inbar), S.vbar_tmp, 1,
+                                  h->nsm, st);
+  // 2. RHS VJP of the ghost-filled stage input
+  if (e == cudaSuccess) {
     S.ah.vbar = S.vbar_tmp;
     S.ah.ubar = S.ubar_tmp;
-    List& L = *h->one;
-    cudaError_t e = rhs_vjp_launch(h, L, *bx, S, param_bar, st);
-    ring_release(h, st);
-    if (e != cudaSuccess) return cuda_fail(e, "amrs_rk_stage_vjp_box");
+    e = rhs_vjp_launch(h, *h->one, *bx, S, param_bar, st);
   }
-  // 3. ghost fold (adjoint of FillPatch), then add into the stage input's cotangent
-  amrs_array4 ub{};
-  ub.p = S.ubar_tmp.p; ub.jstride = S.ubar_tmp.js; ub.kstride = S.ubar_tmp.ks; ub.nstride = S.ubar_tmp.ns;
-  ub.begin[0] = S.ubar_tmp.b0; ub.begin[1] = S.ubar_tmp.b1; ub.begin[2] = S.ubar_tmp.b2;
-  for (int d = 0; d < 3; ++d) ub.end[d] = bx->hi[d] + NGHOST + 1;
-  ub.ncomp = NCONS;
-  if (amrs_status s = amrs_fill_halo_box_adjoint(bx, bc_lo, bc_hi, ub, stream)) return s;
-  // inbar += valid(ubar): the reverse kernel with an empty program routes its
-  // input cotangent into the stage-input cotangent (vbar_tmp is free here)
-  amrs_stage_prog ident{};
-  ident.nops = 0;
-  DArr dummy = S.vbar_tmp;
-  CK(launch_adj_prog(R, to_dprog(&ident), S.ubar_tmp, dummy, to_darr(inbar), dummy, 1, h->nsm, st));
+  // 3. ghost fold (adjoint of FillPatch), then inbar += valid(ubar): the
+  //    reverse kernel with an empty program routes its input cotangent into
+  //    the stage-input cotangent (vbar_tmp is free here)
+  if (e == cudaSuccess) {
+    HaloBox hb;
+    hb.u = S.ubar_tmp;
+    hb.ncomp = NCONS;
+    for (int d = 0; d < 3; ++d) {
+      hb.lo[d] = bx->lo[d]; hb.hi[d] = bx->hi[d]; hb.bc_lo[d] = bc_lo[d]; hb.bc_hi[d] = bc_hi[d];
+    }
+    e = launch_adj_halo(hb, h->nsm, st);
+  }
+  if (e == cudaSuccess) {
+    amrs_stage_prog ident{};
+    ident.nops = 0;
+    e = launch_adj_prog(R, to_dprog(&ident), S.ubar_tmp, S.vbar_tmp, to_darr(inbar), S.vbar_tmp, 1, h->nsm, st);
+  }
+  ring_release(h, st);
+  if (e != cudaSuccess) return cuda_fail(e, "amrs_rk_stage_vjp_box");
   return AMRS_OK;
 }
 

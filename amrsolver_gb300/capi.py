@@ -106,6 +106,7 @@ SIGNATURES = {
                                    ctypes.POINTER(ctypes.c_int32), Array4, Array4, Array4, Array4, _P, _P]),
     "amrs_rk_stage_vjp_box_ghosted": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(StageProg), Array4, Array4, Array4, Array4, _P, _P]),
+    "amrs_set_source": (_S, [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]),
     "amrs_sync_check": (_S, [_P, _P]),
     "amrs_probe_fp64_tflops": (_S, [_P, ctypes.POINTER(ctypes.c_double)]),
     "amrs_debug_wait_timeout": (_S, [_P, ctypes.c_int32, _P]),
@@ -207,6 +208,12 @@ class Handle:
         sc, cl = c_scheme(scheme), c_closures(closures)
         check(L.amrs_create(ctypes.byref(h), ctypes.byref(sc), ctypes.byref(cl), int(device)), "amrs_create")
         self.h = h
+        if int(getattr(scheme, "rhs_source", 0)):
+            self.set_source(getattr(scheme, "body_force", (0.0, 0.0, 0.0)))
+
+    def set_source(self, force, on=True):
+        """amrs_set_source: cns.rhs_source with a body force per unit mass."""
+        check(self._L.amrs_set_source(self.h, 1 if on else 0, d3(force)), "amrs_set_source")
 
     def close(self):
         if self.h:

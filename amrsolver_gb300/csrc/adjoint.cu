@@ -431,6 +431,30 @@ __global__ void __launch_bounds__(256) adj_halo_kernel(HaloBox hb, long long tot
   }
 }
 
+// Reverse of the body-force source (add_source) on the valid cells:
+// ubar(URHO) += vbar(UMX+d) f_d and ubar(UMX+d) += vbar(UET) f_d.
+__global__ void __launch_bounds__(256) adj_source_kernel(BoxRec R, double f0, double f1, double f2, DArr vbar,
+                                                         DArr ubar, long long total) {
+  const int nx = R.hi[0] - R.lo[0] + 1, ny = R.hi[1] - R.lo[1] + 1;
+  const double f[3] = {f0, f1, f2};
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    const int l = (int)g;
+    const int i = l % nx + R.lo[0];
+    const int t = l / nx;
+    const int j = t % ny + R.lo[1];
+    const int k = t / ny + R.lo[2];
+    const double ve = vbar(i, j, k, UET);
+    double rb = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      if (f[d] == 0.0) continue;
+      rb += vbar(i, j, k, UMX + d) * f[d];
+      ubar(i, j, k, UMX + d) += ve * f[d];
+    }
+    ubar(i, j, k, URHO) += rb;
+  }
+}
+
 // ------------------------------------------------------------ launchers --
 static int grid256(long long n, int nsm) {
   long long b = (n + 255) / 256;
@@ -470,6 +494,13 @@ cudaError_t launch_adj_prog(const BoxRec& R, const DProg& prog, const DArr& wbar
                             const DArr& vbar, int accumulate, int nsm, cudaStream_t st) {
   const long long n = (long long)(R.hi[0] - R.lo[0] + 1) * (R.hi[1] - R.lo[1] + 1) * (R.hi[2] - R.lo[2] + 1);
   adj_prog_kernel<<<grid256(n, nsm), 256, 0, st>>>(R, prog, wbar, s1bar, inbar, vbar, n, accumulate);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_source_vjp(const BoxRec& R, const double force[3], const DArr& vbar, const DArr& ubar, int nsm,
+                              cudaStream_t st) {
+  const long long n = (long long)(R.hi[0] - R.lo[0] + 1) * (R.hi[1] - R.lo[1] + 1) * (R.hi[2] - R.lo[2] + 1);
+  adj_source_kernel<<<grid256(n, nsm), 256, 0, st>>>(R, force[0], force[1], force[2], vbar, ubar, n);
   return cudaGetLastError();
 }
 

@@ -41,7 +41,27 @@ struct DClosures {
   int visc_law, cond_law;
   double visc_ref, Tvisc_ref, cond_ref, Tcond_ref;
   double Cshock, Cdamp;
+  int source;       // cns.rhs_source with a body force
+  double force[3];  // body force per unit mass
 };
+
+// compute_rhs's source step (src/tim/CNS_advance.cpp:396-407) with the
+// channel problem's user_source (exm/Channel/prob.h:189-193: rhs(UMX) +=
+// rho fx, rhs(UET) += m_x fx) for a body force f per unit mass: component n
+// of the cell's RHS `ds` gets rho f_d (n = UMX+d) or the m_d f_d in x, y, z
+// order (n = UET), for every d with f_d != 0.  U at offset o: the stage input.
+__device__ __forceinline__ double add_source(const DClosures& c, const double* U, long long o, long long ns, int n,
+                                             double ds) {
+  if (n == UET) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      if (c.force[d] != 0.0) ds = ds + U[o + (UMX + d) * ns] * c.force[d];
+  } else if (n != URHO) {
+    const double f = c.force[n - UMX];
+    if (f != 0.0) ds = ds + U[o + URHO * ns] * f;
+  }
+  return ds;
+}
 
 // visc_const_t::visc / visc_suth_t::visc (src/cls/Closures.h:103-120)
 __device__ __forceinline__ double visc(const DClosures& c, double T) {

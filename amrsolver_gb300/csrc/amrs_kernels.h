@@ -11,7 +11,7 @@ namespace amrs {
 // ---- KEEP fused path (rhs_keep.cu)
 cudaError_t launch_prims(const BoxTable& tb, int s_in, long long ncells, int nsm, cudaStream_t st);
 cudaError_t launch_visc(const BoxTable& tb, long long ncells, int nsm, cudaStream_t st);
-cudaError_t launch_keep_face(int order, bool visc, const BoxTable& tb, int s_in, int s_s1, int s_out,
+cudaError_t launch_keep_face(int order, bool visc, bool src, const BoxTable& tb, int s_in, int s_s1, int s_out,
                              const DProg& prog, int rhs_only, const TmaDesc& tma, int* err, int grid, int nsm,
                              cudaStream_t st);
 bool keep_tile_fits(int order, int tx, int ty);
@@ -98,6 +98,8 @@ cudaError_t launch_weno_riemann_vjp(const BoxTable& tb, const DArr& vbar, const 
 size_t weno_vjp_buffer_bytes(const int n[3]);
 cudaError_t launch_weno_vjp(const BoxTable& tb, const FaceRec& fr, const DArr& vbar, const DArr& ubar, double* buf,
                             const int n[3], int nsm, cudaStream_t st);
+cudaError_t launch_source_vjp(const BoxRec& R, const double force[3], const DArr& vbar, const DArr& ubar, int nsm,
+                              cudaStream_t st);
 cudaError_t launch_adj_prog(const BoxRec& R, const DProg& prog, const DArr& wbar, const DArr& s1bar, const DArr& inbar,
                             const DArr& vbar, int accumulate, int nsm, cudaStream_t st);
 cudaError_t launch_adj_halo(const HaloBox& hb, int nsm, cudaStream_t st);

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -42,6 +43,8 @@ DClosures to_dev(const amrs_closures& c) {
   d.visc_ref = c.visc_ref; d.Tvisc_ref = c.Tvisc_ref;
   d.cond_ref = c.cond_ref; d.Tcond_ref = c.Tcond_ref;
   d.Cshock = c.Cshock; d.Cdamp = c.Cdamp;
+  d.source = 0;
+  d.force[0] = d.force[1] = d.force[2] = 0.0;
   return d;
 }
 
@@ -244,6 +247,7 @@ struct List {
   std::vector<long long> pcell, vcell, gcell, valid, fpre[3], spre[3];
   std::vector<int> fwork;
   std::vector<DClosures> cls;
+  bool source = false;    // some closures carry a source term
   // device
   void* dtab = nullptr;   // all tables in one allocation
   size_t dtab_bytes = 0;
@@ -303,6 +307,8 @@ struct amrs_handle {
   void* encode_fn = nullptr;
   List* one = nullptr;               // reusable single-box list for per-box calls
   WallCfg wall{};                    // code-6 y walls of the per-box calls' domain (amrs_set_domain)
+  int source = 0;                    // rhs_source with a body force (amrs_set_source)
+  double force[3] = {0.0, 0.0, 0.0};
   void* adj = nullptr;               // adjoint scratch (pair and viscous cotangents), grow-only
   size_t adj_bytes = 0;
   BoxRec* dring = nullptr;           // per-call box records of per-box calls (device ring)
@@ -361,6 +367,11 @@ amrs_status list_build(amrs_handle* h, List& L, int n, const amrs_box* boxes, co
   L.cls.resize(std::max(ncl, 1));
   if (ncl > 0) for (int c = 0; c < ncl; ++c) L.cls[c] = to_dev(cls[c]);
   else L.cls[0] = to_dev(h->cl);
+  for (DClosures& c : L.cls) {
+    c.source = h->source;
+    for (int d = 0; d < 3; ++d) c.force[d] = h->force[d];
+  }
+  L.source = h->source != 0;
   const int order = h->sc.order_keep;
   const bool need_faces = !L.fused;
   const bool need_visc = h->sc.rhs_visc != 0;
@@ -600,8 +611,8 @@ amrs_status list_stage(amrs_handle* h, List& L, const DProg& prog, int s_in, int
   if (sc.rhs_visc) CK(launch_visc(L.tb, L.tot_v, nsm, st));
   if (L.fused) {
     // 3. fused KEEP faces + viscous averages + divergence + stage program
-    CK(launch_keep_face(sc.order_keep, sc.rhs_visc != 0, L.tb, s_in, s_s1, s_out, prog, rhs_only, L.tma, h->derr,
-                        L.face_grid, nsm, st));
+    CK(launch_keep_face(sc.order_keep, sc.rhs_visc != 0, L.source, L.tb, s_in, s_s1, s_out, prog, rhs_only, L.tma,
+                        h->derr, L.face_grid, nsm, st));
     return AMRS_OK;
   }
   long long nf[3] = {L.tot_f[0], L.tot_f[1], L.tot_f[2]};
@@ -773,6 +784,21 @@ amrs_status amrs_set_closures(amrs_handle* h, const amrs_closures* closures) {
   if (!h || !closures) return AMRS_ERR_NULL;
   std::lock_guard<std::mutex> lk(h->mu);
   h->cl = *closures;
+  if (h->one) { CK(cudaDeviceSynchronize()); delete h->one; h->one = nullptr; }
+  return AMRS_OK;
+}
+
+amrs_status amrs_set_source(amrs_handle* h, int32_t rhs_source, const double force[3]) {
+  if (!h) return AMRS_ERR_NULL;
+  if (rhs_source && !force) return AMRS_ERR_NULL;
+  std::lock_guard<std::mutex> lk(h->mu);
+  const bool on = rhs_source && (force[0] != 0.0 || force[1] != 0.0 || force[2] != 0.0);
+  for (int d = 0; d < 3; ++d) {
+    if (on && !std::isfinite(force[d])) return AMRS_ERR_SCHEME;
+    h->force[d] = on ? force[d] : 0.0;
+  }
+  h->source = on ? 1 : 0;
+  // the per-box list caches its closures table
   if (h->one) { CK(cudaDeviceSynchronize()); delete h->one; h->one = nullptr; }
   return AMRS_OK;
 }
@@ -1466,6 +1492,10 @@ cudaError_t rhs_vjp_launch(amrs_handle* h, List& L, const amrs_box& B, AdjScratc
     const int nb[3] = {bn(B, 0), bn(B, 1), bn(B, 2)};
     e = launch_weno_riemann_vjp(L.tb, S.ah.vbar, S.ah.ubar, S.wbuf, nb, h->nsm, st);
   }
+  if (e == cudaSuccess && h->source) {
+    const BoxRec& R = L.hbox[0];
+    e = launch_source_vjp(R, h->force, S.ah.vbar, S.ah.ubar, h->nsm, st);
+  }
   if (e == cudaSuccess && jst_scheme(h->sc)) {
     // after the Euler part: the WENO5 pass reads lambda from the array the
     // JST sensor pass overwrites
@@ -1723,8 +1753,8 @@ amrs_status amrs_profile_stage_box(amrs_handle* h, const amrs_box* bx, const dou
     if (e == cudaSuccess && sc.rhs_visc) e = launch_visc(L.tb, L.tot_v, h->nsm, st);
     if (e == cudaSuccess) e = cudaEventRecord(ev[2], st);
     if (e == cudaSuccess && L.fused)
-      e = launch_keep_face(sc.order_keep, sc.rhs_visc != 0, L.tb, 0, 1, 2, p, 0, L.tma, h->derr, L.face_grid,
-                           h->nsm, st);
+      e = launch_keep_face(sc.order_keep, sc.rhs_visc != 0, L.source, L.tb, 0, 1, 2, p, 0, L.tma, h->derr,
+                           L.face_grid, h->nsm, st);
     else if (e == cudaSuccess && sc.flux_euler == 2)
       e = launch_weno_faces(L.tb, L.ft, 0, nf, sc.weno_fast == 0, h->nsm, st);
     else if (e == cudaSuccess && sc.flux_euler == 3)

@@ -208,6 +208,8 @@ extern "C" amrs_status amrs_rhs_box_noalloc(const amrs_scheme* scheme, const amr
   cl.visc_ref = closures->visc_ref; cl.Tvisc_ref = closures->Tvisc_ref;
   cl.cond_ref = closures->cond_ref; cl.Tcond_ref = closures->Tcond_ref;
   cl.Cshock = closures->Cshock; cl.Cdamp = closures->Cdamp;
+  cl.source = 0;  // no source term on this path
+  cl.force[0] = cl.force[1] = cl.force[2] = 0.0;
 
   // table region layout: box | closures | pcell | vcell | fwork | err | segs | cta_seg
   size_t t = 0;
@@ -250,7 +252,7 @@ extern "C" amrs_status amrs_rhs_box_noalloc(const amrs_scheme* scheme, const amr
   int* err = reinterpret_cast<int*>(tab + o_err);
   if (launch_prims(tb, 0, pcell[1], nsm, st) != cudaSuccess) return AMRS_ERR_CUDA;
   if (sc.rhs_visc && launch_visc(tb, vcell[1], nsm, st) != cudaSuccess) return AMRS_ERR_CUDA;
-  if (launch_keep_face(order, sc.rhs_visc != 0, tb, 0, 1, 2, prog, 1, tma, err, (int)G, nsm, st) != cudaSuccess)
+  if (launch_keep_face(order, sc.rhs_visc != 0, false, tb, 0, 1, 2, prog, 1, tma, err, (int)G, nsm, st) != cudaSuccess)
     return AMRS_ERR_CUDA;
   return AMRS_OK;
 }

@@ -129,7 +129,7 @@ __device__ __forceinline__ void ld_qs(const double* buf, int idx, int QS, double
 }
 
 // One work item = one (tx x ty) column tile of one box over a chunk of z.
-template <int ORDER, bool VISC>
+template <int ORDER, bool VISC, bool SRC>
 __global__ void __launch_bounds__(F_THREADS, (ORDER == 6) ? 1 : 2)
 keep_face_kernel(BoxTable tb, int s_in, int s_s1, int s_out, DProg prog_in, int rhs_only, TmaDesc tma,
                  int* err) {
@@ -174,6 +174,7 @@ keep_face_kernel(BoxTable tb, int s_in, int s_s1, int s_out, DProg prog_in, int 
     const DArr Q = R.q, VF = R.vf;
     const DArr Uin = R.slot[s_in], U1 = R.slot[s_s1], Uo = R.slot[s_out];
     const double dxi0 = R.dxinv[0], dxi1 = R.dxinv[1], dxi2 = R.dxinv[2];
+    const bool src = SRC && tb.cls[R.cl].source != 0;  // SRC: a list with a source term
     // allocation bounds of Q (grow(box,3))
     const int qlo0 = R.lo[0] - NGHOST, qhi0 = R.hi[0] + NGHOST;
     const int qlo1 = R.lo[1] - NGHOST, qhi1 = R.hi[1] + NGHOST;
@@ -280,7 +281,8 @@ keep_face_kernel(BoxTable tb, int s_in, int s_s1, int s_out, DProg prog_in, int 
         for (int n = 0; n < 5; ++n) {
           const double* fx = fsx + n * C::F_CAP + cb * (TX + 1) + ca;
           const double* fy = fsy + n * C::F_CAP + cb * TX + ca;
-          const double ds = dxi0 * (fx[0] - fx[1]) + dxi1 * (fy[0] - fy[TX]) + dxi2 * (fzprev[n] - fznew[n]);
+          double ds = dxi0 * (fx[0] - fx[1]) + dxi1 * (fy[0] - fy[TX]) + dxi2 * (fzprev[n] - fznew[n]);
+          if (src) ds = add_source(tb.cls[R.cl], Uin.p, oin, Uin.ns, n, ds);
           if (rhs_only) {
             Uo.p[oo + n * Uo.ns] = ds;
           } else {
@@ -452,7 +454,7 @@ keep_face_kernel(BoxTable tb, int s_in, int s_s1, int s_out, DProg prog_in, int 
 }
 
 // explicit instantiations + launchers
-template <int ORDER, bool VISC>
+template <int ORDER, bool VISC, bool SRC>
 static cudaError_t launch_face_t(const BoxTable& tb, int s_in, int s_s1, int s_out, const DProg& prog, int rhs_only,
                                  const TmaDesc& tma, int* err, int grid, cudaStream_t st) {
   const int smem = keep_smem_bytes<ORDER>();
@@ -464,11 +466,11 @@ static cudaError_t launch_face_t(const BoxTable& tb, int s_in, int s_s1, int s_o
   if (e != cudaSuccess) return e;
   const unsigned long long bit = 1ull << (dev & 63);
   if (dev >= 64 || !(attr_set.load() & bit)) {
-    e = cudaFuncSetAttribute(keep_face_kernel<ORDER, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    e = cudaFuncSetAttribute(keep_face_kernel<ORDER, VISC, SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     attr_set.fetch_or(bit);
   }
-  keep_face_kernel<ORDER, VISC><<<grid, F_THREADS, smem, st>>>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err);
+  keep_face_kernel<ORDER, VISC, SRC><<<grid, F_THREADS, smem, st>>>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err);
   return cudaGetLastError();
 }
 
@@ -490,17 +492,20 @@ cudaError_t launch_visc(const BoxTable& tb, long long ncells, int nsm, cudaStrea
   return cudaGetLastError();
 }
 
-cudaError_t launch_keep_face(int order, bool visc, const BoxTable& tb, int s_in, int s_s1, int s_out,
+cudaError_t launch_keep_face(int order, bool visc, bool src, const BoxTable& tb, int s_in, int s_s1, int s_out,
                              const DProg& prog, int rhs_only, const TmaDesc& tma, int* err, int grid, int nsm,
                              cudaStream_t st) {
   (void)nsm;
   if (grid <= 0) return cudaSuccess;
-  if (order == 2) return visc ? launch_face_t<2, true>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err, grid, st)
-                              : launch_face_t<2, false>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err, grid, st);
-  if (order == 4) return visc ? launch_face_t<4, true>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err, grid, st)
-                              : launch_face_t<4, false>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err, grid, st);
-  return visc ? launch_face_t<6, true>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err, grid, st)
-              : launch_face_t<6, false>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err, grid, st);
+#define AMRS_FACE(O, V, S) launch_face_t<O, V, S>(tb, s_in, s_s1, s_out, prog, rhs_only, tma, err, grid, st)
+#define AMRS_FACE_VS(O) \
+  (visc ? (src ? AMRS_FACE(O, true, true) : AMRS_FACE(O, true, false)) \
+        : (src ? AMRS_FACE(O, false, true) : AMRS_FACE(O, false, false)))
+  if (order == 2) return AMRS_FACE_VS(2);
+  if (order == 4) return AMRS_FACE_VS(4);
+  return AMRS_FACE_VS(6);
+#undef AMRS_FACE_VS
+#undef AMRS_FACE
 }
 
 int keep_ctas_per_sm(int order) { return order == 6 ? 1 : 2; }

@@ -660,10 +660,13 @@ __global__ void __launch_bounds__(256) div_stage_kernel(BoxTable tb, FaceTable f
     const DArr Fx = FR.f[0], Fy = FR.f[1], Fz = FR.f[2];
     const long long ox = Fx.off(i, j, k), oy = Fy.off(i, j, k), oz = Fz.off(i, j, k);
     const DArr Uin = R.slot[s_in], U1 = R.slot[s_s1], Uo = R.slot[s_out];
+    const DClosures& cl = tb.cls[R.cl];
+    const long long oin = Uin.off(i, j, k);
     for (int n = 0; n < 5; ++n) {
-      const double ds = R.dxinv[0] * (Fx.p[ox + n * Fx.ns] - Fx.p[ox + 1 + n * Fx.ns]) +
-                        R.dxinv[1] * (Fy.p[oy + n * Fy.ns] - Fy.p[oy + Fy.js + n * Fy.ns]) +
-                        R.dxinv[2] * (Fz.p[oz + n * Fz.ns] - Fz.p[oz + Fz.ks + n * Fz.ns]);
+      double ds = R.dxinv[0] * (Fx.p[ox + n * Fx.ns] - Fx.p[ox + 1 + n * Fx.ns]) +
+                  R.dxinv[1] * (Fy.p[oy + n * Fy.ns] - Fy.p[oy + Fy.js + n * Fy.ns]) +
+                  R.dxinv[2] * (Fz.p[oz + n * Fz.ns] - Fz.p[oz + Fz.ks + n * Fz.ns]);
+      if (cl.source) ds = add_source(cl, Uin.p, oin, Uin.ns, n, ds);
       if (rhs_only) {
         Uo(i, j, k, n) = ds;
       } else {

@@ -79,6 +79,10 @@ class Scheme:
     weno_fast (not a reference switch): 0 (default) evaluates WENO5 in the
     reference's operation order (bit-identical results); 1 forms the weights
     over a common denominator (faster, rounding differences only).
+
+    rhs_source: cns.rhs_source; the source is the problem's user_source,
+    here a constant body force per unit mass `body_force` (the channel
+    problem's, exm/Channel/prob.h:189-193, is (fx, 0, 0)).
     """
     rhs_euler: int = 1
     rhs_visc: int = 1
@@ -87,6 +91,8 @@ class Scheme:
     art_diss: int = 0
     weno_fast: int = 0
     riemann_weno: int = 0
+    rhs_source: int = 0
+    body_force: tuple = (0.0, 0.0, 0.0)
 
 
 @dataclasses.dataclass

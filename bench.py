@@ -49,7 +49,7 @@ WORKLOAD = "Taylor-Green vortex 128^3 periodic, M=0.1 Re=1600 Pr=0.71, KEEP4 + v
 
 # --scheme: (switches, op-count key, dominant kernel, its ncu summary, kernels of ours per stage, label)
 SCHEMES = {
-    "keep4": (dict(flux_euler=1, order_keep=4, rhs_visc=1), "keep4_visc", "keep_face_kernel<4,true>",
+    "keep4": (dict(flux_euler=1, order_keep=4, rhs_visc=1), "keep4_visc", "keep_face_kernel<4,true,false>",
               "keep_face_kernel_tgv128.md", 4, "KEEP4 + viscous"),
     "weno": (dict(flux_euler=2, rhs_visc=1), "weno_visc", "weno_face_kernel<true> (reference operation order)",
              "weno_face_kernel_tgv96.md", 7, "WENO5-LLF + viscous, reference operation order"),

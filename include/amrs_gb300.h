@@ -136,6 +136,16 @@ amrs_status amrs_set_closures(amrs_handle* h, const amrs_closures* closures);
  * derivative the library does not have): such domains use
  * amrs_rk_stage_vjp_box_ghosted. */
 amrs_status amrs_set_domain(amrs_handle* h, const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3]);
+/* cns.rhs_source (src/CNS.cpp:22,103) with the problem's user_source being a
+ * constant body force per unit mass f, the source step of compute_rhs
+ * (src/tim/CNS_advance.cpp:396-407): after the flux divergence, dSdt(UMX+d)
+ * += rho f_d and dSdt(UET) += m_d f_d (x, y, z order) for every d with
+ * f_d != 0, from the stage input's conserved state.  The channel problem's
+ * user_source (exm/Channel/prob.h:189-193) is f = (fx, 0, 0).  rhs_source 0
+ * or an all-zero force: no source (problems whose user_source is empty).
+ * Applies to the handle's per-box calls (forward and VJP) and to box lists
+ * created afterwards. */
+amrs_status amrs_set_source(amrs_handle* h, int32_t rhs_source, const double force[3]);
 const char* amrs_status_string(amrs_status s);
 /* Last CUDA error string recorded by the library (thread-local). */
 const char* amrs_last_cuda_error(void);

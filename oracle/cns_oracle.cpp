@@ -193,6 +193,8 @@ struct Scheme {
   int flux_euler;  // 1 = KEEP, 2 = WENO5-JS LLF, 3 = WENO5-Riemann (extension), other = MUSCL + Riemann
   int order_keep;  // 2, 4, 6
   int art_diss;    // JST artificial dissipation
+  int rhs_source;  // cns.rhs_source, with the body-force source below
+  double force[3]; // body force per unit mass of the source term
 };
 
 // KEEP coefficients, CPU branch of the reference (src/CNS.cpp:241-252).
@@ -902,6 +904,21 @@ void compute_rhs_box(const Scheme& sc, const Closures& cl, const Box& bx, const 
           ds(i, j, k, n) = R(dxinv[0]) * (F[0](i, j, k, n) - F[0](i + 1, j, k, n)) +
                            R(dxinv[1]) * (F[1](i, j, k, n) - F[1](i, j + 1, k, n)) +
                            R(dxinv[2]) * (F[2](i, j, k, n) - F[2](i, j, k + 1, n));
+
+  // 5. source term (:396-407): the channel problem's user_source
+  //    (exm/Channel/prob.h:189-193: rhs(UMX) += rho fx, rhs(UET) += m_x fx)
+  //    for a body force f per unit mass, each direction with f_d != 0 in
+  //    x, y, z order
+  if (sc.rhs_source) {
+    for (int k = lo2; k <= hi2; ++k)
+      for (int j = lo1; j <= hi1; ++j)
+        for (int i = lo0; i <= hi0; ++i)
+          for (int d = 0; d < 3; ++d) {
+            if (sc.force[d] == 0.0) continue;
+            ds(i, j, k, UMX + d) = ds(i, j, k, UMX + d) + u(i, j, k, URHO) * R(sc.force[d]);
+            ds(i, j, k, UET) = ds(i, j, k, UET) + u(i, j, k, UMX + d) * R(sc.force[d]);
+          }
+  }
 }
 
 // -------------------------------------------------------------- halo fill --
@@ -1090,7 +1107,8 @@ struct OrcClosures {
   double visc_ref, Tvisc_ref, cond_ref, Tcond_ref, Cshock, Cdamp;
 };
 struct OrcScheme {
-  int32_t rhs_euler, rhs_visc, flux_euler, order_keep, art_diss;
+  int32_t rhs_euler, rhs_visc, flux_euler, order_keep, art_diss, rhs_source;
+  double force[3];
 };
 
 static Closures to_cl(const OrcClosures* c) {
@@ -1105,6 +1123,8 @@ static Scheme to_sc(const OrcScheme* s) {
   Scheme sc;
   sc.rhs_euler = s->rhs_euler; sc.rhs_visc = s->rhs_visc; sc.flux_euler = s->flux_euler;
   sc.order_keep = s->order_keep; sc.art_diss = s->art_diss;
+  sc.rhs_source = s->rhs_source;
+  for (int d = 0; d < 3; ++d) sc.force[d] = s->force[d];
   return sc;
 }
 static Box to_box(const int* lo, const int* hi) {

@@ -29,7 +29,8 @@ class CClosures(ctypes.Structure):
 class CScheme(ctypes.Structure):
     _fields_ = [("rhs_euler", ctypes.c_int32), ("rhs_visc", ctypes.c_int32),
                 ("flux_euler", ctypes.c_int32), ("order_keep", ctypes.c_int32),
-                ("art_diss", ctypes.c_int32)]
+                ("art_diss", ctypes.c_int32), ("rhs_source", ctypes.c_int32),
+                ("force", ctypes.c_double * 3)]
 
 
 def c_closures(cl):
@@ -43,7 +44,10 @@ def c_scheme(sc):
     fe = int(sc.flux_euler)
     if fe not in (1, 2):
         fe = 3 if int(getattr(sc, "riemann_weno", 0)) else 0
-    return CScheme(int(sc.rhs_euler), int(sc.rhs_visc), fe, int(sc.order_keep), int(sc.art_diss))
+    src = int(getattr(sc, "rhs_source", 0))
+    f = getattr(sc, "body_force", (0.0, 0.0, 0.0))
+    return CScheme(int(sc.rhs_euler), int(sc.rhs_visc), fe, int(sc.order_keep), int(sc.art_diss), src,
+                   (ctypes.c_double * 3)(*[float(x) for x in f]))
 
 
 def _i3(v):

@@ -129,7 +129,8 @@ struct OrcClosures {
   double visc_ref, Tvisc_ref, cond_ref, Tcond_ref, Cshock, Cdamp;
 };
 struct OrcScheme {
-  int32_t rhs_euler, rhs_visc, flux_euler, order_keep, art_diss;
+  int32_t rhs_euler, rhs_visc, flux_euler, order_keep, art_diss, rhs_source;
+  double force[3];
 };
 
 static PROB::ProbClosures g_cl;
@@ -163,7 +164,8 @@ static int set_closures(const OrcClosures* c) {
 static void set_scheme(const OrcScheme* s) {
   CNS::rhs_euler = s->rhs_euler != 0;
   CNS::rhs_visc = s->rhs_visc != 0;
-  CNS::rhs_source = false;
+  CNS::rhs_source = s->rhs_source != 0;
+  for (int d = 0; d < 3; ++d) g_parm.force[d] = s->force[d];
   CNS::flux_euler = s->flux_euler;
   CNS::art_diss = s->art_diss;
   CentralKEEP::order_keep = s->order_keep;

@@ -45,7 +45,7 @@ inline void inputs() {}
 typedef closures_derived_t<REF_VISC, REF_COND, calorifically_perfect_gas_t> ProbClosures;
 
 struct ProbParm {
-  Real dummy = 0.0;
+  Real force[3] = {0.0, 0.0, 0.0};  // body force per unit mass (user_source)
 };
 
 AMREX_GPU_DEVICE AMREX_FORCE_INLINE void bcnormal(const Real*, Real, const Real*, const Real*, Real*, const int,
@@ -54,8 +54,17 @@ AMREX_GPU_DEVICE AMREX_FORCE_INLINE void bcnormal(const Real*, Real, const Real*
   Abort("bcnormal not available in the oracle build");
 }
 
-AMREX_GPU_DEVICE AMREX_FORCE_INLINE void user_source(int, int, int, const auto&, const auto&, const ProbParm&,
-                                                     ProbClosures const&, auto const) {}
+// A body force per unit mass, as the channel problem's user_source applies
+// its x force (exm/Channel/prob.h:189-193), for each direction with a
+// nonzero component.
+AMREX_GPU_DEVICE AMREX_FORCE_INLINE void user_source(int i, int j, int k, const auto& state, const auto& rhs,
+                                                     const ProbParm& pp, ProbClosures const&, auto const) {
+  for (int d = 0; d < 3; ++d) {
+    if (pp.force[d] == 0.0) continue;
+    rhs(i, j, k, UMX + d) += state(i, j, k, URHO) * pp.force[d];
+    rhs(i, j, k, UET) += state(i, j, k, UMX + d) * pp.force[d];
+  }
+}
 
 }  // namespace PROB
 #endif

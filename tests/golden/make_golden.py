@@ -62,6 +62,14 @@ WALL_CASES = [
     ("weno_visc", dict(flux_euler=2, rhs_visc=1), (5, 6, 4), (0, 3, 0), (2.0, 2.5, 3.0), (0, 1)),
 ]
 
+SOURCE_CASES = [
+    # name, scheme kwargs, body force (cns.rhs_source = 1), box shape, lo, dxinv; the first is the channel
+    # problem's form (fx, 0, 0)
+    ("keep4_visc", dict(flux_euler=1, order_keep=4, rhs_visc=1), (2.5, 0.0, 0.0), (6, 5, 4), (1, 0, -2),
+     (2.0, 2.5, 3.0)),
+    ("weno_visc", dict(flux_euler=2, rhs_visc=1), (0.5, -1.5, 0.25), (5, 6, 4), (0, 0, 0), (2.0, 2.0, 2.0)),
+]
+
 ADV_CASES = [
     # name, order_rk, stages_rk
     ("ssprk3", 3, 3), ("ssprk43", 3, 4), ("ssprkm2_3", 2, 3), ("euler", 1, 1), ("heun", -2, 2), ("rhsonly", 0, 1),
@@ -80,6 +88,22 @@ def write_wall_cases():
         R = ref.rhs(sc, cl, U, dxinv, lo=lo, walls=w)
         np.savez_compressed(os.path.join(HERE, "wall_%s.npz" % name), U=U, dSdt=R, lo=np.array(lo),
                             dxinv=np.array(dxinv), walls=np.array(w),
+                            scheme=np.array([sc.rhs_euler, sc.rhs_visc, sc.flux_euler, sc.order_keep, sc.art_diss]),
+                            closures="const")
+
+
+def write_source_cases():
+    """RHS with cns.rhs_source on and a body-force user_source: the source
+    step of the reference's compute_rhs (rhs_source_*.npz; the `force` entry
+    switches it on when loaded)."""
+    cl = closures("const")
+    ref = pyoracle.reference(cl)
+    for i, (name, skw, force, n, lo, dxinv) in enumerate(SOURCE_CASES):
+        sc = P.Scheme(rhs_source=1, body_force=force, **skw)
+        U = P.random_state(n, seed=400 + i)
+        R = ref.rhs(sc, cl, U, dxinv, lo=lo)
+        np.savez_compressed(os.path.join(HERE, "rhs_source_%s.npz" % name), U=U, dSdt=R, lo=np.array(lo),
+                            dxinv=np.array(dxinv), force=np.array(force),
                             scheme=np.array([sc.rhs_euler, sc.rhs_visc, sc.flux_euler, sc.order_keep, sc.art_diss]),
                             closures="const")
 
@@ -127,6 +151,7 @@ def main():
         halo["bc_" + tag] = np.array([bl, bh])
     np.savez_compressed(os.path.join(HERE, "halo.npz"), V=V, **halo)
     write_wall_cases()
+    write_source_cases()
     print("wrote golden fixtures:", sorted(os.listdir(HERE)))
 
 

@@ -23,6 +23,9 @@ def rhs_cases():
         s = z["scheme"]
         sc = P.Scheme(rhs_euler=int(s[0]), rhs_visc=int(s[1]), flux_euler=int(s[2]), order_keep=int(s[3]),
                       art_diss=int(s[4]))
+        if "force" in z.files:  # cns.rhs_source with a body force
+            sc.rhs_source = 1
+            sc.body_force = tuple(float(v) for v in z["force"])
         out.append(dict(name=os.path.basename(f)[4:-4], U=z["U"], dSdt=z["dSdt"], lo=tuple(int(v) for v in z["lo"]),
                         dxinv=tuple(float(v) for v in z["dxinv"]), scheme=sc, closures=closures(z["closures"])))
     return out

@@ -56,3 +56,36 @@ def test_advance_bitexact(orc, ork, srk):
     a = orc.advance(sc, CL, U, dxinv, (-1, -1, -1), (-1, -1, -1), 3e-3, ork, srk)
     b = REF.advance(sc, CL, U, dxinv, (-1, -1, -1), (-1, -1, -1), 3e-3, ork, srk)
     np.testing.assert_array_equal(P.valid(a), P.valid(b))
+
+
+SOURCE_FORCES = [(3.5, 0.0, 0.0), (0.0, -1.25, 0.0), (0.7, 2.0, -0.3)]
+
+
+@pytest.mark.parametrize("force", SOURCE_FORCES)
+@pytest.mark.parametrize("skw", [dict(flux_euler=1, order_keep=4, rhs_visc=1), dict(flux_euler=2, rhs_visc=1),
+                                 dict(flux_euler=0, rhs_visc=0)], ids=["keep4_visc", "weno_visc", "muscl"])
+def test_rhs_source_bitexact(orc, skw, force):
+    """cns.rhs_source: the source step of the reference's compute_rhs (after
+    the divergence, from the stage input) with a body-force user_source; the
+    first force is the channel problem's form, (fx, 0, 0)."""
+    sc = P.Scheme(rhs_source=1, body_force=force, **skw)
+    rng = np.random.default_rng(17 + len(str(skw)))
+    n = tuple(int(v) for v in rng.integers(4, 9, 3))
+    U = P.random_state(n, seed=int(rng.integers(1 << 30)), amp=0.2)
+    lo = tuple(int(v) for v in rng.integers(-5, 5, 3))
+    dxinv = tuple(float(v) for v in rng.uniform(1.0, 5.0, 3))
+    a = orc.rhs(sc, CL, U, dxinv, lo=lo)
+    np.testing.assert_array_equal(a, REF.rhs(sc, CL, U, dxinv, lo=lo))
+    # the source changed the momentum and energy RHS, not the mass RHS
+    b = orc.rhs(P.Scheme(**skw), CL, U, dxinv, lo=lo)
+    np.testing.assert_array_equal(a[0], b[0])
+    assert not np.array_equal(a[4], b[4])
+
+
+def test_advance_with_source_bitexact(orc):
+    sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1, rhs_source=1, body_force=(2.0, 0.0, 0.0))
+    U, dx = P.tgv(10, mach=0.2)
+    dxinv = [1.0 / h for h in dx]
+    a = orc.advance(sc, CL, U, dxinv, (-1, -1, -1), (-1, -1, -1), 3e-3, 3, 3)
+    b = REF.advance(sc, CL, U, dxinv, (-1, -1, -1), (-1, -1, -1), 3e-3, 3, 3)
+    np.testing.assert_array_equal(P.valid(a), P.valid(b))

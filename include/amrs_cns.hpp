@@ -129,14 +129,19 @@ class CNS {
   static constexpr int NCONS = 5;
   static constexpr int NGHOST = 3;
 
+  // body_force: cns.rhs_source = 1 with a constant body force per unit mass
+  // as the problem's user_source (the channel problem's is {fx, 0, 0});
+  // nullptr: rhs_source = 0.
   CNS(const Geometry& geom, const amrs_scheme& scheme, const amrs_closures& closures, int order_rk = 3,
-      int stages_rk = 3, int device = 0)
-      : CNS(geom, std::vector<Box>{geom.domain}, scheme, closures, order_rk, stages_rk, device) {}
+      int stages_rk = 3, int device = 0, const Real* body_force = nullptr)
+      : CNS(geom, std::vector<Box>{geom.domain}, scheme, closures, order_rk, stages_rk, device, body_force) {}
 
   CNS(const Geometry& geom, const std::vector<Box>& grids, const amrs_scheme& scheme,
-      const amrs_closures& closures, int order_rk = 3, int stages_rk = 3, int device = 0)
+      const amrs_closures& closures, int order_rk = 3, int stages_rk = 3, int device = 0,
+      const Real* body_force = nullptr)
       : geom_(geom), grids_(grids), order_rk_(order_rk), stages_rk_(stages_rk) {
     check(amrs_create(&h_, &scheme, &closures, device), "amrs_create");
+    if (body_force) check(amrs_set_source(h_, 1, body_force), "amrs_set_source");
     for (int i = 0; i < 3; ++i) state_[i].define(grids, NCONS, NGHOST);
     for (int d = 0; d < 3; ++d) dxinv_[d] = 1.0 / geom.dx[d];
     const int n = (int)grids.size();

@@ -39,6 +39,15 @@ class CScheme(ctypes.Structure):
                 ("riemann_weno", ctypes.c_int32)]
 
 
+class CBcNormal(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("Tw", ctypes.c_double), ("Tmin", ctypes.c_double),
+                ("prob_lo", ctypes.c_double * 3), ("prob_hi", ctypes.c_double * 3), ("dx", ctypes.c_double * 3)]
+
+
+def c_bcnormal(bn):
+    return CBcNormal(int(bn.kind), float(bn.Tw), float(bn.Tmin), d3(bn.prob_lo), d3(bn.prob_hi), d3(bn.dx))
+
+
 class CBox(ctypes.Structure):
     _fields_ = [("lo", ctypes.c_int32 * 3), ("hi", ctypes.c_int32 * 3)]
 
@@ -107,6 +116,10 @@ SIGNATURES = {
     "amrs_rk_stage_vjp_box_ghosted": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(StageProg), Array4, Array4, Array4, Array4, _P, _P]),
     "amrs_set_source": (_S, [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]),
+    "amrs_fill_halo_box_bcnormal": (_S, [ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_int32),
+                                         ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(CClosures),
+                                         ctypes.POINTER(CBcNormal), Array4, _P]),
+    "amrs_boxlist_set_bcnormal": (_S, [_P, ctypes.POINTER(CBcNormal)]),
     "amrs_sync_check": (_S, [_P, _P]),
     "amrs_probe_fp64_tflops": (_S, [_P, ctypes.POINTER(ctypes.c_double)]),
     "amrs_debug_wait_timeout": (_S, [_P, ctypes.c_int32, _P]),
@@ -333,6 +346,17 @@ def fill_halo_box(U, bc_lo, bc_hi, lo=(0, 0, 0), stream=None):
           "amrs_fill_halo_box")
 
 
+def fill_halo_box_bcnormal(U, bc_lo, bc_hi, closures, bn, lo=(0, 0, 0), stream=None):
+    """fill_halo_box, then the device bcnormal `bn` (problems.BCNormal)
+    beyond code-6 y sides (amrs_fill_halo_box_bcnormal)."""
+    L = load()
+    nz, ny, nx = (s - 2 * NGHOST for s in U.shape[1:])
+    bx = c_box(lo, (nx, ny, nz))
+    check(L.amrs_fill_halo_box_bcnormal(ctypes.byref(bx), i3(bc_lo), i3(bc_hi), ctypes.byref(c_closures(closures)),
+                                        ctypes.byref(c_bcnormal(bn)), array4(U, lo, NGHOST), _stream_ptr(stream)),
+          "amrs_fill_halo_box_bcnormal")
+
+
 def fill_halo_box_adjoint(ubar, bc_lo, bc_hi, lo=(0, 0, 0), stream=None):
     """Adjoint of fill_halo_box, in place on the ghosted cotangent `ubar`:
     valid cells receive the cotangents of the ghosts filled from them
@@ -423,6 +447,12 @@ class BoxList:
         dom = c_box(dom_lo, dom_n)
         check(self._L.amrs_boxlist_set_domain(self.bl, ctypes.byref(dom), i3(bc_lo), i3(bc_hi)),
               "amrs_boxlist_set_domain")
+
+    def set_bcnormal(self, bn):
+        """Device bcnormal (problems.BCNormal, None: none) beyond the domain's
+        code-6 y sides in every later fill (amrs_boxlist_set_bcnormal)."""
+        check(self._L.amrs_boxlist_set_bcnormal(self.bl, ctypes.byref(c_bcnormal(bn)) if bn is not None else None),
+              "amrs_boxlist_set_bcnormal")
 
     def fill_halo(self, slot, stream=None):
         check(self._L.amrs_boxlist_fill_halo(self.bl, slot, _stream_ptr(stream)), "amrs_boxlist_fill_halo")

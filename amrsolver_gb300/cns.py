@@ -22,12 +22,14 @@ class CNSLevel:
 
     def __init__(self, scheme, closures, U0, dx, bc_lo=(-1, -1, -1), bc_hi=(-1, -1, -1), lo=(0, 0, 0),
                  order_rk=3, stages_rk=3, device=0, bcnormal=None):
-        """`bcnormal(t)`, if given, fills the ghost cells beyond the ext_dir
-        sides (codes 1, 6) of the ghosted state tensor `t` in place after the
-        library's fill, as the problem's bcnormal does in cns_bcfill
-        (src/set/bcs.cpp:30-100); written with torch operations, it is
-        differentiated by torch autograd in the adjoint.  Without it those
-        ghost cells keep the values of U0."""
+        """`bcnormal`, if given, fills the ghost cells beyond the ext_dir
+        sides (codes 1, 6) after the library's fill, as the problem's
+        bcnormal does in cns_bcfill (src/set/bcs.cpp:30-100): either a
+        callable `bcnormal(t)` on the ghosted state tensor written with torch
+        operations (differentiated by torch autograd in the adjoint), or a
+        problems.BCNormal that the library evaluates on the device beyond
+        code-6 y sides (forward only).  Without it those ghost cells keep the
+        values of U0."""
         self.scheme, self.closures = scheme, closures
         self.bcnormal = bcnormal
         self.h = capi.Handle(scheme, closures, device)
@@ -66,9 +68,13 @@ class CNSLevel:
     def fill_patch(self, t, stream=None):
         """Ghost fill of `t` in place (single-level FillPatch): periodic
         images and physical BCs, then the ext_dir ghosts by `bcnormal`."""
-        capi.fill_halo_box(t, self.bc_lo, self.bc_hi, self.lo, stream)
-        if self.bcnormal is not None:
+        if self.bcnormal is None:
+            capi.fill_halo_box(t, self.bc_lo, self.bc_hi, self.lo, stream)
+        elif callable(self.bcnormal):
+            capi.fill_halo_box(t, self.bc_lo, self.bc_hi, self.lo, stream)
             self.bcnormal(t)
+        else:
+            capi.fill_halo_box_bcnormal(t, self.bc_lo, self.bc_hi, self.closures, self.bcnormal, self.lo, stream)
 
     def has_ext_dir(self):
         return any(b in (1, 6) for b in self.bc_lo + self.bc_hi)
@@ -80,6 +86,9 @@ class CNSLevel:
         ghosts are constants and their cotangents are simply not used."""
         if self.bcnormal is None:
             return gbar
+        if not callable(self.bcnormal):
+            raise NotImplementedError("the adjoint needs the bcnormal as a torch function; the device bcnormal "
+                                      "is forward only")
         with torch.enable_grad():
             x = t.detach().clone().requires_grad_(True)
             y = x.clone()

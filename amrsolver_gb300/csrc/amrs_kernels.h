@@ -127,6 +127,17 @@ struct LevelDomain {
 };
 cudaError_t launch_halo_level(const BoxTable& tb, const long long* gpre, const int* owner, long long total, int slot,
                               const LevelDomain& dom, int nsm, cudaStream_t st);
+// A problem bcnormal evaluated on the device for y sides of code 6 (kind 1:
+// the channel problem's isothermal no-slip wall), after the library's fill.
+struct DBcNormal {
+  int kind;
+  double Tw, Tmin;
+  double prob_lo[3], prob_hi[3], dx[3];
+};
+cudaError_t launch_bcnormal_box(const DArr& u, const int lo[3], const int hi[3], const int bc_lo[3],
+                                const int bc_hi[3], const DClosures& cl, const DBcNormal& bn, cudaStream_t st);
+cudaError_t launch_bcnormal_list(const BoxTable& tb, int slot, const LevelDomain& dom, const DBcNormal& bn, int nsm,
+                                 cudaStream_t st);
 cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t st);
 // amrex::average_down of cell-centred data (coarse box lo, extents n, ratio r).
 cudaError_t launch_avgdown(const DArr& fine, const DArr& crse, const int lo[3], const int n[3], const int r[3],

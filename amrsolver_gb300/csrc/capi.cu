@@ -48,6 +48,24 @@ DClosures to_dev(const amrs_closures& c) {
   return d;
 }
 
+amrs_status check_bcnormal(const amrs_bcnormal& b) {
+  if (b.kind < 0 || b.kind > 1) return AMRS_ERR_BC;
+  if (b.kind == 1) {
+    if (!(b.Tw > 0.0) || !std::isfinite(b.Tw) || !std::isfinite(b.Tmin)) return AMRS_ERR_BC;
+    if (!(b.dx[1] > 0.0) || !(b.prob_hi[1] > b.prob_lo[1])) return AMRS_ERR_BC;
+  }
+  return AMRS_OK;
+}
+
+DBcNormal to_dbcn(const amrs_bcnormal& b) {
+  DBcNormal d{};
+  d.kind = b.kind;
+  d.Tw = b.Tw;
+  d.Tmin = b.Tmin;
+  for (int k = 0; k < 3; ++k) { d.prob_lo[k] = b.prob_lo[k]; d.prob_hi[k] = b.prob_hi[k]; d.dx[k] = b.dx[k]; }
+  return d;
+}
+
 DArr to_darr(const amrs_array4& a) {
   DArr d;
   d.p = a.p; d.js = a.jstride; d.ks = a.kstride; d.ns = a.nstride;
@@ -271,6 +289,7 @@ struct List {
   int has_bc = 0;
   int bc_lo[3] = {-1, -1, -1}, bc_hi[3] = {-1, -1, -1};
   LevelDomain dom{};
+  DBcNormal bcn{};         // device bcnormal of the code-6 y sides (kind 0: none)
   int* d_owner = nullptr;  // has_bc == 2: owning box of every grown cell's source (-1: valid cell)
   WallCfg wall{};          // code-6 y walls of the list's domain (amrs_boxlist_set_domain)
   // device-resident time loop (amrs_rk_run_boxlist)
@@ -883,6 +902,21 @@ amrs_status amrs_fill_halo_box(const amrs_box* domain, const int32_t bc_lo[3], c
   return AMRS_OK;
 }
 
+amrs_status amrs_fill_halo_box_bcnormal(const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3],
+                                        const amrs_closures* closures, const amrs_bcnormal* bnp, amrs_array4 state,
+                                        void* stream) {
+  if (!closures || !bnp) return AMRS_ERR_NULL;
+  if (amrs_status s = check_bcnormal(*bnp)) return s;
+  if (state.ncomp < NCONS) return AMRS_ERR_LAYOUT;
+  if (amrs_status s = amrs_fill_halo_box(domain, bc_lo, bc_hi, state, stream)) return s;
+  const int lo[3] = {domain->lo[0], domain->lo[1], domain->lo[2]};
+  const int hi[3] = {domain->hi[0], domain->hi[1], domain->hi[2]};
+  const int bl[3] = {bc_lo[0], bc_lo[1], bc_lo[2]}, bh[3] = {bc_hi[0], bc_hi[1], bc_hi[2]};
+  CK(launch_bcnormal_box(to_darr(state), lo, hi, bl, bh, to_dev(*closures), to_dbcn(*bnp),
+                         static_cast<cudaStream_t>(stream)));
+  return AMRS_OK;
+}
+
 amrs_status amrs_average_down(const amrs_box* crse_box, const int32_t ratio[3], amrs_array4 fine, amrs_array4 crse,
                                int32_t scomp, int32_t ncomp, void* stream) {
   if (!crse_box || !ratio) return AMRS_ERR_NULL;
@@ -1083,7 +1117,13 @@ amrs_status level_owner_table(const List& L, const LevelDomain& dom, std::vector
 
 // Ghost fill of one state slot of every box of a list (before a stage).
 cudaError_t list_fill(amrs_handle* h, List& L, int slot, cudaStream_t st) {
-  if (L.has_bc == 2) return launch_halo_level(L.tb, L.ft.gpre, L.d_owner, L.tot_g, slot, L.dom, h->nsm, st);
+  if (L.has_bc == 2) {
+    cudaError_t e = launch_halo_level(L.tb, L.ft.gpre, L.d_owner, L.tot_g, slot, L.dom, h->nsm, st);
+    // then the problem's bcnormal beyond code-6 y sides (it reads the
+    // first interior row, ghost columns included, that the fill wrote)
+    if (e == cudaSuccess && L.bcn.kind) e = launch_bcnormal_list(L.tb, slot, L.dom, L.bcn, h->nsm, st);
+    return e;
+  }
   return launch_halo_list(L.tb, L.ft.gpre, L.tot_g, slot, L.bc_lo, L.bc_hi, h->nsm, st);
 }
 
@@ -1194,6 +1234,23 @@ amrs_status amrs_boxlist_set_domain(amrs_boxlist* bl, const amrs_box* domain, co
   L.dom = dom;
   L.has_bc = 2;
   if (L.graph) { cudaGraphExecDestroy(L.graph); L.graph = nullptr; }
+  if (L.run_graph) { cudaGraphExecDestroy(L.run_graph); L.run_graph = nullptr; }
+  return AMRS_OK;
+}
+
+amrs_status amrs_boxlist_set_bcnormal(amrs_boxlist* bl, const amrs_bcnormal* bnp) {
+  if (!bl) return AMRS_ERR_NULL;
+  DBcNormal d{};
+  if (bnp) {
+    if (amrs_status s = check_bcnormal(*bnp)) return s;
+    d = to_dbcn(*bnp);
+  }
+  List& L = bl->L;
+  CK(cudaSetDevice(bl->h->device));
+  CK(cudaDeviceSynchronize());  // queued fills may read the old setting
+  L.bcn = d;
+  if (L.graph) { cudaGraphExecDestroy(L.graph); L.graph = nullptr; }
+  if (L.run_graph) { cudaGraphExecDestroy(L.run_graph); L.run_graph = nullptr; }
   return AMRS_OK;
 }
 

@@ -166,6 +166,116 @@ cudaError_t launch_halo(const HaloBox& hb, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------ device bcnormal --
+// The ghost cell (i, j, k) beyond a code-6 y side (side 0: below the domain,
+// 1: above) from the first interior row jf, as cns_bcfill
+// (src/set/bcs.cpp:40-100) calls the channel problem's bcnormal
+// (exm/Channel/prob.h:158-186): x = prob_lo + (j + 0.5) dx of the ghost,
+// dratio = de/di (ghost-to-wall over first-cell-to-wall distance), no-slip
+// velocity (the interior velocity negated), the interior pressure, the wall
+// temperature extrapolated, T = max(Tw + dratio (Tw - T_int), Tmin), and
+// rho = p / (R T), written back as conserved variables.
+__device__ void bcnormal_isothermal_cell(const DArr& U, int i, int j, int k, int jf, int side,
+                                         const DClosures& c, const DBcNormal& bn) {
+  const double rho = U(i, jf, k, URHO), mx = U(i, jf, k, UMX), my = U(i, jf, k, UMY), mz = U(i, jf, k, UMZ);
+  const double et = U(i, jf, k, UET);
+  const double ue = -mx / rho, ve = -my / rho, we = -mz / rho;
+  const double eint = (et - 0.5 * (mx * mx + my * my + mz * mz) / rho) / rho;
+  const double p = (c.gamma - 1.0) * rho * eint;
+  const double Tint = p / (c.Rspec * rho);
+  const double x = bn.prob_lo[1] + (double)(j + 0.5) * bn.dx[1];
+  double di, de;
+  if (side == 0) {
+    di = (double)(jf + 0.5) * bn.dx[1] - bn.prob_lo[1];
+    de = bn.prob_lo[1] - x;
+  } else {
+    di = bn.prob_hi[1] - (double)(jf + 0.5) * bn.dx[1];
+    de = x - bn.prob_hi[1];
+  }
+  const double dratio = de / di;
+  const double Te = rmax(bn.Tw + dratio * (bn.Tw - Tint), bn.Tmin);
+  const double re = p / (c.Rspec * Te);
+  const double ekin = 0.5 * (ue * ue + ve * ve + we * we);
+  const double eint_e = p / (re * (c.gamma - 1.0));
+  U(i, j, k, URHO) = re;
+  U(i, j, k, UMX) = re * ue;
+  U(i, j, k, UMY) = re * ve;
+  U(i, j, k, UMZ) = re * we;
+  U(i, j, k, UET) = re * (eint_e + ekin);
+}
+
+// One box that is the domain: every ghost row beyond a code-6 y side, over
+// the whole grown x/z extent (the x/z ghost columns of the first interior
+// row were filled by the library's fill before).
+__global__ void __launch_bounds__(256) bcnormal_box_kernel(DArr U, int lo0, int lo1, int lo2, int hi0, int hi1,
+                                                           int hi2, int wlo, int whi, DClosures c, DBcNormal bn) {
+  const int g = NGHOST;
+  const int nx = hi0 - lo0 + 1 + 2 * g, nz = hi2 - lo2 + 1 + 2 * g;
+  const long long total = (long long)nx * nz * 2 * g;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % nx) + lo0 - g;
+    const long long r = t / nx;
+    const int k = (int)(r % nz) + lo2 - g;
+    const int row = (int)(r / nz);  // 0..g-1 below, g..2g-1 above
+    const int side = row >= g;
+    if (side ? !whi : !wlo) continue;
+    const int gi = side ? row - g + 1 : row + 1;  // ghost distance 1..g
+    const int j = side ? hi1 + gi : lo1 - gi;
+    bcnormal_isothermal_cell(U, i, j, k, side ? hi1 : lo1, side, c, bn);
+  }
+}
+
+// Every box of a level whose y extent touches a code-6 side of the domain:
+// the box's own ghost rows beyond that side (its first interior row and the
+// ghost columns of it were filled by halo_level_kernel).
+__global__ void __launch_bounds__(256) bcnormal_list_kernel(BoxTable tb, int slot, LevelDomain dom, DBcNormal bn) {
+  if (list_idle(tb)) return;
+  const int g = NGHOST;
+  for (int b = blockIdx.y; b < tb.n; b += gridDim.y) {
+    const BoxRec& R = tb.box[b];
+    const bool wlo = dom.bc_lo[1] == 6 && R.lo[1] == dom.lo[1];
+    const bool whi = dom.bc_hi[1] == 6 && R.hi[1] == dom.hi[1];
+    if (!wlo && !whi) continue;
+    const int nx = R.hi[0] - R.lo[0] + 1 + 2 * g, nz = R.hi[2] - R.lo[2] + 1 + 2 * g;
+    const long long total = (long long)nx * nz * 2 * g;
+    const DArr U = R.slot[slot];
+    const DClosures& c = tb.cls[R.cl];
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+      const int i = (int)(t % nx) + R.lo[0] - g;
+      const long long r = t / nx;
+      const int k = (int)(r % nz) + R.lo[2] - g;
+      const int row = (int)(r / nz);
+      const int side = row >= g;
+      if (side ? !whi : !wlo) continue;
+      const int gi = side ? row - g + 1 : row + 1;
+      const int j = side ? R.hi[1] + gi : R.lo[1] - gi;
+      bcnormal_isothermal_cell(U, i, j, k, side ? R.hi[1] : R.lo[1], side, c, bn);
+    }
+  }
+}
+
+cudaError_t launch_bcnormal_box(const DArr& u, const int lo[3], const int hi[3], const int bc_lo[3],
+                                const int bc_hi[3], const DClosures& cl, const DBcNormal& bn, cudaStream_t st) {
+  const int wlo = bc_lo[1] == 6, whi = bc_hi[1] == 6;
+  if (bn.kind != 1 || (!wlo && !whi)) return cudaSuccess;
+  const long long total = (long long)(hi[0] - lo[0] + 7) * (hi[2] - lo[2] + 7) * 2 * NGHOST;
+  long long blocks = (total + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  bcnormal_box_kernel<<<(int)blocks, 256, 0, st>>>(u, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], wlo, whi, cl, bn);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bcnormal_list(const BoxTable& tb, int slot, const LevelDomain& dom, const DBcNormal& bn, int nsm,
+                                 cudaStream_t st) {
+  if (bn.kind != 1 || (dom.bc_lo[1] != 6 && dom.bc_hi[1] != 6)) return cudaSuccess;
+  const int gy = tb.n < nsm * 4 ? tb.n : nsm * 4;
+  dim3 grid(8, (unsigned)(gy < 1 ? 1 : gy));
+  bcnormal_list_kernel<<<grid, 256, 0, st>>>(tb, slot, dom, bn);
+  return cudaGetLastError();
+}
+
 // ----------------------------------------------------------- time step ----
 // cns_estdt (src/cls/CNS_K.h:12-47, z-velocity from UMY as there) reduced
 // with min over cells.  Positive doubles order like their bit patterns, so

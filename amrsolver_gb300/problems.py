@@ -96,6 +96,27 @@ class Scheme:
 
 
 @dataclasses.dataclass
+class BCNormal:
+    """A problem bcnormal the library evaluates on the device beyond code-6
+    y sides (amrs_bcnormal).  kind 1: the channel problem's isothermal
+    no-slip wall (exm/Channel/prob.h:158-186) with wall temperature Tw and
+    the floor Tmin (50 there); prob_lo / prob_hi / dx: the geometry, as
+    cns_bcfill computes the ghost/first-cell distance ratio from them."""
+    Tw: float
+    prob_lo: tuple
+    prob_hi: tuple
+    dx: tuple
+    Tmin: float = 0.0
+    kind: int = 1
+
+    @staticmethod
+    def channel_wall(Tw, n, dx, prob_lo=(0.0, 0.0, 0.0), Tmin=0.0):
+        """Geometry from the cell counts n and sizes dx (prob_hi = prob_lo + n dx)."""
+        hi = tuple(float(prob_lo[d]) + n[d] * float(dx[d]) for d in range(3))
+        return BCNormal(float(Tw), tuple(float(v) for v in prob_lo), hi, tuple(float(v) for v in dx), float(Tmin))
+
+
+@dataclasses.dataclass
 class BoxSpec:
     lo: tuple
     hi: tuple

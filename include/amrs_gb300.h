@@ -201,6 +201,27 @@ amrs_status amrs_rk_stage_box(amrs_handle* h, const amrs_box* bx, const double d
 amrs_status amrs_fill_halo_box(const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3],
                                amrs_array4 state, void* stream);
 
+/* A problem bcnormal the library evaluates on the device, for y sides of
+ * code 6, after its own fill (the order of AMReX's FillPatch: periodic
+ * images and physical BCs first, then cns_bcfill, src/set/bcs.cpp:11-106).
+ * kind 0: none (the caller's bcnormal fills those ghosts).  kind 1: the
+ * channel problem's isothermal no-slip wall (exm/Channel/prob.h:158-186):
+ * from the first interior cell of the ghost's column, the velocity negated,
+ * the pressure kept, T = max(Tw + dratio (Tw - T_int), Tmin) with dratio the
+ * ghost-to-wall over first-cell-to-wall distance computed as cns_bcfill
+ * does from prob_lo, prob_hi and dx (geometry.prob_lo / prob_hi, the
+ * geometry's CellSize; cell centres at prob_lo + (index + 0.5) dx), and
+ * rho = p / (R T).  The channel problem uses Tmin = 50. */
+typedef struct amrs_bcnormal {
+  int32_t kind;
+  double Tw, Tmin;
+  double prob_lo[3], prob_hi[3], dx[3];
+} amrs_bcnormal;
+/* amrs_fill_halo_box, then the bcnormal beyond code-6 y sides. */
+amrs_status amrs_fill_halo_box_bcnormal(const amrs_box* domain, const int32_t bc_lo[3], const int32_t bc_hi[3],
+                                        const amrs_closures* closures, const amrs_bcnormal* bn, amrs_array4 state,
+                                        void* stream);
+
 /* cfl * min over the valid box of dx_d/(|u_d|+c): CNS::estTimeStep
  * (src/CNS.cpp:380-395, kernel cns_estdt src/cls/CNS_K.h:12-47).  Writes the
  * result to *dt_device (device pointer) without a host sync. */
@@ -245,6 +266,11 @@ amrs_status amrs_boxlist_set_bc(amrs_boxlist* bl, const int32_t bc_lo[3], const 
  * Host-synchronising (uploads the owner table). */
 amrs_status amrs_boxlist_set_domain(amrs_boxlist* bl, const amrs_box* domain, const int32_t bc_lo[3],
                                     const int32_t bc_hi[3]);
+/* The level fill of amrs_boxlist_set_domain followed by a device bcnormal
+ * beyond the domain's code-6 y sides (amrs_bcnormal; NULL or kind 0: none),
+ * for every box touching such a side, in every later fill, step graph and
+ * device time loop of the list.  Host-synchronising. */
+amrs_status amrs_boxlist_set_bcnormal(amrs_boxlist* bl, const amrs_bcnormal* bn);
 /* Ghost fill of slot `slot` of every box with the codes of
  * amrs_boxlist_set_bc or the level of amrs_boxlist_set_domain. */
 amrs_status amrs_boxlist_fill_halo(amrs_boxlist* bl, int32_t slot, void* stream);

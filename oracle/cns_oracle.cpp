@@ -1226,6 +1226,59 @@ int orc_fill_halo(const int* lo, const int* hi, const int* bc_lo, const int* bc_
   return 0;
 }
 
+// The channel problem's bcnormal (exm/Channel/prob.h:158-186) as cns_bcfill
+// calls it (src/set/bcs.cpp:40-100) for every ghost cell beyond a code-6 y
+// side, after the fill above: s_int = the column's first interior cell,
+// dratio = de/di from prob_lo, prob_hi and dx, no-slip velocity, the
+// interior pressure, T = max(Tw + dratio (Tw - T_int), Tmin), rho = p/(R T).
+struct OrcBcNormal {
+  int32_t kind;
+  double Tw, Tmin;
+  double prob_lo[3], prob_hi[3], dx[3];
+};
+
+int orc_fill_halo_bcnormal(const int* lo, const int* hi, const int* bc_lo, const int* bc_hi, double* U,
+                           const OrcClosures* c, const OrcBcNormal* bn) {
+  if (int rc = orc_fill_halo(lo, hi, bc_lo, bc_hi, U, NCONS)) return rc;
+  if (!c || !bn) return 1;
+  if (bn->kind != 1) return 0;
+  const Box b = to_box(lo, hi);
+  Arr<double> u = make_arr<double>(U, b, NGHOST);
+  const double gamma = c->gamma, Rs = c->Rspec;
+  for (int side = 0; side < 2; ++side) {
+    if ((side ? bc_hi[1] : bc_lo[1]) != 6) continue;
+    const int jf = side ? hi[1] : lo[1];
+    for (int g = 1; g <= NGHOST; ++g) {
+      const int j = side ? jf + g : jf - g;
+      for (int k = lo[2] - NGHOST; k <= hi[2] + NGHOST; ++k)
+        for (int i = lo[0] - NGHOST; i <= hi[0] + NGHOST; ++i) {
+          const double rho = u(i, jf, k, URHO), mx = u(i, jf, k, UMX), my = u(i, jf, k, UMY);
+          const double mz = u(i, jf, k, UMZ), et = u(i, jf, k, UET);
+          const double ue = -mx / rho, ve = -my / rho, we = -mz / rho;
+          const double eint = (et - 0.5 * (mx * mx + my * my + mz * mz) / rho) / rho;
+          const double p = (gamma - 1.0) * rho * eint;
+          const double Tint = p / (Rs * rho);
+          const double x = bn->prob_lo[1] + (double)(j + 0.5) * bn->dx[1];
+          const double di = side ? bn->prob_hi[1] - (double)(jf + 0.5) * bn->dx[1]
+                                 : (double)(jf + 0.5) * bn->dx[1] - bn->prob_lo[1];
+          const double de = side ? x - bn->prob_hi[1] : bn->prob_lo[1] - x;
+          const double dratio = de / di;
+          const double t = bn->Tw + dratio * (bn->Tw - Tint);
+          const double Te = (t < bn->Tmin) ? bn->Tmin : t;
+          const double re = p / (Rs * Te);
+          const double ekin = 0.5 * (ue * ue + ve * ve + we * we);
+          const double eint_e = p / (re * (gamma - 1.0));
+          u(i, j, k, URHO) = re;
+          u(i, j, k, UMX) = re * ue;
+          u(i, j, k, UMY) = re * ve;
+          u(i, j, k, UMZ) = re * we;
+          u(i, j, k, UET) = re * (eint_e + ekin);
+        }
+    }
+  }
+  return 0;
+}
+
 // cfl * min over the valid box of dx/(|u|+c): CNS::estTimeStep (src/CNS.cpp:380-395).
 double orc_est_timestep(const OrcClosures* c, const int* lo, const int* hi, const double* dx,
                         const double* U, int nghost, double cfl) {

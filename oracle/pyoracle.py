@@ -33,6 +33,11 @@ class CScheme(ctypes.Structure):
                 ("force", ctypes.c_double * 3)]
 
 
+class CBcNormal(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("Tw", ctypes.c_double), ("Tmin", ctypes.c_double),
+                ("prob_lo", ctypes.c_double * 3), ("prob_hi", ctypes.c_double * 3), ("dx", ctypes.c_double * 3)]
+
+
 def c_closures(cl):
     return CClosures(cl.gamma, cl.cv, cl.cp, cl.Rspec, int(cl.visc_law), int(cl.cond_law),
                      cl.visc_ref, cl.Tvisc_ref, cl.cond_ref, cl.Tcond_ref, cl.Cshock, cl.Cdamp)
@@ -97,6 +102,10 @@ class Oracle:
             L.orc_compute_rhs_count.argtypes = [ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ip,
                                                 ip, dp, dp, ctypes.POINTER(ctypes.c_longlong)]
             L.orc_compute_rhs_count.restype = ctypes.c_int
+        if hasattr(L, "orc_fill_halo_bcnormal"):
+            L.orc_fill_halo_bcnormal.argtypes = [ip, ip, ip, ip, dp, ctypes.POINTER(CClosures),
+                                                 ctypes.POINTER(CBcNormal)]
+            L.orc_fill_halo_bcnormal.restype = ctypes.c_int
 
     # -------------------------------------------------------------- calls --
     def rhs(self, scheme, closures, U, dxinv, lo=(0, 0, 0), nthreads=1, walls=None):
@@ -160,6 +169,18 @@ class Oracle:
         if per_phase:
             return per
         return {k: sum(per[ph][k] for ph in self.PHASES) for k in keys}
+
+    def fill_halo_bcnormal(self, U, bc_lo, bc_hi, closures, bn, lo=(0, 0, 0)):
+        """fill_halo, then the channel problem's isothermal bcnormal beyond
+        code-6 y sides; bn: an object with kind, Tw, Tmin, prob_lo, prob_hi, dx."""
+        assert U.flags.c_contiguous
+        nz, ny, nx = (s - 2 * NG for s in U.shape[1:])
+        hi = (lo[0] + nx - 1, lo[1] + ny - 1, lo[2] + nz - 1)
+        cb = CBcNormal(int(bn.kind), float(bn.Tw), float(bn.Tmin), _d3(bn.prob_lo), _d3(bn.prob_hi), _d3(bn.dx))
+        rc = self.lib.orc_fill_halo_bcnormal(_i3(lo), _i3(hi), _i3(bc_lo), _i3(bc_hi), _ptr(U),
+                                             ctypes.byref(c_closures(closures)), ctypes.byref(cb))
+        if rc:
+            raise RuntimeError("orc_fill_halo_bcnormal failed: %d" % rc)
 
     def fill_halo(self, U, bc_lo, bc_hi, lo=(0, 0, 0)):
         """In-place ghost fill of a single-box domain."""

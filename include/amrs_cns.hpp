@@ -171,6 +171,10 @@ class CNS {
   const std::vector<Box>& boxArray() const { return grids_; }
   Real curTime() const { return time_; }
   void setStream(cudaStream_t s) { stream_ = s; }
+  // The problem's bcnormal beyond code-6 y sides evaluated on the device in
+  // every FillPatch of the level (amrs_bcnormal kind 1: the channel
+  // problem's isothermal no-slip wall); nullptr: the ghosts stay the caller's.
+  void setBcNormal(const amrs_bcnormal* bn) { check(amrs_boxlist_set_bcnormal(bl_, bn), "amrs_boxlist_set_bcnormal"); }
 
   // CNS::compute_rhs: S ghost-filled (3 ghosts), dSdt valid-only; the
   // reference's MFIter loop, one amrs_rhs_box per box.

@@ -141,3 +141,35 @@ def test_bad_bcnormal_is_rejected():
     bn = P.BCNormal(Tw=-1.0, prob_lo=(0.0, 0.0, 0.0), prob_hi=(1.0, 1.0, 1.0), dx=(0.125, 0.125, 0.125))
     with pytest.raises(capi.AmrsError):
         capi.fill_halo_box_bcnormal(U, (-1, 6, -1), (-1, 6, -1), CL, bn)
+
+
+def test_device_time_loop_with_walls_bcnormal_and_source():
+    """The channel level's whole run as one launch (conditional-node time
+    loop, fixed dt; the fill with the device bcnormal is a node of its
+    body): equals the same steps taken one by one."""
+    n = (16, 12, 8)
+    U = channel_state(n, CL, seed=31)
+    dx = (2.0 / n[0], 1.0 / n[1], 1.0 / n[2])
+    bc = (-1, 6, -1)
+    Tw = 1.0 / CL.gamma / CL.Rspec
+    bn = P.BCNormal.channel_wall(Tw, n, dx, Tmin=0.5)
+    sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1, rhs_source=1, body_force=(0.8, 0.0, 0.0))
+    los, fields = split(U, [[8], [], []])
+    h = capi.Handle(sc, CL)
+    slots = [[dev(f) for _ in range(3)] for f in fields]
+    blist = capi.BoxList(h, los, slots, [1.0 / v for v in dx])
+    blist.set_domain((0, 0, 0), n, bc, bc)
+    blist.set_bcnormal(bn)
+    blist.run(3, 3, stop_time=1e9, max_steps=6, dt=1.5e-3)
+    t, dt, steps = blist.run_state()
+    h.sync_check()
+    assert steps == 6
+    lev = cns.CNSLevel(sc, CL, U, dx, bc_lo=bc, bc_hi=bc, bcnormal=bn)
+    for _ in range(6):
+        lev.advance(lev.time, 1.5e-3)
+    lev.h.sync_check()
+    one = lev.valid().cpu().numpy()
+    for lo, sl in zip(los, slots):
+        V = sl[0][:, G:-G, G:-G, G:-G].cpu().numpy()
+        x0, y0, z0 = lo
+        np.testing.assert_array_equal(V, one[:, z0:z0 + V.shape[1], y0:y0 + V.shape[2], x0:x0 + V.shape[3]])

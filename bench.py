@@ -21,6 +21,8 @@ Also reported on the same JSON line:
             steps and the adjoint of the final step, with the roofline
             fraction of the whole step; KEEP4 + viscous and the WENO5 ->
             Riemann extension + viscous timed on the same state;
+  channel   the reference's channel configuration (walls, device bcnormal,
+            body force, Sutherland air) as its own 2 x 2 x 1 decomposition;
   cpu_baseline  the CPU oracle on all host cores and on one thread (bounded
                 samples).
 
@@ -691,6 +693,76 @@ def bench_large(torch, capi, P, peak, n=256, steps=20):
     return res
 
 
+def bench_channel(torch, capi, P, steps=10):
+    """The reference's channel configuration: 96 x 128 x 64 cells over
+    0.08214 x 0.0136871 x 0.02738 m, x and z periodic, code-6 y walls
+    (exm/Channel/inputs), air with Sutherland laws, wall temperature 500 K,
+    bulk Mach 1.5, the x body force of the example's parameters
+    (exm/Channel/prob.h ProbParm), KEEP4 + viscous + source, the isothermal
+    no-slip bcnormal on the device; the example's decomposition
+    (max_grid_size 64, blocking factor 16: 2 x 2 x 1 boxes of 48 x 64 x 64),
+    one CUDA graph per SSPRK3 step.  A laminar profile with a seeded
+    perturbation stands in for the example's initial field."""
+    n = (96, 128, 64)
+    ext = (0.08214, 0.0136871, 0.02738)
+    dx = tuple(ext[d] / n[d] for d in range(3))
+    cl = P.Closures.air_sutherland()
+    g = P.NGHOST
+    h_half, Tw, u_tau, re_tau, re_b, mach_b, muw = 0.006845, 500.0, 35.0, 220.0, 3.0e3, 1.5, 2.670533348e-5
+    rho_w = re_tau * muw / (u_tau * h_half)
+    pw = rho_w * cl.Rspec * Tw
+    ub = mach_b * math.sqrt(cl.gamma * cl.Rspec * Tw)
+    rho_b = re_b * muw / (ub * h_half)
+    fx = rho_w * u_tau * u_tau / (h_half * rho_b)
+    rng = np.random.default_rng(2026)
+    shape = (n[2] + 2 * g, n[1] + 2 * g, n[0] + 2 * g)
+    y = (np.arange(-g, n[1] + g) + 0.5) * dx[1]
+    prof = 1.5 * ub * (1.0 - ((y - h_half) / h_half) ** 2)
+    u = prof[None, :, None] * (1.0 + 0.02 * rng.standard_normal(shape))
+    v = 0.01 * ub * rng.standard_normal(shape)
+    w = 0.01 * ub * rng.standard_normal(shape)
+    rho = np.full(shape, pw / (cl.Rspec * Tw))
+    U = P.prims_to_cons(rho, u, v, w, np.full(shape, pw), cl.gamma)
+    sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1, rhs_source=1, body_force=(fx, 0.0, 0.0))
+    h = capi.Handle(sc, cl)
+    los, slots = [], []
+    for y0 in (0, 64):
+        for x0 in (0, 48):
+            B = np.ascontiguousarray(U[:, :, y0:y0 + 64 + 2 * g, x0:x0 + 48 + 2 * g])
+            t = torch.from_numpy(B).cuda()
+            los.append((x0, y0, 0))
+            slots.append([t, t.clone(), t.clone()])
+    bl = capi.BoxList(h, los, slots, [1.0 / v_ for v_ in dx])
+    bl.set_domain((0, 0, 0), n, (-1, 6, -1), (-1, 6, -1))
+    bl.set_bcnormal(P.BCNormal.channel_wall(Tw, n, dx, Tmin=50.0))
+    cmax = math.sqrt(cl.gamma * cl.Rspec * Tw) + 1.5 * ub * 1.1
+    dt = 0.3 * min(dx) / cmax
+    s = [0, 1, 2]
+
+    def step():
+        r = bl.step(3, 3, dt, s[0], s[1], s[2], use_graph=True)
+        others = [q for q in (0, 1, 2) if q != r]
+        s[0], s[1], s[2] = r, others[0], others[1]
+
+    for _ in range(2):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    h.sync_check()
+    ms = e0.elapsed_time(e1) / steps
+    finite = all(bool(torch.isfinite(sl[s[0]]).all()) for sl in slots)
+    cells = n[0] * n[1] * n[2]
+    return {"workload": "channel 96x128x64 (x/z periodic, code-6 y walls with the device isothermal bcnormal), "
+                        "air Sutherland, KEEP4 + viscous + x body force, 2x2x1 boxes of 48x64x64, graph per step",
+            "cells": cells, "dt": dt, "steps": steps, "ms_per_step": ms,
+            "cell_updates_per_s": cells / (ms * 1e-3), "finite": finite}
+
+
 def run_gpu(args, rank, world, local):
     import torch
     from amrsolver_gb300 import capi, cns
@@ -848,6 +920,7 @@ def run_gpu(args, rank, world, local):
                 torch, P, scheme=dict(flux_euler=0, riemann_weno=1, rhs_visc=1), label="WENO5-Riemann + viscous")
             result["level"] = bench_level(torch, capi, P, n=n)
             result["sod_device_loop"] = bench_sod(torch, capi, P)
+            result["channel"] = bench_channel(torch, capi, P)
         if not args.skip_large:
             result["large"] = bench_large(torch, capi, P, peak)
         if not args.skip_cpu:

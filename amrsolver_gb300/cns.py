@@ -28,8 +28,8 @@ class CNSLevel:
         callable `bcnormal(t)` on the ghosted state tensor written with torch
         operations (differentiated by torch autograd in the adjoint), or a
         problems.BCNormal that the library evaluates on the device beyond
-        code-6 y sides (forward only).  Without it those ghost cells keep the
-        values of U0."""
+        code-6 y sides (the adjoint differentiates the same formula written
+        in torch).  Without it those ghost cells keep the values of U0."""
         self.scheme, self.closures = scheme, closures
         self.bcnormal = bcnormal
         self.h = capi.Handle(scheme, closures, device)
@@ -86,13 +86,12 @@ class CNSLevel:
         ghosts are constants and their cotangents are simply not used."""
         if self.bcnormal is None:
             return gbar
-        if not callable(self.bcnormal):
-            raise NotImplementedError("the adjoint needs the bcnormal as a torch function; the device bcnormal "
-                                      "is forward only")
+        fill = self.bcnormal if callable(self.bcnormal) else _isothermal_wall_torch(self.bcnormal, self.closures,
+                                                                                   self.bc_lo, self.bc_hi, self.lo)
         with torch.enable_grad():
             x = t.detach().clone().requires_grad_(True)
             y = x.clone()
-            self.bcnormal(y)
+            fill(y)
             (gx,) = torch.autograd.grad(y, x, grad_outputs=gbar)
         return gx
 
@@ -163,3 +162,44 @@ class CNSLevel:
             if cfl is not None:
                 dt_cur = self.compute_new_dt(cfl, dt_cur, stop_time)
         return steps
+
+
+def _isothermal_wall_torch(bn, cl, bc_lo, bc_hi, lo):
+    """The device bcnormal of kind 1 (the channel problem's isothermal
+    no-slip wall beyond code-6 y sides) as torch operations on the ghosted
+    state, for differentiating it by autograd in the adjoint: the same
+    formula, with the floor max(T, Tmin) passing the derivative along the
+    branch taken."""
+    g = NGHOST
+
+    def fill(t):
+        ny = t.shape[2] - 2 * g
+        for side in (0, 1):
+            if (bc_hi if side else bc_lo)[1] != 6:
+                continue
+            jf = g if side == 0 else g + ny - 1  # tensor row of the first interior cell
+            s = t[:, :, jf, :].clone()
+            rho = s[0]
+            ue, ve, we = -s[1] / rho, -s[2] / rho, -s[3] / rho
+            eint = (s[4] - 0.5 * (s[1] * s[1] + s[2] * s[2] + s[3] * s[3]) / rho) / rho
+            p = (cl.gamma - 1.0) * rho * eint
+            tint = p / (cl.Rspec * rho)
+            jdom = lo[1] if side == 0 else lo[1] + ny - 1  # index of the first interior row
+            for gi in range(1, g + 1):
+                j = jdom - gi if side == 0 else jdom + gi
+                x = bn.prob_lo[1] + (j + 0.5) * bn.dx[1]
+                if side == 0:
+                    dratio = (bn.prob_lo[1] - x) / ((jdom + 0.5) * bn.dx[1] - bn.prob_lo[1])
+                else:
+                    dratio = (x - bn.prob_hi[1]) / (bn.prob_hi[1] - (jdom + 0.5) * bn.dx[1])
+                te = torch.clamp_min(bn.Tw + dratio * (bn.Tw - tint), bn.Tmin)
+                re = p / (cl.Rspec * te)
+                ekin = 0.5 * (ue * ue + ve * ve + we * we)
+                row = jf - gi if side == 0 else jf + gi
+                t[0, :, row, :] = re
+                t[1, :, row, :] = re * ue
+                t[2, :, row, :] = re * ve
+                t[3, :, row, :] = re * we
+                t[4, :, row, :] = re * (p / (re * (cl.gamma - 1.0)) + ekin)
+
+    return fill

@@ -173,3 +173,44 @@ def test_device_time_loop_with_walls_bcnormal_and_source():
         V = sl[0][:, G:-G, G:-G, G:-G].cpu().numpy()
         x0, y0, z0 = lo
         np.testing.assert_array_equal(V, one[:, z0:z0 + V.shape[1], y0:y0 + V.shape[2], x0:x0 + V.shape[3]])
+
+
+def test_step_vjp_through_device_bcnormal_vs_fd():
+    """The adjoint of a walled step whose ghosts the device bcnormal fills:
+    its derivative comes from the same formula in torch (autograd), checked
+    against central differences of whole steps."""
+    from amrsolver_gb300 import adjoint
+    n = (12, 10, 8)
+    U = channel_state(n, CL, seed=13)
+    dx = (1.0 / n[0], 1.0 / n[1], 1.0 / n[2])
+    Tw = 1.0 / CL.gamma / CL.Rspec
+    bn = P.BCNormal.channel_wall(Tw, n, dx, Tmin=0.0)
+    sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1, rhs_source=1, body_force=(0.8, 0.0, 0.0))
+    bc = (-1, 6, -1)
+    lev = cns.CNSLevel(sc, CL, U, dx, bc_lo=bc, bc_hi=bc, bcnormal=bn)
+    dt = 4e-3
+    Uv = dev(P.valid(U).copy())
+    g = dev(np.random.default_rng(5).standard_normal(Uv.shape))
+
+    def ghosted(x):
+        S = torch.zeros(lev.shape, dtype=torch.float64, device="cuda")
+        S[:, G:-G, G:-G, G:-G] = x
+        return S
+
+    stages, _ = adjoint._forward_step(lev, ghosted(Uv), dt)
+    ubar, _ = adjoint._step_vjp(lev, stages, dt, g)
+
+    def f(x):
+        _, out = adjoint._forward_step(lev, ghosted(x), dt)
+        return float(torch.sum(g * out[:, G:-G, G:-G, G:-G]))
+
+    eps = 1e-6
+    for k in range(4):
+        W = np.random.default_rng(50 + k).standard_normal(Uv.shape)
+        for c in range(5):
+            W[c] *= float(Uv[c].abs().mean()) + 1e-3
+        W = dev(W)
+        fd = (f(Uv + eps * W) - f(Uv - eps * W)) / (2 * eps)
+        ad = float(torch.sum(ubar * W))
+        assert abs(fd - ad) <= 1e-6 * abs(ad), (k, fd, ad)
+    lev.h.sync_check()

@@ -66,7 +66,10 @@ int main(int argc, char** argv) {
   const double gamma = 1.4, cv = 1.0 / (gamma - 1.0), cp = gamma / (gamma - 1.0);
   amrs_closures cl{gamma, cv, cp, 1.0, 0, 0, mu, 110.4, cp * mu / 0.71, 194.0, 1.0, 0.01};
   try {
-    amrs::CNS lev(geom, grids, sc, cl, 3, 3, 0);
+    // optional x body force (cns.rhs_source with the channel problem's user_source form)
+    const double fx = argc > 10 ? std::atof(argv[10]) : 0.0;
+    const double bf[3] = {fx, 0.0, 0.0};
+    amrs::CNS lev(geom, grids, sc, cl, 3, 3, 0, fx != 0.0 ? bf : nullptr);
     amrs::MultiFab& S = lev.get_new_data();
     for (int b = 0; b < S.size(); ++b) copy_box(U, n, 3, S.fab(b), 3, true, 3);
     lev.FillPatch(S);

@@ -122,6 +122,8 @@ SIGNATURES = {
     "amrs_boxlist_set_bcnormal": (_S, [_P, ctypes.POINTER(CBcNormal)]),
     "amrs_sync_check": (_S, [_P, _P]),
     "amrs_probe_fp64_tflops": (_S, [_P, ctypes.POINTER(ctypes.c_double)]),
+    "amrs_probe_fp64_tflops_timed": (_S, [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_double)]),
     "amrs_debug_wait_timeout": (_S, [_P, ctypes.c_int32, _P]),
     "amrs_average_down": (_S, [ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_int32), Array4, Array4, ctypes.c_int32,
                                ctypes.c_int32, _P]),
@@ -327,10 +329,17 @@ class Handle:
                                              int(reps), _stream_ptr(stream), ms), "amrs_profile_stage_box")
         return tuple(ms)
 
-    def probe_fp64_tflops(self):
+    def probe_fp64_tflops(self, seconds=None):
+        """Measured FP64 FMA rate (TFLOP/s).  With `seconds`, the timed launch
+        runs about that long and (tflops, launch ms) is returned."""
         v = ctypes.c_double()
-        check(self._L.amrs_probe_fp64_tflops(self.h, ctypes.byref(v)), "amrs_probe_fp64_tflops")
-        return v.value
+        if seconds is None:
+            check(self._L.amrs_probe_fp64_tflops(self.h, ctypes.byref(v)), "amrs_probe_fp64_tflops")
+            return v.value
+        ms = ctypes.c_double()
+        check(self._L.amrs_probe_fp64_tflops_timed(self.h, float(seconds), ctypes.byref(v), ctypes.byref(ms)),
+              "amrs_probe_fp64_tflops_timed")
+        return v.value, ms.value
 
     def debug_wait_timeout(self, polls=4096, stream=None):
         """Run the bounded-wait failure path once (amrs_debug_wait_timeout);

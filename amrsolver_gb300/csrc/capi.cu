@@ -1747,30 +1747,49 @@ amrs_status amrs_debug_wait_timeout(amrs_handle* h, int32_t polls, void* stream)
 }
 
 // Measured FP64 FMA throughput of the handle's device in TFLOP/s (an FMA
-// counts 2 flops): 2 CTAs of 256 threads per SM, eight DFMA chains each,
-// timed with CUDA events after one warm-up launch.  Host-synchronising.
-amrs_status amrs_probe_fp64_tflops(amrs_handle* h, double* tflops) {
+// counts 2 flops): 4 CTAs of 256 threads per SM, sixteen DFMA chains per
+// thread.  A short launch calibrates the loop count so that the timed launch
+// runs for about `seconds` (clamped to [0.01, 10]); it is timed with CUDA
+// events after the calibration launch.  *ms receives its duration (callers
+// sample the SM clock over it).  Host-synchronising.
+amrs_status amrs_probe_fp64_tflops_timed(amrs_handle* h, double seconds, double* tflops, double* ms_out) {
   if (!h || !tflops) return AMRS_ERR_NULL;
+  if (!(seconds >= 0.01 && seconds <= 10.0)) return AMRS_ERR_SIZE;
   CK(cudaSetDevice(h->device));
-  const int blocks = 2 * h->nsm, iters = 8192;
+  const int blocks = 4 * h->nsm, threads = 256, chains = 16;
   double* buf = nullptr;
-  CK(cudaMalloc(&buf, sizeof(double) * blocks * 256));
+  CK(cudaMalloc(&buf, sizeof(double) * blocks * threads));
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  cudaError_t e = launch_fp64_probe(buf, blocks, iters, 0);
-  if (e == cudaSuccess) e = cudaEventRecord(e0, 0);
-  if (e == cudaSuccess) e = launch_fp64_probe(buf, blocks, iters, 0);
-  if (e == cudaSuccess) e = cudaEventRecord(e1, 0);
-  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  auto timed = [&](int iters, float* ms) {
+    cudaError_t e = cudaEventRecord(e0, 0);
+    if (e == cudaSuccess) e = launch_fp64_probe(buf, blocks, iters, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, 0);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+    return e;
+  };
   float ms = 0.f;
-  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  int iters = 4096;
+  cudaError_t e = timed(iters, &ms);  // calibration (also the warm-up)
+  if (e == cudaSuccess && ms > 0.f) {
+    const double want = seconds * 1e3 / ms * iters;
+    iters = (int)std::min(std::max(want, 4096.0), (double)(1 << 30));
+    e = timed(iters, &ms);
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(buf);
-  if (e != cudaSuccess) return cuda_fail(e, "amrs_probe_fp64_tflops");
-  *tflops = 2.0 * 8.0 * (double)blocks * 256.0 * iters / (ms * 1e-3) / 1e12;
+  if (e != cudaSuccess) return cuda_fail(e, "amrs_probe_fp64_tflops_timed");
+  *tflops = 2.0 * chains * (double)blocks * threads * iters / (ms * 1e-3) / 1e12;
+  if (ms_out) *ms_out = ms;
   return AMRS_OK;
+}
+
+// The same probe with a timed launch of about 0.2 s.
+amrs_status amrs_probe_fp64_tflops(amrs_handle* h, double* tflops) {
+  return amrs_probe_fp64_tflops_timed(h, 0.2, tflops, nullptr);
 }
 
 // Per-kernel timing of one RK stage of one box (KEEP fused path): the

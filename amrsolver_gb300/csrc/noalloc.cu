@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 
@@ -116,9 +117,16 @@ extern "C" amrs_status amrs_rhs_box_noalloc(const amrs_scheme* scheme, const amr
                                             amrs_array4 dsdt, void* stream) {
   if (!scheme || !closures || !bx || !dxinv) return AMRS_ERR_NULL;
   const amrs_scheme& sc = *scheme;
-  if (!(sc.rhs_euler && sc.flux_euler == 1 && !sc.art_diss &&
+  // the switches amrs_create accepts, restricted to the fused KEEP path
+  if (!(sc.rhs_euler == 1 && sc.flux_euler == 1 && sc.art_diss == 0 && (sc.weno_fast == 0 || sc.weno_fast == 1) &&
+        (sc.riemann_weno == 0 || sc.riemann_weno == 1) && (sc.rhs_visc == 0 || sc.rhs_visc == 1) &&
         (sc.order_keep == 2 || sc.order_keep == 4 || sc.order_keep == 6)))
     return AMRS_ERR_SCHEME;
+  // transport laws: 0 constant, 1 Sutherland (src/cls/Closures.h:103-166)
+  if ((closures->visc_law != 0 && closures->visc_law != 1) || (closures->cond_law != 0 && closures->cond_law != 1))
+    return AMRS_ERR_SCHEME;
+  for (int d = 0; d < 3; ++d)
+    if (!(dxinv[d] > 0.0) || !std::isfinite(dxinv[d])) return AMRS_ERR_BOX;
   int n[3];
   for (int d = 0; d < 3; ++d) {
     n[d] = bx->hi[d] - bx->lo[d] + 1;
@@ -130,6 +138,13 @@ extern "C" amrs_status amrs_rhs_box_noalloc(const amrs_scheme* scheme, const amr
   std::lock_guard<std::mutex> lk(g_na_mu);
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return AMRS_ERR_CUDA;
+  // the scratch address below belongs to the current device: a stream of
+  // another device would run the kernels against the wrong array
+  if (st) {
+    int sdev = -1;
+    if (cudaStreamGetDevice(st, &sdev) != cudaSuccess) return AMRS_ERR_CUDA;
+    if (sdev != dev) return AMRS_ERR_STATE;
+  }
   double* base = nullptr;
   int nsm = 0;
   if (amrs_status s = na_setup(dev, &base, &nsm)) return s;
@@ -235,7 +250,8 @@ extern "C" amrs_status amrs_rhs_box_noalloc(const amrs_scheme* scheme, const amr
   // pageable host memory it waits for the stream's earlier work and returns
   // once the staging is consumed, so the static host buffer can be reused.
   if (cudaMemcpyAsync(tab, host, t, cudaMemcpyHostToDevice, st) != cudaSuccess) return AMRS_ERR_CUDA;
-  BoxTable tb;
+  BoxTable tb{};  // every field defined: tb.active stays null (no device time loop here)
+  tb.active = nullptr;
   tb.box = reinterpret_cast<const BoxRec*>(tab + o_box);
   tb.pcell = reinterpret_cast<const long long*>(tab + o_p);
   tb.vcell = reinterpret_cast<const long long*>(tab + o_v);
@@ -249,6 +265,9 @@ extern "C" amrs_status amrs_rhs_box_noalloc(const amrs_scheme* scheme, const amr
   tma.maps = nullptr;
   tma.enabled = 0;
   DProg prog{};
+  // The face kernel takes a flag word that only its TMA staging's bounded
+  // waits write; this path stages with plain loads (tma.enabled = 0), so
+  // nothing can raise it and there is nothing to read back.
   int* err = reinterpret_cast<int*>(tab + o_err);
   if (launch_prims(tb, 0, pcell[1], nsm, st) != cudaSuccess) return AMRS_ERR_CUDA;
   if (sc.rhs_visc && launch_visc(tb, vcell[1], nsm, st) != cudaSuccess) return AMRS_ERR_CUDA;

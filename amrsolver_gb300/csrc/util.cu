@@ -518,14 +518,21 @@ cudaError_t launch_totals(const BoxTable& tb, int slot, long long nvalid, double
 // ------------------------------------------------------- FP64 probe ----
 // Eight independent DFMA chains per thread: the FP64 pipe's issue rate, the
 // denominator of this path's roofline (the path is FP64-bound on GB300).
+// FP64 peak probe: sixteen independent DFMA chains per thread (latency
+// hidden many times over at 32 warps per SM), nothing else in the loop body
+// but the chains, so the FP64 pipe is the only unit the loop can saturate.
 __global__ void __launch_bounds__(256) fp64_probe_kernel(double* out, int iters, double s) {
-  double a0 = threadIdx.x * 1e-3 + 1.0, a1 = a0 + 0.1, a2 = a0 + 0.2, a3 = a0 + 0.3, a4 = a0 + 0.4, a5 = a0 + 0.5,
-         a6 = a0 + 0.6, a7 = a0 + 0.7;
+  double a[16];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) a[c] = threadIdx.x * 1e-3 + 1.0 + 0.05 * c;
   for (int it = 0; it < iters; ++it) {
-    a0 = fma(a0, s, 0.5); a1 = fma(a1, s, 0.5); a2 = fma(a2, s, 0.5); a3 = fma(a3, s, 0.5);
-    a4 = fma(a4, s, 0.5); a5 = fma(a5, s, 0.5); a6 = fma(a6, s, 0.5); a7 = fma(a7, s, 0.5);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) a[c] = fma(a[c], s, 0.5);
   }
-  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  double r = 0.0;
+#pragma unroll
+  for (int c = 0; c < 16; ++c) r += a[c];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = r;
 }
 
 cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t st) {

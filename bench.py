@@ -47,7 +47,6 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cell-updates/s per RK3 step"
 UNIT = "cell-updates/s"
-WORKLOAD = "Taylor-Green vortex 128^3 periodic, M=0.1 Re=1600 Pr=0.71, KEEP4 + viscous, SSPRK3"
 
 # --scheme: (switches, op-count key, dominant kernel, its ncu summary, kernels of ours per stage, label)
 SCHEMES = {
@@ -71,6 +70,14 @@ def workload_name(scheme, n):
 
 
 # --------------------------------------------------------------- helpers --
+def headline_config(n, scheme, world, state_bytes):
+    """The `config` of the headline line, identical in both arms."""
+    return {"workload": workload_name(scheme, n), "cells": n ** 3,
+            "l2": "inputs larger than L2 (3 ghosted states + scratch, %.2f GB of states alone)"
+            % (3 * state_bytes / 1e9),
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -222,7 +229,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "l2": "inputs larger than L2"},
+        "config": headline_config(n, "keep4", world, U.nbytes),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": "full 128^3 SSPRK3 steps, OpenMP over k-planes on %d threads" % cores},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -621,7 +628,7 @@ def bench_large(torch, capi, P, peak, n=256, steps=20):
         achieved = flops_step / (ms_fwd * 1e-3) / 1e12
         res["weno_fast" if fast else "weno_reference_order"] = {
             "ms_per_step": ms_fwd, "cell_updates_per_s": n ** 3 / (ms_fwd * 1e-3),
-            "achieved_tflops_algorithmic": achieved, "frac_of_measured_fp64_peak": achieved / peak,
+            "achieved_tflops_algorithmic": achieved, "frac_of_fp64_peak": achieved / peak,
             "forward_step_keeping_stages_ms": f0.elapsed_time(f1), "adjoint_step_ms": f1.elapsed_time(f2),
             "adjoint_over_forward": f1.elapsed_time(f2) / ms_fwd,
             "recomputed_final_step_bit_identical": same,
@@ -660,7 +667,7 @@ def bench_large(torch, capi, P, peak, n=256, steps=20):
     kms = e0.elapsed_time(e1) / ksteps
     kach = kflops / (kms * 1e-3) / 1e12
     res["keep4_visc"] = {"ms_per_step": kms, "cell_updates_per_s": n ** 3 / (kms * 1e-3), "steps": ksteps,
-                         "achieved_tflops_algorithmic": kach, "frac_of_measured_fp64_peak": kach / peak}
+                         "achieved_tflops_algorithmic": kach, "frac_of_fp64_peak": kach / peak}
     del lev
     gc.collect()
     torch.cuda.empty_cache()
@@ -866,7 +873,7 @@ def run_gpu(args, rank, world, local):
             face_flops = weno_face_flops(spec[1], n)
             # reads U (40), point fluxes (120) and lambda (24) per cell, writes 3 x 5 face values
             algo_bytes_face = n ** 3 * (40 + 120 + 24) + 3 * (n + 1) * n * n * 40
-        peak = lev.h.probe_fp64_tflops()
+        peak, peak_info = fp64_peak(torch, lev.h, local)
         S0 = lev.S
         out = torch.empty_like(S0)
         s1 = lev.bufs[(lev.cur + 1) % 3]
@@ -878,9 +885,9 @@ def run_gpu(args, rank, world, local):
         tf = kms[2]
         achieved = face_flops / (tf * 1e-3) / 1e12
         roofline = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                    "traffic": None, "kernel": spec[2],
-                    "peak_source": "measured: DFMA-chain probe kernel (amrs_probe_fp64_tflops), FMA = 2 flops",
+                    "traffic": None, "kernel": spec[2], "peak_source": peak_info,
                     "algorithmic_flops_per_launch": face_flops, "ms_per_launch": tf,
+                    "staging": "tma" if lev.h.tma_enabled() else "plain loads",
                     "stage_kernel_ms": {"prims": kms[0], "visc_cells": kms[1], "faces": kms[2]},
                     "hbm_peak_gbs_measured": None}
         try:
@@ -899,10 +906,7 @@ def run_gpu(args, rank, world, local):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_all, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload_name(args.scheme, n), "cells": n ** 3,
-                       "l2": "inputs larger than L2 (3 ghosted states + scratch, %.2f GB of states alone)"
-                       % (3 * U.nbytes / 1e9), "parallelism": "replicas" if world > 1 else "single GPU",
-                       "tma": lev.h.tma_enabled()},
+            "config": headline_config(n, args.scheme, world, U.nbytes),
             "e2e": {"value": replica_throughput(n ** 3, world, ms_e2e), "unit": UNIT, "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes},
             "roofline": roofline,
@@ -925,7 +929,69 @@ def run_gpu(args, rank, world, local):
             result["large"] = bench_large(torch, capi, P, peak)
         if not args.skip_cpu:
             result["cpu_baseline"] = cpu_baseline_sample()
+        result["summary"] = summary_of(result)
     return result
+
+
+def fp64_peak(torch, h, local, seconds=1.5):
+    """FP64 roofline denominator: the larger of (a) the DFMA-chain probe
+    (amrs_probe_fp64_tflops_timed, one launch of about `seconds`) and (b) the
+    nominal rate of the pipe, SMs x 2 DFMA lanes per clock x 2 flops x the
+    median SM clock sampled over the probe's launch."""
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.2)
+    tf, ms = h.probe_fp64_tflops(seconds=seconds)
+    clk = clocks.stop()
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
+    info = {"probe_tflops": tf, "probe_ms": ms, "sms": nsm, "probe_sm_mhz_median": clk.get("sm_mhz"),
+            "sm_max_mhz": clk.get("sm_max_mhz"), "probe_clock_reasons": clk.get("reasons"),
+            "rule": "max(probe, nominal at the sampled SM clock); FMA = 2 flops"}
+    nominal = None
+    if mhz:
+        nominal = nsm * 2 * 2 * mhz * 1e6 / 1e12
+        info["nominal_tflops_at_sampled_mhz"] = nominal
+        info["probe_frac_of_nominal"] = tf / nominal
+        info["probe_ms_x_mhz"] = ms * mhz
+    if clk.get("sm_max_mhz"):
+        info["nominal_tflops_at_max_mhz"] = nsm * 4 * clk["sm_max_mhz"] * 1e6 / 1e12
+    peak = max(tf, nominal or 0.0)
+    info["chosen"] = "probe" if peak == tf else "nominal at sampled clock"
+    return peak, info
+
+
+def summary_of(result):
+    """A compact digest of the metric's numbers, printed as the line's last
+    key: cell-updates/s batched vs per box, adjoint / forward step time, and
+    the roofline fractions (of the FP64 peak in `roofline.peak`)."""
+    out = {"headline_cell_updates_per_s": result.get("value"), "headline_e2e": result["e2e"]["value"],
+           "face_kernel_frac": result["roofline"]["frac"], "fp64_peak_tflops": result["roofline"]["peak"]}
+    b = result.get("batched")
+    if b:
+        out["batched_graph_cell_updates_per_s"] = b["batched_graph_cell_updates_per_s"]
+        out["per_box_cell_updates_per_s"] = b["per_box_cell_updates_per_s"]
+        out["batched_speedup"] = b["speedup"]
+        if "tuned" in b:
+            out["batched_tuned_over_default"] = b["tuned"].get("tuned_over_default")
+    e = result.get("ensemble")
+    if e:
+        out["ensemble_cell_updates_per_s"] = e["cell_updates_per_s"]
+    a = result.get("adjoint")
+    if a:
+        out["adjoint_over_forward_keep4_tgv64"] = a.get("adjoint_over_forward")
+    c = result.get("adjoint_checkpointed")
+    if c:
+        out["checkpointed_200_steps_adjoint_over_forward"] = c.get("adjoint_over_forward")
+    lg = result.get("large")
+    if lg:
+        for k in ("weno_reference_order", "weno_fast", "keep4_visc"):
+            if k in lg:
+                out["large_256_%s_frac" % k] = lg[k].get("frac_of_fp64_peak")
+                out["large_256_%s_cell_updates_per_s" % k] = lg[k].get("cell_updates_per_s")
+        if "weno_reference_order" in lg:
+            out["large_256_adjoint_over_forward"] = lg["weno_reference_order"].get("adjoint_over_forward")
+    return out
 
 
 def read_traffic(path):

@@ -175,11 +175,14 @@ amrs_status amrs_rhs_box(amrs_handle* h, const amrs_box* bx, const double dxinv[
  * memory pool owns all device memory, or one with a fixed device-memory
  * budget); this variant of the fused KEEP + viscous RHS keeps its scratch in
  * one static device array of the library instead of a handle.  Limits:
- * KEEP without JST only, boxes of at most 32 cells per direction
- * (AMRS_ERR_SIZE beyond); the array (6.9 MB) lives on every device that
- * loads the library until exit; every call shares it, so calls that overlap
- * on the GPU race.  The first call on a device looks the array's address up
- * with that device current: make it before any stream capture.  Results
+ * KEEP 2/4/6 with or without viscous terms, no JST and no source term
+ * (AMRS_ERR_SCHEME otherwise, also for transport laws other than 0/1),
+ * boxes of at most 32 cells per direction (AMRS_ERR_SIZE beyond); the array
+ * (6.9 MB) lives on every device that loads the library until exit; every
+ * call shares it, so calls that overlap on the GPU race.  The kernels run on
+ * the current device: a `stream` of another device is refused
+ * (AMRS_ERR_STATE).  The first call on a device looks the array's address
+ * up with that device current: make it before any stream capture.  Results
  * are identical to amrs_rhs_box. */
 amrs_status amrs_rhs_box_noalloc(const amrs_scheme* scheme, const amrs_closures* closures, const amrs_box* bx,
                                  const double dxinv[3], amrs_array4 state, amrs_array4 dsdt, void* stream);
@@ -383,9 +386,15 @@ amrs_status amrs_average_down(const amrs_box* crse_box, const int32_t ratio[3], 
  * Asynchronous on `stream`. */
 amrs_status amrs_debug_wait_timeout(amrs_handle* h, int32_t polls, void* stream);
 /* FP64 FMA throughput of the device (TFLOP/s, FMA = 2 flops), measured
- * by a DFMA-chain kernel: the roofline denominator of this FP64-bound path.
- * Host-synchronising. */
+ * by a DFMA-chain kernel (4 CTAs x 256 threads per SM, 16 independent
+ * chains per thread) over one launch of about 0.2 s: a measured
+ * denominator of this FP64-bound path's roofline.  Host-synchronising. */
 amrs_status amrs_probe_fp64_tflops(amrs_handle* h, double* tflops);
+/* The same probe with a timed launch of about `seconds` (0.01..10); *ms
+ * (may be NULL) receives the launch's duration, so that a caller sampling
+ * the SM clock over it can relate the rate to the clock.
+ * Host-synchronising. */
+amrs_status amrs_probe_fp64_tflops_timed(amrs_handle* h, double seconds, double* tflops, double* ms);
 /* Per-kernel timing of one RK stage of one box: CUDA events around the
  * kernels on `stream`, averaged over `reps`.  ms[0] primitives (plus the
  * WENO5 point fluxes), ms[1] viscous cell fluxes, ms[2] the Euler face

@@ -1,9 +1,10 @@
 """Build recipe for the CPU oracle library (test infrastructure only).
 
 `build_oracle()` compiles oracle/cns_oracle.cpp with g++ into
-oracle/_build/liboracle.so.  `build_ref()` runs oracle/build_ref.sh, which
-compiles the reference's own kernel sources (when the reference tree is
-present on this machine) into oracle/_ref/libcnsref.so.
+oracle/_build/liboracle.so.  `build_ref(root)` runs oracle/build_ref.sh, which
+compiles the reference's own kernel sources from the reference tree `root`
+(or $AMRS_REFERENCE_ROOT) into oracle/_ref/libcnsref_*.so; with no tree
+named, or none there, it does nothing.
 """
 import os
 import subprocess
@@ -28,14 +29,18 @@ def build_oracle(force=False):
     return LIB
 
 
-def build_ref(refroot="/root/reference"):
-    """Compile the reference sources into oracle/_ref (skipped when absent)."""
-    if not os.path.isdir(os.path.join(refroot, "src", "rhs")):
+def build_ref(refroot=None):
+    """Compile the reference sources of the tree `refroot` (default: the
+    AMRS_REFERENCE_ROOT environment variable) into oracle/_ref; skipped when
+    no tree is named or the named one lacks src/rhs."""
+    refroot = refroot or os.environ.get("AMRS_REFERENCE_ROOT")
+    if not refroot or not os.path.isdir(os.path.join(refroot, "src", "rhs")):
         return None
     subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh"), refroot])
     return REF_LIB
 
 
 if __name__ == "__main__":
+    import sys
     print(build_oracle(force=True))
-    print(build_ref())
+    print(build_ref(sys.argv[1] if len(sys.argv) > 1 else None))

@@ -3,12 +3,12 @@
 # into oracle/_ref/ against the AMReX stand-in in oracle/ref_shim/.
 # Test infrastructure only: the outputs are oracles, never product code.
 #
-#   bash oracle/build_ref.sh [REFERENCE_ROOT]
+#   bash oracle/build_ref.sh REFERENCE_ROOT     (or AMRS_REFERENCE_ROOT set)
 #
 # Two libraries, one per closure family the reference ships
 # (src/cls/Closures.h): constant viscosity/conductivity and Sutherland.
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${AMRS_REFERENCE_ROOT:?usage: build_ref.sh REFERENCE_ROOT (or set AMRS_REFERENCE_ROOT)}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 mkdir -p "$OUT"

@@ -112,7 +112,7 @@ def main():
     build.build_oracle()
     for kind in ("const", "suth"):
         if pyoracle.reference(closures(kind)) is None:
-            raise SystemExit("reference build missing: run bash oracle/build_ref.sh first")
+            raise SystemExit("reference build missing: run bash oracle/build_ref.sh REFERENCE_ROOT first")
     out = {}
     for i, (name, kind, skw, n, lo, dxinv) in enumerate(RHS_CASES):
         cl = closures(kind)

@@ -20,6 +20,12 @@ class AmrsError(RuntimeError):
     pass
 
 
+# Order of the 21 values of amrs_boxlist_prim_stats / amrs_prim_stats_box.
+PRIM_STATS_KEYS = (["min_" + q for q in ("rho", "u", "v", "w", "T", "p")]
+                   + ["max_" + q for q in ("rho", "u", "v", "w", "T", "p")]
+                   + ["%s_%s" % (a, d) for d in "xyz" for a in ("max_u_plus_c", "max_u_minus_c", "cfl")])
+
+
 class Array4(ctypes.Structure):
     _fields_ = [("p", ctypes.c_void_p), ("jstride", ctypes.c_int64), ("kstride", ctypes.c_int64),
                 ("nstride", ctypes.c_int64), ("begin", ctypes.c_int32 * 3), ("end", ctypes.c_int32 * 3),
@@ -106,6 +112,9 @@ SIGNATURES = {
     "amrs_boxlist_run_state": (_S, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                     ctypes.POINTER(ctypes.c_int32), _P]),
     "amrs_boxlist_totals": (_S, [_P, ctypes.c_int32, ctypes.c_double, _P, _P]),
+    "amrs_boxlist_prim_stats": (_S, [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.c_double, _P, _P]),
+    "amrs_prim_stats_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double), Array4, ctypes.c_double,
+                                 _P, _P]),
     "amrs_rhs_vjp_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double), Array4, Array4, Array4,
                               _P, _P]),
     "amrs_fill_halo_box_adjoint": (_S, [ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_int32),
@@ -122,6 +131,7 @@ SIGNATURES = {
     "amrs_boxlist_set_bcnormal": (_S, [_P, ctypes.POINTER(CBcNormal)]),
     "amrs_sync_check": (_S, [_P, _P]),
     "amrs_probe_fp64_tflops": (_S, [_P, ctypes.POINTER(ctypes.c_double)]),
+    "amrs_set_check_nonfinite": (_S, [_P, ctypes.c_int32]),
     "amrs_probe_fp64_tflops_timed": (_S, [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_double)]),
     "amrs_debug_wait_timeout": (_S, [_P, ctypes.c_int32, _P]),
@@ -274,6 +284,16 @@ class Handle:
                                             ctypes.c_void_p(dt_dev.data_ptr()), _stream_ptr(stream)),
               "amrs_est_timestep_box")
 
+    def prim_stats(self, U, dx, dt, out, lo=(0, 0, 0), ng=NGHOST, stream=None):
+        """CNS::printTotal's primitive extrema and CFL table of one box into
+        the cuda tensor `out` (21 doubles; see PRIM_STATS_KEYS)."""
+        nz, ny, nx = (s - 2 * ng for s in U.shape[1:])
+        bx = c_box(lo, (nx, ny, nz))
+        check(self._L.amrs_prim_stats_box(self.h, ctypes.byref(bx), d3(dx), array4(U, lo, ng), float(dt),
+                                          ctypes.c_void_p(out.data_ptr()), _stream_ptr(stream)),
+              "amrs_prim_stats_box")
+        return out
+
     def sync_check(self, stream=None):
         check(self._L.amrs_sync_check(self.h, _stream_ptr(stream)), "amrs_sync_check")
 
@@ -328,6 +348,11 @@ class Handle:
                                              array4(Uin, lo, NGHOST), array4(U1, lo, g1), array4(Uout, lo, go),
                                              int(reps), _stream_ptr(stream), ms), "amrs_profile_stage_box")
         return tuple(ms)
+
+    def set_check_nonfinite(self, on=True):
+        """Opt in (or out) of the non-finite check after every stage and RHS;
+        sync_check then raises AmrsError with AMRS_ERR_NONFINITE."""
+        check(self._L.amrs_set_check_nonfinite(self.h, int(bool(on))), "amrs_set_check_nonfinite")
 
     def probe_fp64_tflops(self, seconds=None):
         """Measured FP64 FMA rate (TFLOP/s).  With `seconds`, the timed launch
@@ -493,6 +518,13 @@ class BoxList:
         check(self._L.amrs_boxlist_run_state(self.bl, ctypes.byref(t), ctypes.byref(d), ctypes.byref(n),
                                              _stream_ptr(stream)), "amrs_boxlist_run_state")
         return t.value, d.value, n.value
+
+    def prim_stats(self, slot, dx, dt, out, stream=None):
+        """Primitive extrema and CFL table over every box (slot -1: the
+        primitives of the last RHS's stage input) into `out` (21 doubles)."""
+        check(self._L.amrs_boxlist_prim_stats(self.bl, int(slot), d3(dx), float(dt), ctypes.c_void_p(out.data_ptr()),
+                                              _stream_ptr(stream)), "amrs_boxlist_prim_stats")
+        return out
 
     def totals(self, slot, scale, out, stream=None):
         """Conserved totals of `slot` times `scale` into the cuda tensor `out` (5 doubles)."""

@@ -149,6 +149,17 @@ class CNSLevel:
         v = self.valid()
         return (v.reshape(NCONS, -1).sum(dim=1) * vol).cpu().numpy()
 
+    def print_total(self, dt):
+        """What CNS::printTotal reports (src/CNS.cpp:532-611): the conserved
+        totals, the min/max of each primitive and the convective CFL table
+        for time step dt, from the current state; a dict keyed as
+        capi.PRIM_STATS_KEYS plus 'totals'."""
+        out = torch.empty(21, dtype=torch.float64, device=self.dev)
+        self.h.prim_stats(self.S, self.dx, dt, out, self.lo)
+        d = dict(zip(capi.PRIM_STATS_KEYS, out.cpu().numpy().tolist()))
+        d["totals"] = self.totals().tolist()
+        return d
+
     def run(self, stop_time, max_step, cfl=None, dt=None):
         """The reference's main loop (src/main.cpp:66-75) for one level."""
         steps = 0

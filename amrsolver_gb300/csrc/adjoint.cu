@@ -28,6 +28,7 @@ struct AdjRec {
   DArr pair[3][3];  // [d][l-1]: NQA comps lo-end (0..5) + hi-end (6..11) over grow(box,3)
   DArr vg;      // viscous cotangents over grow(box,1): centre u,v,w,T (0..3), gradients (4..15)
   int visc;     // vg holds data (the viscous reverse pass ran)
+  double* part; // per-block partial sums of d/d(visc_ref), d/d(cond_ref): 2 per block of adj_visc_kernel
 };
 
 __device__ __forceinline__ double vget(const DArr& v, const BoxRec& R, int i, int j, int k, int n) {
@@ -146,7 +147,11 @@ __global__ void __launch_bounds__(256) adj_pair_kernel(BoxTable tb, AdjRec ar, l
 }
 
 // VJP of the cell viscous fluxes (viscous_cell in amrs_device.cuh) for every
-// cell of grow(box,1); accumulates d/d(visc_ref) and d/d(cond_ref) per block.
+// cell of grow(box,1).  With `pbar`, each block also sums d/d(visc_ref) and
+// d/d(cond_ref) over its cells in a fixed order (grid-stride, then warp
+// shuffles, then the warps in order) into ar.part; adj_param_sum_kernel adds
+// the blocks' sums in block order.  No atomics: the result is the same bits
+// on every run.
 __global__ void __launch_bounds__(256) adj_visc_kernel(BoxTable tb, AdjRec ar, long long total, double* pbar) {
   const BoxRec& R = tb.box[0];
   const DClosures& cl = tb.cls[R.cl];
@@ -234,16 +239,39 @@ __global__ void __launch_bounds__(256) adj_visc_kernel(BoxTable tb, AdjRec ar, l
     for (int n = 0; n < 12; ++n) G.p[og + (4 + n) * G.ns] = gb[n];
   }
   if (pbar) {
+    __shared__ double wsum[2][8];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       mu_acc += __shfl_down_sync(0xffffffffu, mu_acc, off);
       la_acc += __shfl_down_sync(0xffffffffu, la_acc, off);
     }
     if ((threadIdx.x & 31) == 0) {
-      atomicAdd(&pbar[0], mu_acc);
-      atomicAdd(&pbar[1], la_acc);
+      wsum[0][threadIdx.x >> 5] = mu_acc;
+      wsum[1][threadIdx.x >> 5] = la_acc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double m = 0.0, a = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+        m += wsum[0][w];
+        a += wsum[1][w];
+      }
+      ar.part[2 * blockIdx.x] = m;
+      ar.part[2 * blockIdx.x + 1] = a;
     }
   }
+}
+
+// pbar += the per-block sums of adj_visc_kernel, in block order.
+__global__ void adj_param_sum_kernel(const double* part, int nblocks, double* pbar) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double m = 0.0, a = 0.0;
+  for (int b = 0; b < nblocks; ++b) {
+    m += part[2 * b];
+    a += part[2 * b + 1];
+  }
+  pbar[0] += m;
+  pbar[1] += a;
 }
 
 // Qbar gather + cons2prim VJP for every cell of grow(box,3).
@@ -471,6 +499,8 @@ cudaError_t launch_rhs_vjp(int order, const BoxTable& tb, const AdjRecHost& ah, 
     for (int l = 0; l < 3; ++l) ar.pair[d][l] = ah.pair[d][l];
   ar.vg = ah.vg;
   ar.visc = ah.visc;
+  ar.part = ah.part;
+  if (pbar && !ah.part) return cudaErrorInvalidValue;
   const int H = order / 2;
   const long long n0 = ah.n[0], n1 = ah.n[1], n2 = ah.n[2];
   long long npair = 0;
@@ -481,7 +511,11 @@ cudaError_t launch_rhs_vjp(int order, const BoxTable& tb, const AdjRecHost& ah, 
   else if (order == 4) adj_pair_kernel<4><<<grid256(npair, nsm), 256, 0, st>>>(tb, ar, npair);
   else if (order == 6) adj_pair_kernel<6><<<grid256(npair, nsm), 256, 0, st>>>(tb, ar, npair);
   const long long nv = (n0 + 2) * (n1 + 2) * (n2 + 2);
-  if (ah.visc) adj_visc_kernel<<<grid256(nv, nsm), 256, 0, st>>>(tb, ar, nv, pbar);
+  if (ah.visc) {
+    const int nbv = grid256(nv, nsm);  // at most 8 blocks per SM: ah.part holds 2 x 8 x nsm doubles
+    adj_visc_kernel<<<nbv, 256, 0, st>>>(tb, ar, nv, pbar);
+    if (pbar) adj_param_sum_kernel<<<1, 32, 0, st>>>(ah.part, nbv, pbar);
+  }
   const long long ng = (n0 + 6) * (n1 + 6) * (n2 + 6);
   if (order == 0) adj_gather_kernel<0><<<grid256(ng, nsm), 256, 0, st>>>(tb, ar, ng, 0);
   else if (order == 2) adj_gather_kernel<2><<<grid256(ng, nsm), 256, 0, st>>>(tb, ar, ng, H);

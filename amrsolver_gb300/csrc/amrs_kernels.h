@@ -78,6 +78,7 @@ struct AdjRecHost {
   DArr vg;          // 16 comps over grow(box,1)
   int n[3];
   int visc;
+  double* part;     // 2 x 8 x nsm doubles: per-block parameter-cotangent sums (needed when pbar is given)
 };
 // order 0: viscous part and cons2prim reverse only (no KEEP pairs)
 cudaError_t launch_rhs_vjp(int order, const BoxTable& tb, const AdjRecHost& ah, double* pbar, int nsm,
@@ -117,6 +118,13 @@ cudaError_t launch_run_step_done(RunCtl* c, cudaGraphConditionalHandle cond, cud
 cudaError_t launch_run_begin(RunCtl* c, cudaStream_t st);
 cudaError_t launch_copy_slot(const BoxTable& tb, int from, int to, long long nvalid, int nsm, cudaStream_t st);
 int totals_blocks(long long nvalid, int nsm);
+// CNS::printTotal's primitive extrema and CFL table over the valid cells
+// (slot -1: the primitive scratch of the last RHS); out: 21 device doubles
+cudaError_t launch_prim_stats(const BoxTable& tb, const long long* vpre, int slot, double dt, const double dx[3],
+                              long long nvalid, unsigned long long* cells, double* out, int nsm, cudaStream_t st);
+// raises *flag when a valid cell of `slot` holds a NaN or an infinity
+cudaError_t launch_nonfinite_check(const BoxTable& tb, const long long* vpre, int slot, long long nvalid, int* flag,
+                                   int nsm, cudaStream_t st);
 cudaError_t launch_totals(const BoxTable& tb, int slot, long long nvalid, double scale, double* part, double* out,
                           int nsm, cudaStream_t st);
 

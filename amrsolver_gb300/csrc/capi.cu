@@ -301,7 +301,9 @@ struct List {
   size_t d_tot_n = 0;
   double* d_step_dt = nullptr;  // dt the step graph's stage programs read
   double h_step_dt = 0.0;
+  unsigned long long* d_stats = nullptr;  // reduction cells of the printTotal statistics
   ~List() {
+    if (d_stats) cudaFree(d_stats);
     if (d_step_dt) cudaFree(d_step_dt);
     if (run_graph) cudaGraphExecDestroy(run_graph);
     if (d_run) cudaFree(d_run);
@@ -320,7 +322,8 @@ struct amrs_handle {
   int nsm = 0;
   amrs_scheme sc{};
   amrs_closures cl{};
-  int* derr = nullptr;               // device error flag (bounded waits)
+  int* derr = nullptr;               // device flags: [0] bounded waits timed out, [1] non-finite result
+  int check_nonfinite = 0;           // amrs_set_check_nonfinite
   unsigned long long* dred = nullptr;  // reduction cell
   bool tma_ok = true;
   void* encode_fn = nullptr;
@@ -632,6 +635,7 @@ amrs_status list_stage(amrs_handle* h, List& L, const DProg& prog, int s_in, int
     // 3. fused KEEP faces + viscous averages + divergence + stage program
     CK(launch_keep_face(sc.order_keep, sc.rhs_visc != 0, L.source, L.tb, s_in, s_s1, s_out, prog, rhs_only, L.tma,
                         h->derr, L.face_grid, nsm, st));
+    if (h->check_nonfinite) CK(launch_nonfinite_check(L.tb, L.ft.vpre, s_out, L.tot_valid, h->derr + 1, nsm, st));
     return AMRS_OK;
   }
   long long nf[3] = {L.tot_f[0], L.tot_f[1], L.tot_f[2]};
@@ -660,6 +664,7 @@ amrs_status list_stage(amrs_handle* h, List& L, const DProg& prog, int s_in, int
   }
   if (sc.rhs_visc) CK(launch_visc_face_add(L.tb, L.ft, nf, nsm, st));
   CK(launch_div_stage(L.tb, L.ft, s_in, s_s1, s_out, prog, rhs_only, L.tot_valid, nsm, st));
+  if (h->check_nonfinite) CK(launch_nonfinite_check(L.tb, L.ft.vpre, s_out, L.tot_valid, h->derr + 1, nsm, st));
   return AMRS_OK;
 }
 
@@ -959,6 +964,30 @@ amrs_status amrs_est_timestep_box(amrs_handle* h, const amrs_box* bx, const doub
   cudaError_t e = launch_estdt(L.tb, 0, L.tot_valid, cfl, h->dred, dt_device, h->nsm, st);
   ring_release(h, st);
   if (e != cudaSuccess) return cuda_fail(e, "launch_estdt");
+  return AMRS_OK;
+}
+
+amrs_status amrs_prim_stats_box(amrs_handle* h, const amrs_box* bx, const double dx[3], amrs_array4 state, double dt,
+                                double* out, void* stream) {
+  if (!h || !bx || !dx || !out) return AMRS_ERR_NULL;
+  if (!box_ok(*bx)) return AMRS_ERR_BOX;
+  if (!covers(state, *bx, 0, NCONS)) return AMRS_ERR_LAYOUT;
+  double dxinv[3];
+  for (int d = 0; d < 3; ++d) {
+    if (!(dx[d] > 0.0)) return AMRS_ERR_BOX;
+    dxinv[d] = 1.0 / dx[d];
+  }
+  std::lock_guard<std::mutex> lk(h->mu);
+  CK(cudaSetDevice(h->device));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  amrs_array4 slots[3] = {state, state, state};
+  if (amrs_status s = one_box(h, bx, dxinv, slots, 3, st)) return s;
+  List& L = *h->one;
+  cudaError_t e = cudaSuccess;
+  if (!L.d_stats) e = cudaMalloc(&L.d_stats, 32 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = launch_prim_stats(L.tb, L.ft.vpre, 0, dt, dx, L.tot_valid, L.d_stats, out, h->nsm, st);
+  ring_release(h, st);
+  if (e != cudaSuccess) return cuda_fail(e, "amrs_prim_stats_box");
   return AMRS_OK;
 }
 
@@ -1312,7 +1341,7 @@ amrs_status amrs_rk_step_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t sta
   if (!L.d_step_dt) CK(cudaMalloc(&L.d_step_dt, sizeof(double)));
   L.h_step_dt = dt;
   CK(cudaMemcpyAsync(L.d_step_dt, &L.h_step_dt, sizeof(double), cudaMemcpyHostToDevice, st));
-  const int key[6] = {order_rk, stages_rk, s1, w1, w2, 1};
+  const int key[6] = {order_rk, stages_rk, s1, w1, w2, 1 + 2 * bl->h->check_nonfinite};
   if (!L.graph || std::memcmp(key, L.graph_key, sizeof(key)) != 0) {
     if (L.graph) { cudaGraphExecDestroy(L.graph); L.graph = nullptr; }
     cudaStream_t cs;
@@ -1356,7 +1385,7 @@ amrs_status amrs_rk_run_boxlist(amrs_boxlist* bl, int32_t order_rk, int32_t stag
   CK(cudaSetDevice(h->device));
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (!L.d_run) CK(cudaMalloc(&L.d_run, sizeof(RunCtl)));
-  const int key[6] = {order_rk, stages_rk, s1, w1, w2, use_cfl};
+  const int key[6] = {order_rk, stages_rk, s1, w1, w2, use_cfl + 2 * h->check_nonfinite};
   if (!L.run_graph || std::memcmp(key, L.run_key, sizeof(key)) != 0) {
     if (L.run_graph) { CK(cudaStreamSynchronize(st)); cudaGraphExecDestroy(L.run_graph); L.run_graph = nullptr; }
     // outer graph: one conditional WHILE node whose body is one step
@@ -1439,6 +1468,20 @@ amrs_status amrs_boxlist_run_state(amrs_boxlist* bl, double* time, double* dt, i
   return AMRS_OK;
 }
 
+amrs_status amrs_boxlist_prim_stats(amrs_boxlist* bl, int32_t slot, const double dx[3], double dt, double* out,
+                                    void* stream) {
+  if (!bl || !dx || !out) return AMRS_ERR_NULL;
+  List& L = bl->L;
+  if (slot < -1 || slot >= L.nslots) return AMRS_ERR_SIZE;
+  for (int d = 0; d < 3; ++d)
+    if (!(dx[d] > 0.0)) return AMRS_ERR_BOX;
+  CK(cudaSetDevice(bl->h->device));
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!L.d_stats) CK(cudaMalloc(&L.d_stats, 32 * sizeof(unsigned long long)));
+  CK(launch_prim_stats(L.tb, L.ft.vpre, slot, dt, dx, L.tot_valid, L.d_stats, out, bl->h->nsm, st));
+  return AMRS_OK;
+}
+
 amrs_status amrs_boxlist_totals(amrs_boxlist* bl, int32_t slot, double scale, double* totals, void* stream) {
   if (!bl || !totals) return AMRS_ERR_NULL;
   List& L = bl->L;
@@ -1463,7 +1506,7 @@ namespace {
 // (12 comps over grow(box,3)), viscous cotangents (16 comps over
 // grow(box,1)), a valid-cell dSdt cotangent and a ghosted state cotangent.
 struct AdjScratch {
-  AdjRecHost ah;
+  AdjRecHost ah{};
   DArr vbar_tmp, ubar_tmp;
   double* wbuf = nullptr;  // WENO / MUSCL per-face and per-cell cotangent slots
   double* jbuf = nullptr;  // JST per-face and per-cell cotangent slots
@@ -1500,6 +1543,7 @@ amrs_status adj_prepare(amrs_handle* h, const amrs_box& B, AdjScratch& S, cudaSt
                                                          : 0;
   const size_t o_w = off; off = align_up(off + euler_bytes, 256);
   const size_t o_j = off; off = align_up(off + (jst_scheme(h->sc) ? jst_vjp_buffer_bytes(nb) : 0), 256);
+  const size_t o_part = off; off = align_up(off + sizeof(double) * 2 * 8 * (size_t)h->nsm, 256);
   if (off > h->adj_bytes) {
     if (h->adj) { CK(cudaStreamSynchronize(st)); cudaFree(h->adj); h->adj = nullptr; h->adj_bytes = 0; }
     CK(cudaMalloc(&h->adj, off));
@@ -1523,6 +1567,7 @@ amrs_status adj_prepare(amrs_handle* h, const amrs_box& B, AdjScratch& S, cudaSt
   S.ah.visc = h->sc.rhs_visc != 0;
   S.wbuf = reinterpret_cast<double*>(P + o_w);
   S.jbuf = reinterpret_cast<double*>(P + o_j);  // WENO or MUSCL per-face / per-cell slots
+  S.ah.part = reinterpret_cast<double*>(P + o_part);
   if (H > 0) CK(cudaMemsetAsync(P + o_pair, 0, cells(3) * 12 * 8 * 3 * H, st));
   return AMRS_OK;
 }
@@ -1722,18 +1767,32 @@ amrs_status amrs_rk_stage_vjp_box_ghosted(amrs_handle* h, const amrs_box* bx, co
   return AMRS_OK;
 }
 
-// Synchronise `stream`, then report (and clear) the device error flag set by
-// bounded waits.  Host-synchronising.
+// Synchronise `stream`, then report (and clear) one raised device flag: a
+// bounded wait that timed out first, else a non-finite result seen by the
+// opt-in check.  Host-synchronising.
 amrs_status amrs_sync_check(amrs_handle* h, void* stream) {
   if (!h) return AMRS_ERR_NULL;
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
-  int flag = 0;
-  CK(cudaMemcpy(&flag, h->derr, sizeof(int), cudaMemcpyDeviceToHost));
-  if (flag) {
+  int flag[2] = {0, 0};
+  CK(cudaMemcpy(flag, h->derr, sizeof(flag), cudaMemcpyDeviceToHost));
+  if (flag[0]) {
     CK(cudaMemset(h->derr, 0, sizeof(int)));
     return AMRS_ERR_TIMEOUT;
   }
+  if (flag[1]) {
+    CK(cudaMemset(h->derr + 1, 0, sizeof(int)));
+    return AMRS_ERR_NONFINITE;
+  }
+  return AMRS_OK;
+}
+
+// Opt-in detection of non-finite results (see the header).
+amrs_status amrs_set_check_nonfinite(amrs_handle* h, int32_t on) {
+  if (!h) return AMRS_ERR_NULL;
+  if (on != 0 && on != 1) return AMRS_ERR_SIZE;
+  std::lock_guard<std::mutex> lk(h->mu);
+  h->check_nonfinite = on;
   return AMRS_OK;
 }
 

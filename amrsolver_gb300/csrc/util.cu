@@ -429,6 +429,156 @@ __global__ void __launch_bounds__(256) copy_slot_kernel(BoxTable tb, int from, i
   }
 }
 
+// Non-finite check of slot `slot` over the valid cells of every box: raises
+// *flag when any component is a NaN or an infinity (exponent bits all ones,
+// tested on the integer bits, so the FP64 pipe is not used).  One extra
+// read of the slot (40 B per cell); run only when the caller opted in.
+__global__ void __launch_bounds__(256) nonfinite_check_kernel(BoxTable tb, const long long* vpre, int slot,
+                                                              long long total, int* flag) {
+  if (list_idle(tb)) return;
+  int bad = 0;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    const int b = find_box_ll(vpre, tb.n, g);
+    const BoxRec& R = tb.box[b];
+    const int nx = R.hi[0] - R.lo[0] + 1, ny = R.hi[1] - R.lo[1] + 1;
+    const long long l = g - vpre[b];
+    const int i = (int)(l % nx) + R.lo[0];
+    const long long t = l / nx;
+    const int j = (int)(t % ny) + R.lo[1], k = (int)(t / ny) + R.lo[2];
+    const DArr A = R.slot[slot];
+    const long long o = A.off(i, j, k);
+#pragma unroll
+    for (int n = 0; n < NCONS; ++n) {
+      const unsigned long long bits = (unsigned long long)__double_as_longlong(A.p[o + n * A.ns]);
+      bad |= (bits & 0x7ff0000000000000ull) == 0x7ff0000000000000ull;
+    }
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+cudaError_t launch_nonfinite_check(const BoxTable& tb, const long long* vpre, int slot, long long nvalid, int* flag,
+                                   int nsm, cudaStream_t st) {
+  long long blocks = (nvalid + 255) / 256;
+  if (blocks > (long long)nsm * 4) blocks = (long long)nsm * 4;
+  if (blocks < 1) blocks = 1;
+  nonfinite_check_kernel<<<(int)blocks, 256, 0, st>>>(tb, vpre, slot, nvalid, flag);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------- printTotal stats ----
+// CNS::printTotal's primitive extrema and convective CFL table
+// (src/CNS.cpp:532-611; pointCFL, src/cls/CNS_K.h:49-59) over the valid
+// cells of every box.  Extrema do not depend on the order they are taken
+// in, so each warp reduces with shuffles and lane 0 folds its values into
+// order-preserving integer encodings with atomicMin/atomicMax: race-free,
+// and the same bits on every run.  The CFL entry of direction d is
+// max(|u_d + c|, |u_d - c|) * dt / dx_d per cell, maximised: rounding is
+// monotonic, so this equals the reference's max(A0, A1) * dt / dx_d of the
+// global maxima A0, A1.
+__device__ __forceinline__ unsigned long long ord_enc(double x) {
+  if (x == 0.0) x = 0.0;  // -0 counts as +0
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double ord_dec(unsigned long long e) {
+  const unsigned long long b = (e >> 63) ? (e & 0x7fffffffffffffffull) : ~e;
+  return __longlong_as_double((long long)b);
+}
+
+constexpr int NSTAT = 21;  // min[6], max[6], table[3][3]
+
+__global__ void prim_stats_init(unsigned long long* cells) {
+  const int t = threadIdx.x;
+  if (t < NSTAT) cells[t] = t < 6 ? ~0ull : 0ull;
+}
+
+__global__ void __launch_bounds__(256) prim_stats_kernel(BoxTable tb, const long long* vpre, int slot, double dt,
+                                                         double dx0, double dx1, double dx2, long long total,
+                                                         unsigned long long* cells) {
+  double mn[6], mx[6], t[9];
+#pragma unroll
+  for (int n = 0; n < 6; ++n) { mn[n] = __longlong_as_double(0x7ff0000000000000ll); mx[n] = -mn[n]; }
+#pragma unroll
+  for (int n = 0; n < 9; ++n) t[n] = 0.0;
+  const double dxs[3] = {dx0, dx1, dx2};
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    const int b = find_box_ll(vpre, tb.n, g);
+    const BoxRec& R = tb.box[b];
+    const DClosures& cl = tb.cls[R.cl];
+    const int nx = R.hi[0] - R.lo[0] + 1, ny = R.hi[1] - R.lo[1] + 1;
+    const long long l = g - vpre[b];
+    const int i = (int)(l % nx) + R.lo[0];
+    const long long tt = l / nx;
+    const int j = (int)(tt % ny) + R.lo[1], k = (int)(tt / ny) + R.lo[2];
+    double q[NQ];
+    if (slot >= 0) {
+      const DArr A = R.slot[slot];
+      const long long o = A.off(i, j, k);
+      double u[NCONS];
+#pragma unroll
+      for (int n = 0; n < NCONS; ++n) u[n] = A.p[o + n * A.ns];
+      cons2prim(u, q, cl);
+    } else {
+      const DArr Q = R.q;
+      const long long o = Q.off(i, j, k);
+#pragma unroll
+      for (int n = 0; n < 6; ++n) q[n] = Q.p[o + n * Q.ns];
+    }
+#pragma unroll
+    for (int n = 0; n < 6; ++n) {
+      mn[n] = fmin(mn[n], q[n]);
+      mx[n] = fmax(mx[n], q[n]);
+    }
+    const double sos = sqrt(cl.gamma * cl.Rspec * q[QT]);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double a0 = fabs(q[QU + d] + sos), a1 = fabs(q[QU + d] - sos);
+      t[3 * d] = fmax(t[3 * d], a0);
+      t[3 * d + 1] = fmax(t[3 * d + 1], a1);
+      t[3 * d + 2] = fmax(t[3 * d + 2], fmax(a0, a1) * dt / dxs[d]);
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int n = 0; n < 6; ++n) {
+      mn[n] = fmin(mn[n], __shfl_down_sync(0xffffffffu, mn[n], off));
+      mx[n] = fmax(mx[n], __shfl_down_sync(0xffffffffu, mx[n], off));
+    }
+#pragma unroll
+    for (int n = 0; n < 9; ++n) t[n] = fmax(t[n], __shfl_down_sync(0xffffffffu, t[n], off));
+  }
+  if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+    for (int n = 0; n < 6; ++n) {
+      if (mn[n] <= mx[n]) {  // this warp saw a cell
+        atomicMin(&cells[n], ord_enc(mn[n]));
+        atomicMax(&cells[6 + n], ord_enc(mx[n]));
+      }
+    }
+#pragma unroll
+    for (int n = 0; n < 9; ++n) atomicMax(&cells[12 + n], ord_enc(t[n]));
+  }
+}
+
+__global__ void prim_stats_final(const unsigned long long* cells, double* out) {
+  const int t = threadIdx.x;
+  if (t < NSTAT) out[t] = ord_dec(cells[t]);
+}
+
+cudaError_t launch_prim_stats(const BoxTable& tb, const long long* vpre, int slot, double dt, const double dx[3],
+                              long long nvalid, unsigned long long* cells, double* out, int nsm, cudaStream_t st) {
+  prim_stats_init<<<1, 32, 0, st>>>(cells);
+  long long blocks = (nvalid + 255) / 256;
+  if (blocks > (long long)nsm * 4) blocks = (long long)nsm * 4;
+  if (blocks < 1) blocks = 1;
+  prim_stats_kernel<<<(int)blocks, 256, 0, st>>>(tb, vpre, slot, dt, dx[0], dx[1], dx[2], nvalid, cells);
+  prim_stats_final<<<1, 32, 0, st>>>(cells, out);
+  return cudaGetLastError();
+}
+
 // Conserved totals of slot `slot` over the valid cells of every box:
 // per-block sums in a fixed order, then one block sums the partials in
 // block order (deterministic; not the serial sum's rounding).

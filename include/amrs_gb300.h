@@ -230,6 +230,10 @@ amrs_status amrs_fill_halo_box_bcnormal(const amrs_box* domain, const int32_t bc
  * result to *dt_device (device pointer) without a host sync. */
 amrs_status amrs_est_timestep_box(amrs_handle* h, const amrs_box* bx, const double dx[3], double cfl,
                                   amrs_array4 state, double* dt_device, void* stream);
+/* amrs_boxlist_prim_stats for one box's state (valid cells of `state`, the
+ * same 21 doubles into `out`, device memory).  Asynchronous on `stream`. */
+amrs_status amrs_prim_stats_box(amrs_handle* h, const amrs_box* bx, const double dx[3], amrs_array4 state, double dt,
+                                double* out, void* stream);
 
 /* ---- box lists: one persistent launch over many boxes ---------------- */
 
@@ -316,6 +320,22 @@ amrs_status amrs_boxlist_run_state(amrs_boxlist* bl, double* time, double* dt, i
  * there) into totals[0..4] (device memory), one reduction on the device in
  * a fixed order (deterministic; not the rounding of a serial sum). */
 amrs_status amrs_boxlist_totals(amrs_boxlist* bl, int32_t slot, double scale, double* totals, void* stream);
+/* The rest of CNS::printTotal (src/CNS.cpp:543-611): the min and max of each
+ * primitive and the convective CFL table of pointCFL (src/cls/CNS_K.h:49-59)
+ * over the valid cells of every box.  slot >= 0: primitives of that state
+ * slot (cons2prim as compute_rhs forms them); slot = -1: the list's primitive
+ * scratch, i.e. the primitives of the stage input the list's last RHS read,
+ * which is what the reference's Vprimsmf holds when printTotal reads it.
+ * out (device memory, 21 doubles): min[6] and max[6] of (rho, u, v, w, T, p),
+ * then for d = x, y, z: max |u_d + c|, max |u_d - c| and CFL_d = (the larger
+ * of the two) * dt / dx_d, with c = sqrt(gamma Rspec T) from each box's
+ * closures.  The reference accumulates its table in one shared array from
+ * every GPU thread without synchronisation; here warps reduce and fold into
+ * order-preserving integer cells with atomic min/max: extrema are exact, so
+ * the result is the same on every run (-0.0 counts as +0.0).  Asynchronous on
+ * `stream`. */
+amrs_status amrs_boxlist_prim_stats(amrs_boxlist* bl, int32_t slot, const double dx[3], double dt, double* out,
+                                    void* stream);
 
 /* ---- adjoint ----------------------------------------------------------- */
 
@@ -364,10 +384,20 @@ amrs_status amrs_rk_stage_vjp_box_ghosted(amrs_handle* h, const amrs_box* bx, co
 
 /* ---- diagnostics ---------------------------------------------------- */
 
-/* Synchronise `stream`, then report and clear the device error flag that a
- * bounded device-side wait raises when it gives up (AMRS_ERR_TIMEOUT).
+/* Synchronise `stream`, then report and clear one raised device flag: the
+ * flag a bounded device-side wait raises when it gives up (AMRS_ERR_TIMEOUT)
+ * first, else the flag of the non-finite check (AMRS_ERR_NONFINITE).
  * Host-synchronising. */
 amrs_status amrs_sync_check(amrs_handle* h, void* stream);
+/* Opt-in detection of non-finite results (no counterpart in the reference,
+ * whose runs carry NaNs on silently).  With on = 1, every RK stage and RHS
+ * the handle runs (per-box calls, box-list steps and graphs, the device time
+ * loop) ends with a check of the values it wrote over the valid cells; a
+ * NaN or an infinity raises a device flag that the next amrs_sync_check
+ * reports as AMRS_ERR_NONFINITE.  Costs one read of the written state per
+ * stage; off (0) by default.  Box-list graphs recorded before the switch
+ * changed are re-recorded on their next launch. */
+amrs_status amrs_set_check_nonfinite(amrs_handle* h, int32_t on);
 /* amrex::average_down for cell-centred data on a Cartesian grid, the call
  * CNS::avgDown makes after a fine level's step (src/CNS.cpp:513-530): every
  * cell of `crse_box` (coarse index space) becomes the mean of its

@@ -1285,6 +1285,50 @@ double orc_est_timestep(const OrcClosures* c, const int* lo, const int* hi, cons
   return cns_estdt(to_box(lo, hi), U, dx, to_cl(c), nghost) * cfl;
 }
 
+// CNS::printTotal's primitive extrema and convective CFL table
+// (src/CNS.cpp:532-611) of one ghosted box: cons2prim over the valid cells,
+// min/max of each primitive (rho, u, v, w, T, p), and pointCFL
+// (src/cls/CNS_K.h:49-59) cell by cell in k, j, i order from a zeroed table:
+// row d = (max |u_d + c|, max |u_d - c|, CFL_d), c = sqrt(gamma Rspec T),
+// CFL_d = max(row d's first two) * dt / dx_d.  out: min[6], max[6], table[9].
+int orc_prim_stats(const OrcClosures* c, const int* lo, const int* hi, const double* dx, const double* U,
+                   double dt, double* out) {
+  if (!c || !lo || !hi || !dx || !U || !out) return 1;
+  const Box b = to_box(lo, hi);
+  const Closures cl = to_cl(c);
+  Arr<double> u = make_arr<double>(const_cast<double*>(U), b, NGHOST);
+  std::vector<double> qv((size_t)b.cells() * NPRIM);
+  Arr<double> q = make_arr<double>(qv.data(), b, 0);
+  for (int k = b.lo[2]; k <= b.hi[2]; ++k)
+    for (int j = b.lo[1]; j <= b.hi[1]; ++j)
+      for (int i = b.lo[0]; i <= b.hi[0]; ++i) cons2prim(i, j, k, u, q, cl);
+  for (int n = 0; n < NPRIM; ++n) {
+    double mn = q(b.lo[0], b.lo[1], b.lo[2], n), mx = mn;
+    for (int k = b.lo[2]; k <= b.hi[2]; ++k)
+      for (int j = b.lo[1]; j <= b.hi[1]; ++j)
+        for (int i = b.lo[0]; i <= b.hi[0]; ++i) {
+          mn = rmin(mn, q(i, j, k, n));
+          mx = rmax(mx, q(i, j, k, n));
+        }
+    out[n] = mn;
+    out[NPRIM + n] = mx;
+  }
+  double t[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int k = b.lo[2]; k <= b.hi[2]; ++k)
+    for (int j = b.lo[1]; j <= b.hi[1]; ++j)
+      for (int i = b.lo[0]; i <= b.hi[0]; ++i) {
+        const double sos = std::sqrt(cl.gamma * cl.Rspec * q(i, j, k, QT));
+        for (int d = 0; d < 3; ++d) {
+          t[d][0] = rmax(t[d][0], std::fabs(q(i, j, k, QU + d) + sos));
+          t[d][1] = rmax(t[d][1], std::fabs(q(i, j, k, QU + d) - sos));
+          t[d][2] = rmax(t[d][0], t[d][1]) * dt / dx[d];
+        }
+      }
+  for (int d = 0; d < 3; ++d)
+    for (int e = 0; e < 3; ++e) out[2 * NPRIM + 3 * d + e] = t[d][e];
+  return 0;
+}
+
 // Number of stages of an RK variant, or -1 if the reference rejects it.
 int orc_rk_nstages(int order_rk, int stages_rk) {
   StageProg st[8];

@@ -102,6 +102,9 @@ class Oracle:
             L.orc_compute_rhs_count.argtypes = [ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ip,
                                                 ip, dp, dp, ctypes.POINTER(ctypes.c_longlong)]
             L.orc_compute_rhs_count.restype = ctypes.c_int
+        if hasattr(L, "orc_prim_stats"):
+            L.orc_prim_stats.argtypes = [ctypes.POINTER(CClosures), ip, ip, dp, dp, ctypes.c_double, dp]
+            L.orc_prim_stats.restype = ctypes.c_int
         if hasattr(L, "orc_fill_halo_bcnormal"):
             L.orc_fill_halo_bcnormal.argtypes = [ip, ip, ip, ip, dp, ctypes.POINTER(CClosures),
                                                  ctypes.POINTER(CBcNormal)]
@@ -181,6 +184,20 @@ class Oracle:
                                              ctypes.byref(c_closures(closures)), ctypes.byref(cb))
         if rc:
             raise RuntimeError("orc_fill_halo_bcnormal failed: %d" % rc)
+
+    def prim_stats(self, closures, U, dx, dt, lo=(0, 0, 0)):
+        """CNS::printTotal's primitive min/max and pointCFL table of one
+        ghosted box: 21 values, min[6], max[6] of (rho, u, v, w, T, p), then per
+        direction max|u+c|, max|u-c|, CFL."""
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        nz, ny, nx = (s - 2 * NG for s in U.shape[1:])
+        hi = (lo[0] + nx - 1, lo[1] + ny - 1, lo[2] + nz - 1)
+        out = np.empty(21)
+        rc = self.lib.orc_prim_stats(ctypes.byref(c_closures(closures)), _i3(lo), _i3(hi), _d3(dx), _ptr(U),
+                                     float(dt), _ptr(out))
+        if rc:
+            raise RuntimeError("orc_prim_stats failed: %d" % rc)
+        return out
 
     def fill_halo(self, U, bc_lo, bc_hi, lo=(0, 0, 0)):
         """In-place ghost fill of a single-box domain."""

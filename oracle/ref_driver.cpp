@@ -10,6 +10,7 @@
 // compiling that file, which needs the full AMReX AmrLevel machinery.
 #include <CNS.h>
 #include <CNS_K.h>
+#include <CNS_hydro_K.h>
 
 #include <cstdint>
 #include <cstring>
@@ -317,6 +318,47 @@ int orc_advance(const OrcScheme* s, const OrcClosures* c, const int* lo, const i
   lev.state[0].old_time = 0.0;
   lev.advance(0.0, dt, 1, 1);
   copy_valid_out(*lev.state[0].new_data, S2, NGHOST);
+  return 0;
+}
+
+// CNS::printTotal's primitive extrema and convective CFL table
+// (src/CNS.cpp:532-611) of one ghosted box: the reference's own cons2prim
+// (src/rhs/CNS_hydro_K.h:15-34) over the valid cells, the min and max of each
+// primitive, and the reference's own pointCFL (src/cls/CNS_K.h:49-59) applied
+// cell by cell in one thread (k, j, i order) to a zero-initialised table, as
+// the CPU build runs it.  out: min[6], max[6] (rho, u, v, w, T, p), then row d
+// of the table: max |u_d + c|, max |u_d - c|, CFL_d.
+int orc_prim_stats(const OrcClosures* c, const int* lo, const int* hi, const double* dx, const double* U, double dt,
+                   double* out) {
+  if (int rc = set_closures(c)) return rc;
+  Box bx(IntVect(lo[0], lo[1], lo[2]), IntVect(hi[0], hi[1], hi[2]));
+  Box gb = grow(bx, NGHOST);
+  Array4<const Real> u(const_cast<double*>(U), {gb.lo[0], gb.lo[1], gb.lo[2]},
+                       {gb.hi[0] + 1, gb.hi[1] + 1, gb.hi[2] + 1}, NCONS);
+  FArrayBox qf(bx, NPRIM);
+  Array4<Real> q = qf.array();
+  for (int k = bx.lo[2]; k <= bx.hi[2]; ++k)
+    for (int j = bx.lo[1]; j <= bx.hi[1]; ++j)
+      for (int i = bx.lo[0]; i <= bx.hi[0]; ++i) cons2prim(i, j, k, u, q, g_cl);
+  for (int n = 0; n < NPRIM; ++n) {
+    Real mn = q(bx.lo[0], bx.lo[1], bx.lo[2], n), mx = mn;
+    for (int k = bx.lo[2]; k <= bx.hi[2]; ++k)
+      for (int j = bx.lo[1]; j <= bx.hi[1]; ++j)
+        for (int i = bx.lo[0]; i <= bx.hi[0]; ++i) {
+          mn = amrex::min(mn, q(i, j, k, n));
+          mx = amrex::max(mx, q(i, j, k, n));
+        }
+    out[n] = mn;
+    out[NPRIM + n] = mx;
+  }
+  Array2D<Real, 0, 2, 0, 2> arr{};
+  GpuArray<Real, AMREX_SPACEDIM> dxa = {{dx[0], dx[1], dx[2]}};
+  Array4<const Real> qc = q;
+  for (int k = bx.lo[2]; k <= bx.hi[2]; ++k)
+    for (int j = bx.lo[1]; j <= bx.hi[1]; ++j)
+      for (int i = bx.lo[0]; i <= bx.hi[0]; ++i) pointCFL(i, j, k, arr, qc, g_cl, dxa, dt);
+  for (int d = 0; d < 3; ++d)
+    for (int e = 0; e < 3; ++e) out[2 * NPRIM + 3 * d + e] = arr(d, e);
   return 0;
 }
 

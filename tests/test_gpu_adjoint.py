@@ -230,3 +230,24 @@ def test_checkpointed_gradient_vs_fd_tgv64_200_steps():
     lev.h.sync_check()
     assert abs(g_v0 - fd_v0) <= 1e-6 * abs(fd_v0), (g_v0, fd_v0)
     assert abs(g_mu - fd_mu) <= 1e-6 * abs(fd_mu), (g_mu, fd_mu)
+
+
+def test_parameter_gradient_bitwise_repeatable():
+    """d KE / d(mu, k) is reduced in a fixed order (per-block sums, then the
+    blocks in order, no atomics): two runs give the same bits, and the
+    state cotangent too."""
+    n, nsteps, dt, every = 24, 6, 1e-2, 3
+    sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1)
+    U, dx = P.tgv(n, mach=0.1, amp=1.0)
+    cl = P.Closures.nondimensional(1.0 / 400.0)
+    outs = []
+    for _ in range(3):
+        lev = cns.CNSLevel(sc, cl, U, dx)
+        adj = adjoint.CheckpointedAdjoint(lev, every=every)
+        ubar0, pbar, _ = adj.run(dev(P.valid(U).copy()), nsteps, dt, adjoint.kinetic_energy_grad)
+        lev.h.sync_check()
+        outs.append((ubar0.cpu().numpy(), pbar.cpu().numpy()))
+    assert np.all(outs[0][1] != 0.0)
+    for u, p in outs[1:]:
+        np.testing.assert_array_equal(p, outs[0][1])
+        np.testing.assert_array_equal(u, outs[0][0])

@@ -89,3 +89,19 @@ def test_advance_with_source_bitexact(orc):
     a = orc.advance(sc, CL, U, dxinv, (-1, -1, -1), (-1, -1, -1), 3e-3, 3, 3)
     b = REF.advance(sc, CL, U, dxinv, (-1, -1, -1), (-1, -1, -1), 3e-3, 3, 3)
     np.testing.assert_array_equal(P.valid(a), P.valid(b))
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_prim_stats_bitexact(orc, seed):
+    """CNS::printTotal's primitive extrema and the reference's own pointCFL
+    table (src/cls/CNS_K.h:49-59) against the restatement."""
+    rng = np.random.default_rng(seed)
+    n = tuple(int(v) for v in rng.integers(3, 9, 3))
+    U = P.random_state(n, seed=seed + 50, amp=0.3)
+    lo = tuple(int(v) for v in rng.integers(-5, 5, 3))
+    dx = tuple(float(v) for v in rng.uniform(0.1, 0.5, 3))
+    dt = float(rng.uniform(1e-3, 1e-2))
+    a = orc.prim_stats(CL, U, dx, dt, lo=lo)
+    b = REF.prim_stats(CL, U, dx, dt, lo=lo)
+    np.testing.assert_array_equal(a, b)
+    assert np.all(a[:6] <= a[6:12]) and np.all(a[12:] > 0)

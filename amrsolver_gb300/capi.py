@@ -112,6 +112,9 @@ SIGNATURES = {
     "amrs_boxlist_run_state": (_S, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                     ctypes.POINTER(ctypes.c_int32), _P]),
     "amrs_boxlist_totals": (_S, [_P, ctypes.c_int32, ctypes.c_double, _P, _P]),
+    "amrs_boxlist_set_schedule": (_S, [_P, ctypes.c_int32]),
+    "amrs_boxlist_face_grid": (ctypes.c_int32, [_P]),
+    "amrs_boxlist_get_tiles": (_S, [_P, _P]),
     "amrs_boxlist_prim_stats": (_S, [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.c_double, _P, _P]),
     "amrs_prim_stats_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double), Array4, ctypes.c_double,
                                  _P, _P]),
@@ -468,6 +471,19 @@ class BoxList:
         """tiles: per box (tx, ty, kchunk)."""
         flat = (ctypes.c_int32 * (3 * self.n))(*[int(v) for t in tiles for v in t])
         check(self._L.amrs_boxlist_set_tiles(self.bl, flat), "amrs_boxlist_set_tiles")
+
+    def set_schedule(self, waves):
+        """Shares of the face-kernel schedule per resident CTA (1..8)."""
+        check(self._L.amrs_boxlist_set_schedule(self.bl, int(waves)), "amrs_boxlist_set_schedule")
+
+    def face_grid(self):
+        return int(self._L.amrs_boxlist_face_grid(self.bl))
+
+    def get_tiles(self):
+        """Current per-box (tx, ty, kchunk)."""
+        flat = (ctypes.c_int32 * (3 * self.n))()
+        check(self._L.amrs_boxlist_get_tiles(self.bl, flat), "amrs_boxlist_get_tiles")
+        return [tuple(flat[3 * b:3 * b + 3]) for b in range(self.n)]
 
     def set_bc(self, bc_lo, bc_hi):
         if bc_lo is None:

@@ -279,6 +279,7 @@ struct List {
   long long tot_p = 0, tot_v = 0, tot_g = 0, tot_valid = 0, tot_f[3] = {0, 0, 0}, tot_s[3] = {0, 0, 0};
   int tot_work = 0;
   int face_grid = 0;  // CTAs of the balanced face-kernel schedule
+  int waves = 1;      // shares of the schedule per resident CTA (amrs_boxlist_set_schedule)
   cudaGraphExec_t graph = nullptr;
   int graph_key[6] = {0, 0, 0, 0, 0, 0};
   double graph_dt = 0.0;
@@ -508,7 +509,7 @@ amrs_status list_build(amrs_handle* h, List& L, int n, const amrs_box* boxes, co
         colplanes += bn(boxes[b], 2);
       }
     }
-    const long long G = std::min<long long>((long long)keep_ctas_per_sm(order) * h->nsm, colplanes);
+    const long long G = std::min<long long>((long long)L.waves * keep_ctas_per_sm(order) * h->nsm, colplanes);
     const double per = total / (double)G;
     int cta = 0;
     double acc = 0.0;
@@ -1057,7 +1058,9 @@ amrs_status relist_with_tiles(amrs_boxlist* bl, const std::vector<int>& tiles) {
     o.Cshock = d.Cshock; o.Cdamp = d.Cdamp;
   }
   std::vector<amrs_box> boxes = L.boxes;
+  // recorded graphs hold the old tables' addresses
   if (L.graph) { cudaGraphExecDestroy(L.graph); L.graph = nullptr; }
+  if (L.run_graph) { cudaGraphExecDestroy(L.run_graph); L.run_graph = nullptr; }
   return list_build(bl->h, L, L.n, boxes.data(), dxinv.data(), L.nslots, states.data(), cidx.data(),
                     (int)cls.size(), cls.data(), tiles.data());
 }
@@ -1195,6 +1198,36 @@ amrs_status amrs_boxlist_set_tiles(amrs_boxlist* bl, const int32_t* tiles) {
   CK(cudaSetDevice(bl->h->device));
   CK(cudaDeviceSynchronize());
   return relist_with_tiles(bl, t);
+}
+
+amrs_status amrs_boxlist_set_schedule(amrs_boxlist* bl, int32_t waves) {
+  if (!bl) return AMRS_ERR_NULL;
+  if (waves < 1 || waves > 8) return AMRS_ERR_SIZE;
+  List& L = bl->L;
+  std::lock_guard<std::mutex> lk(bl->h->mu);
+  CK(cudaSetDevice(bl->h->device));
+  CK(cudaDeviceSynchronize());
+  L.waves = waves;
+  std::vector<int> t(3 * L.n);
+  for (int b = 0; b < L.n; ++b) {
+    t[3 * b] = L.hbox[b].tx;
+    t[3 * b + 1] = L.hbox[b].ty;
+    t[3 * b + 2] = L.hbox[b].kc;
+  }
+  return relist_with_tiles(bl, t);
+}
+
+int32_t amrs_boxlist_face_grid(amrs_boxlist* bl) { return bl ? bl->L.face_grid : -1; }
+
+amrs_status amrs_boxlist_get_tiles(amrs_boxlist* bl, int32_t* tiles) {
+  if (!bl || !tiles) return AMRS_ERR_NULL;
+  const List& L = bl->L;
+  for (int b = 0; b < L.n; ++b) {
+    tiles[3 * b] = L.hbox[b].tx;
+    tiles[3 * b + 1] = L.hbox[b].ty;
+    tiles[3 * b + 2] = L.hbox[b].kc;
+  }
+  return AMRS_OK;
 }
 
 amrs_status amrs_boxlist_set_bc(amrs_boxlist* bl, const int32_t bc_lo[3], const int32_t bc_hi[3]) {

@@ -275,7 +275,8 @@ def cpu_baseline_sample():
 def bench_batched(torch, capi, P, nboxes=512, steps=3, warmup=2):
     """Config: 512 uneven boxes (edges {8..64}), one SSPRK3 step; persistent
     box-list launches in a CUDA graph vs per-box launches (one box list of
-    one box each)."""
+    one box each); then the autotuner on the batched list."""
+    from amrsolver_gb300 import autotune
     specs, fields, dx = P.batched_boxes(nboxes)
     cl = P.Closures.nondimensional(1.0 / 1600.0)
     sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1)
@@ -315,11 +316,17 @@ def bench_batched(torch, capi, P, nboxes=512, steps=3, warmup=2):
     ms_p = e0.elapsed_time(e1) / steps
     for s in singles:
         s.close()
+    res = {"workload": "512 uneven boxes, edges from {8,16,24,32,48,64}, KEEP4 + viscous, one SSPRK3 step",
+           "cells": cells, "batched_graph_cell_updates_per_s": cells / (ms_b * 1e-3),
+           "per_box_cell_updates_per_s": cells / (ms_p * 1e-3), "ms_batched": ms_b, "ms_per_box": ms_p,
+           "speedup": ms_p / ms_b}
+    # autotuner sweep over tile shapes per box class and the schedule's
+    # z coarsening, timed on this list's own graph step
+    rep = autotune.tune_level(bl, [tuple(s.shape) for s in specs], dt=1e-4, use_cache=False)
+    res["tuned"] = tuned_section(rep, cells)
+    res["tuned_speedup_over_per_box"] = ms_p / rep["tuned_ms"]
     bl.close()
-    return {"workload": "512 uneven boxes, edges from {8,16,24,32,48,64}, KEEP4 + viscous, one SSPRK3 step",
-            "cells": cells, "batched_graph_cell_updates_per_s": cells / (ms_b * 1e-3),
-            "per_box_cell_updates_per_s": cells / (ms_p * 1e-3), "ms_batched": ms_b, "ms_per_box": ms_p,
-            "speedup": ms_p / ms_b}
+    return res
 
 
 def bench_ensemble(torch, capi, P, nmembers=64, n=48, steps=3, warmup=2):
@@ -483,7 +490,9 @@ def bench_level(torch, capi, P, n=128, box=32, steps=10, warmup=3):
     """TGV n^3 as the reference runs it: a level of (n/box)^3 boxes of box^3
     cells whose ghosts come from their neighbours (single-level FillPatch
     across the level, periodic images included), one CUDA graph per SSPRK3
-    step; the same number of cell updates as the single-box headline."""
+    step; the same number of cell updates as the single-box headline.  Then
+    the autotuner on this level."""
+    from amrsolver_gb300 import autotune
     U, dx = P.tgv(n)
     cl = P.Closures.nondimensional(1.0 / 1600.0)
     h = capi.Handle(P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1), cl)
@@ -513,9 +522,24 @@ def bench_level(torch, capi, P, n=128, box=32, steps=10, warmup=3):
     torch.cuda.synchronize()
     h.sync_check()
     ms = e0.elapsed_time(e1) / steps
-    return {"workload": "TGV %d^3 as %d boxes of %d^3, ghosts from neighbours (level FillPatch in the graph), "
-                        "KEEP4 + viscous, one SSPRK3 step" % (n, m ** 3, box),
-            "ms_per_step": ms, "cell_updates_per_s": n ** 3 / (ms * 1e-3), "result_slot": r}
+    res = {"workload": "TGV %d^3 as %d boxes of %d^3, ghosts from neighbours (level FillPatch in the graph), "
+                       "KEEP4 + viscous, one SSPRK3 step" % (n, m ** 3, box),
+           "ms_per_step": ms, "cell_updates_per_s": n ** 3 / (ms * 1e-3), "result_slot": r}
+    res["tuned"] = tuned_section(autotune.tune_level(bl, [(box, box, box)] * m ** 3, dt=dt, use_cache=False),
+                                 n ** 3)
+    bl.close()
+    return res
+
+
+def tuned_section(rep, cells):
+    """The autotuner's report in the JSON line: default vs tuned step time
+    (each best of three graph launches, timed back to back at the end of the
+    sweep), the choice and the sweep size."""
+    return {"default_ms_per_step": rep["default_ms"], "tuned_ms_per_step": rep["tuned_ms"],
+            "tuned_over_default": rep["tuned_over_default"],
+            "tuned_cell_updates_per_s": cells / (rep["tuned_ms"] * 1e-3), "waves": rep["waves"],
+            "class_tiles": rep["class_tiles"], "candidates_timed": rep["candidates_timed"],
+            "sweep": [[e["candidate"], e["waves"], round(e["ms"], 4)] for e in rep["sweep"]]}
 
 
 def bench_sod(torch, capi, P):
@@ -974,6 +998,9 @@ def summary_of(result):
         out["batched_speedup"] = b["speedup"]
         if "tuned" in b:
             out["batched_tuned_over_default"] = b["tuned"].get("tuned_over_default")
+    lv = result.get("level")
+    if lv and "tuned" in lv:
+        out["level_64x32cubed_tuned_over_default"] = lv["tuned"]["tuned_over_default"]
     e = result.get("ensemble")
     if e:
         out["ensemble_cell_updates_per_s"] = e["cell_updates_per_s"]

@@ -285,6 +285,18 @@ amrs_status amrs_boxlist_fill_halo(amrs_boxlist* bl, int32_t slot, void* stream)
 /* Per-box tiles in one call: tiles[3*b + {0,1,2}] = (tx, ty, kchunk) of
  * box b (the autotuner's output). */
 amrs_status amrs_boxlist_set_tiles(amrs_boxlist* bl, const int32_t* tiles);
+/* Work distribution of the fused face kernel (no counterpart in the
+ * reference, whose MFIter loop launches box by box): the (tile column x
+ * plane) work of all boxes is cut into `waves` x (resident CTAs) equal shares
+ * (1 <= waves <= 8; default 1).  One wave gives each CTA the longest z run
+ * (the fewest z prologues); more waves give shorter runs that later CTAs
+ * pick up as earlier ones finish.  The autotuner sweeps it with the tile
+ * shapes.  Host-synchronising; recorded graphs of the list are re-recorded. */
+amrs_status amrs_boxlist_set_schedule(amrs_boxlist* bl, int32_t waves);
+/* CTAs of the list's face-kernel schedule (0 for the face-array path). */
+int32_t amrs_boxlist_face_grid(amrs_boxlist* bl);
+/* The list's current per-box tiles, in the layout of amrs_boxlist_set_tiles. */
+amrs_status amrs_boxlist_get_tiles(amrs_boxlist* bl, int32_t* tiles);
 
 /* RK stage over all boxes: stage input slot `in`, old state slot `s1`,
  * output slot `out` (valid cells).  One launch per kernel kind. */

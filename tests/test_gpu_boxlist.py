@@ -116,3 +116,27 @@ def test_tile_shapes_do_not_change_bits(orc):
     for o in outs[1:]:
         for a, b in zip(outs[0], o):
             np.testing.assert_array_equal(a[:, 3:-3, 3:-3, 3:-3], b[:, 3:-3, 3:-3, 3:-3])
+
+
+def test_schedule_waves_do_not_change_bits():
+    """The schedule's z coarsening (amrs_boxlist_set_schedule) only moves
+    work between CTAs: every setting gives the same bits."""
+    specs, fields, dx = P.batched_boxes(nboxes=5, seed=4, edges=(16, 24, 40))
+    cl = P.Closures.nondimensional(1.0 / 1000.0)
+    sc = P.Scheme(flux_euler=1, order_keep=4, rhs_visc=1)
+    dxinv = [1.0 / v for v in dx]
+    h = capi.Handle(sc, cl)
+    outs, grids = [], []
+    for waves in (1, 2, 3, 8):
+        slots = [[torch.from_numpy(U).cuda() for _ in range(3)] for U in fields]
+        bl = capi.BoxList(h, [s.lo for s in specs], slots, dxinv)
+        bl.set_schedule(waves)
+        grids.append(bl.face_grid())
+        res = bl.step(3, 3, 1e-3, use_graph=True)
+        h.sync_check()
+        outs.append([slots[b][res].cpu().numpy() for b in range(len(specs))])
+        bl.close()
+    assert grids[0] < grids[1] < grids[2] <= grids[3]
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            np.testing.assert_array_equal(a[:, 3:-3, 3:-3, 3:-3], b[:, 3:-3, 3:-3, 3:-3])

@@ -88,7 +88,7 @@ class _Timer:
         return best
 
 
-def tune_level(bl, shapes, s1=0, w1=1, w2=2, dt=1e-4, reps=3, max_classes=4, min_gain=0.01,
+def tune_level(bl, shapes, s1=0, w1=1, w2=2, dt=1e-4, reps=3, max_classes=4, min_gain=0.005,
                cache_path=DEFAULT_CACHE, use_cache=True):
     """Tune tiles per (nx, ny) class and the schedule's waves of box list `bl`
     whose boxes have valid extents `shapes` ((nx, ny, nz) per box), apply the

@@ -8,6 +8,7 @@ no CPU fallback: without the compiled library or a GPU, calls fail.
 from __future__ import annotations
 
 import ctypes
+import weakref
 import os
 
 from . import build as _build
@@ -236,6 +237,9 @@ class Handle:
         sc, cl = c_scheme(scheme), c_closures(closures)
         check(L.amrs_create(ctypes.byref(h), ctypes.byref(sc), ctypes.byref(cl), int(device)), "amrs_create")
         self.h = h
+        # box lists created on this handle: closed before it (a list must not
+        # outlive its handle, whatever order a garbage collection finds them in)
+        self._lists = weakref.WeakSet()
         if int(getattr(scheme, "rhs_source", 0)):
             self.set_source(getattr(scheme, "body_force", (0.0, 0.0, 0.0)))
 
@@ -245,6 +249,8 @@ class Handle:
 
     def close(self):
         if self.h:
+            for bl in list(self._lists):
+                bl.close()
             self._L.amrs_destroy(self.h)
             self.h = None
 
@@ -425,6 +431,7 @@ class BoxList:
         L = load()
         self._L = L
         self.handle = handle
+        self.bl = None
         n = len(los)
         self.n = n
         self.nslots = len(slots[0])
@@ -452,6 +459,7 @@ class BoxList:
         check(L.amrs_boxlist_create(handle.h, n, boxes, dx, self.nslots, arr, ci, ncl, cls, ctypes.byref(bl)),
               "amrs_boxlist_create")
         self.bl = bl
+        handle._lists.add(self)
 
     def close(self):
         if self.bl:

@@ -344,6 +344,7 @@ struct amrs_handle {
 
 struct amrs_boxlist {
   amrs_handle* h;
+  int device = 0;  // the handle's device, kept so that destroying the list never reads the handle
   List L;
 };
 
@@ -1010,6 +1011,7 @@ amrs_status amrs_boxlist_create(amrs_handle* h, int32_t nboxes, const amrs_box* 
   amrs_boxlist* bl = new (std::nothrow) amrs_boxlist();
   if (!bl) return AMRS_ERR_ALLOC;
   bl->h = h;
+  bl->device = h->device;
   amrs_status s = list_build(h, bl->L, nboxes, boxes, dxinv3, nslots, states, closure_index,
                              closure_index ? nclosures : 0, closures, nullptr);
   if (s) { delete bl; return s; }
@@ -1019,9 +1021,10 @@ amrs_status amrs_boxlist_create(amrs_handle* h, int32_t nboxes, const amrs_box* 
 
 amrs_status amrs_boxlist_destroy(amrs_boxlist* bl) {
   if (!bl) return AMRS_ERR_NULL;
-  cudaSetDevice(bl->h->device);
-  cudaDeviceSynchronize();
+  cudaError_t e = cudaSetDevice(bl->device);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
   delete bl;
+  if (e != cudaSuccess) return cuda_fail(e, "amrs_boxlist_destroy");
   return AMRS_OK;
 }
 

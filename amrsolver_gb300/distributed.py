@@ -297,6 +297,12 @@ class DistributedLevel:
         """Valid cells of local box b (global index) in the current slot."""
         return self.slots[self.lidx[b]][self.cur][:, G:-G, G:-G, G:-G]
 
+    def close(self):
+        """Release the backend's library objects (box list before handle)."""
+        close = getattr(self.backend, "close", None)
+        if close:
+            close()
+
 
 class LibraryBackend:
     """Stages of the local boxes through the library: one box list of the
@@ -309,11 +315,18 @@ class LibraryBackend:
         if dev.type != "cuda":
             raise RuntimeError("the library backend needs the rank's CUDA device")
         self.h = capi.Handle(lev.scheme, lev.closures, dev.index or 0)
-        self.lev = lev
-        los = [lev.boxes[b][0] for b in lev.local]
-        self.bl = capi.BoxList(self.h, los, lev.slots, [1.0 / v for v in lev.dx]) if lev.local else None
+        # what the dt reduction reads, not the level itself (no reference cycle)
+        self.slots, self.dx = lev.slots, lev.dx
+        self.los = [lev.boxes[b][0] for b in lev.local]
+        self.bl = capi.BoxList(self.h, self.los, lev.slots, [1.0 / v for v in lev.dx]) if lev.local else None
         self.reduce_device = dev
         self._dt = torch.empty(1, dtype=torch.float64, device=dev)
+
+    def close(self):
+        if self.bl is not None:
+            self.bl.close()
+            self.bl = None
+        self.h.close()
 
     def stage(self, prog, s_in, s1, s_out):
         if self.bl is not None:
@@ -321,8 +334,7 @@ class LibraryBackend:
 
     def local_dt(self, cfl, slot):
         best = float("inf")
-        for i, b in enumerate(self.lev.local):
-            U = self.lev.slots[i][slot]
-            self.h.est_timestep(U, self.lev.dx, cfl, self._dt, lo=self.lev.boxes[b][0])
+        for i, lo in enumerate(self.los):
+            self.h.est_timestep(self.slots[i][slot], self.dx, cfl, self._dt, lo=lo)
             best = min(best, float(self._dt.item()))
         return best

@@ -241,7 +241,9 @@ amrs_status amrs_prim_stats_box(amrs_handle* h, const amrs_box* bx, const double
  * states[b*nslots + s] is slot s of box b (all ghosted with 3 cells);
  * out[b] receives dSdt in amrs_rhs_boxlist.  The scratch arena grows to the
  * list's needs at creation.  Optional per-box closure index (ensembles):
- * closure_index[b] selects closures[closure_index[b]]. */
+ * closure_index[b] selects closures[closure_index[b]].  The list uses its
+ * handle until it is destroyed: destroy every list before its handle
+ * (amrs_boxlist_destroy itself reads nothing from the handle). */
 typedef struct amrs_boxlist amrs_boxlist;
 amrs_status amrs_boxlist_create(amrs_handle* h, int32_t nboxes, const amrs_box* boxes, const double* dxinv3,
                                 int32_t nslots, const amrs_array4* states, const int32_t* closure_index,

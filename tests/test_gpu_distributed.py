@@ -44,3 +44,4 @@ def test_sharded_level_one_rank_matches_oracle(orc, case):
     for b, (lo, n) in enumerate(boxes):
         ref = S[:, G + lo[2]:G + lo[2] + n[2], G + lo[1]:G + lo[1] + n[1], G + lo[0]:G + lo[0] + n[0]]
         np.testing.assert_array_equal(lev.valid(b).cpu().numpy(), ref)
+    lev.close()

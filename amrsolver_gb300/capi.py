@@ -136,6 +136,8 @@ SIGNATURES = {
     "amrs_sync_check": (_S, [_P, _P]),
     "amrs_probe_fp64_tflops": (_S, [_P, ctypes.POINTER(ctypes.c_double)]),
     "amrs_set_check_nonfinite": (_S, [_P, ctypes.c_int32]),
+    "amrs_debug_ddiv_check": (_S, [_P, ctypes.c_uint64, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64),
+                                   ctypes.POINTER(ctypes.c_double)]),
     "amrs_probe_fp64_tflops_timed": (_S, [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_double)]),
     "amrs_debug_wait_timeout": (_S, [_P, ctypes.c_int32, _P]),
@@ -357,6 +359,15 @@ class Handle:
                                              array4(Uin, lo, NGHOST), array4(U1, lo, g1), array4(Uout, lo, go),
                                              int(reps), _stream_ptr(stream), ms), "amrs_profile_stage_box")
         return tuple(ms)
+
+    def ddiv_check(self, seed, count):
+        """(mismatches, first mismatch (a, b, hardware, library)) of the
+        integer-pipe division against the hardware one on the device."""
+        nb = ctypes.c_int64()
+        first = (ctypes.c_double * 4)()
+        check(self._L.amrs_debug_ddiv_check(self.h, int(seed), int(count), ctypes.byref(nb), first),
+              "amrs_debug_ddiv_check")
+        return nb.value, tuple(first)
 
     def set_check_nonfinite(self, on=True):
         """Opt in (or out) of the non-finite check after every stage and RHS;

@@ -1882,6 +1882,28 @@ amrs_status amrs_probe_fp64_tflops_timed(amrs_handle* h, double seconds, double*
   return AMRS_OK;
 }
 
+// The integer-pipe division against the hardware one (see the header).
+amrs_status amrs_debug_ddiv_check(amrs_handle* h, uint64_t seed, int64_t count, int64_t* mismatches, double* first) {
+  if (!h || !mismatches || !first) return AMRS_ERR_NULL;
+  if (count < 1 || count > (1ll << 40)) return AMRS_ERR_SIZE;
+  CK(cudaSetDevice(h->device));
+  unsigned long long* bad = nullptr;
+  double* dfirst = nullptr;
+  CK(cudaMalloc(&bad, sizeof(unsigned long long)));
+  cudaError_t e = cudaMalloc(&dfirst, 4 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemset(bad, 0, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(dfirst, 0, 4 * sizeof(double));
+  if (e == cudaSuccess) e = launch_ddiv_check(seed, count, bad, dfirst, h->nsm, 0);
+  unsigned long long nb = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&nb, bad, sizeof(nb), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(first, dfirst, 4 * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(bad);
+  if (dfirst) cudaFree(dfirst);
+  if (e != cudaSuccess) return cuda_fail(e, "amrs_debug_ddiv_check");
+  *mismatches = (int64_t)nb;
+  return AMRS_OK;
+}
+
 // The same probe with a timed launch of about 0.2 s.
 amrs_status amrs_probe_fp64_tflops(amrs_handle* h, double* tflops) {
   return amrs_probe_fp64_tflops_timed(h, 0.2, tflops, nullptr);

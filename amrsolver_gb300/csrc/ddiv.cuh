@@ -1,0 +1,144 @@
+// Correctly rounded FP64 division a / b (IEEE round to nearest, ties to
+// even) computed on the integer pipe.
+//
+// Why: on this GPU the FP64 pipe issues 2 lanes per clock per SM and every
+// kernel of the path is bound by it; a hardware-style FP64 division
+// (reciprocal seed plus Newton steps in DFMA) costs several FP64 issue slots.
+// The same correctly rounded quotient can be formed from the operands' bits
+// with 32/64-bit integer multiplies, which run on a unit with far more lanes
+// and overlap with the FP64 work of other warps.  The quotient is the same
+// number (IEEE division is correctly rounded, so any correct method gives the
+// same bits): kernels that must match the reference bit for bit may use it.
+//
+// Method (long division by a fixed-point reciprocal with Newton-Raphson
+// refinement and an exact remainder correction, as in integer division by
+// invariant divisors, Granlund & Montgomery 1994, Moller & Granlund 2011):
+//   significands ma, mb in [2^52, 2^53); d = mb * 2^11 in [2^63, 2^64)
+//   y0  ~ 2^127 / d from a correctly rounded FP32 reciprocal of d's top 24
+//       bits (relative error < 2^-22)
+//   y  <- y + y (2^127 - d y) / 2^127, twice (error squares each time; the
+//       truncations leave |y - 2^127/d| <= 4 units, relative < 2^-61)
+//   Q~ = floor((ma * 2^11) y / 2^74), within 1 of Q = floor(ma 2^53 / mb)
+//   R  = ma 2^53 - Q~ mb (exact in 64 bits since |R| < 2^54), one
+//       correction step each way gives Q and 0 <= R < mb
+//   Q in [2^53, 2^54): 54 quotient bits, the last one is the rounding bit and
+//       R != 0 the sticky bit; Q in [2^52, 2^53): 53 bits, rounding decided
+//       by comparing 2R with mb.
+// Domain: both operands normal and finite, and a result exponent that is
+// normal with room for a rounding carry; anything else (zeros, subnormals,
+// infinities, NaNs, results that overflow or underflow) takes the
+// hardware division, so the function equals a / b for every input.
+#pragma once
+#include <stdint.h>
+
+#ifdef __CUDACC__
+#define AMRS_HD __host__ __device__ __forceinline__
+#else
+#include <string.h>
+#define AMRS_HD inline
+#endif
+
+namespace amrs {
+
+AMRS_HD uint64_t ddiv_mulhi(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+AMRS_HD uint64_t ddiv_bits(double x) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t u;
+  memcpy(&u, &x, 8);
+  return u;
+#endif
+}
+
+AMRS_HD double ddiv_from_bits(uint64_t u) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)u);
+#else
+  double x;
+  memcpy(&x, &u, 8);
+  return x;
+#endif
+}
+
+// Correctly rounded reciprocal of a float holding an integer in [2^23, 2^24),
+// returned as its bits.
+AMRS_HD uint32_t ddiv_rcp_bits(uint32_t dt) {
+#ifdef __CUDA_ARCH__
+  const float f = __uint_as_float(0x4B000000u | (dt & 0x7FFFFFu));  // == dt exactly
+  return __float_as_uint(__frcp_rn(f));
+#else
+  float f, r;
+  const uint32_t fb = 0x4B000000u | (dt & 0x7FFFFFu);
+  memcpy(&f, &fb, 4);
+  r = 1.0f / f;
+  uint32_t rb;
+  memcpy(&rb, &r, 4);
+  return rb;
+#endif
+}
+
+// One Newton-Raphson step of y ~ 2^127 / d (d in [2^63, 2^64)).
+AMRS_HD uint64_t ddiv_newton(uint64_t d, uint64_t y) {
+  const uint64_t plo = d * y, phi = ddiv_mulhi(d, y);
+  // e = 2^127 - d y as (ehi * 2^64 + elo), elo dropped: |ehi| < 2^43 here
+  const int64_t ehi = (int64_t)((1ull << 63) - phi - (plo != 0 ? 1ull : 0ull));
+  const uint64_t m = ehi < 0 ? (uint64_t)(-ehi) : (uint64_t)ehi;
+  const uint64_t lo = y * m, hi = ddiv_mulhi(y, m);
+  const uint64_t corr = (hi << 1) | (lo >> 63);  // y |e| / 2^127
+  if (ehi < 0) return y - corr;
+  const uint64_t s = y + corr;
+  return s < y ? ~0ull : s;  // 2^127 / d <= 2^64: clamp a carry
+}
+
+// a / b, correctly rounded; the integer path where its domain holds.
+AMRS_HD double ddiv_rn(double a, double b) {
+  const uint64_t ua = ddiv_bits(a), ub = ddiv_bits(b);
+  const int ea = (int)((ua >> 52) & 0x7FF), eb = (int)((ub >> 52) & 0x7FF);
+  const int E = ea - eb + 1023;  // biased exponent of the quotient when ma >= mb
+  if (ea == 0 || ea == 0x7FF || eb == 0 || eb == 0x7FF || E < 2 || E > 2045) return a / b;
+  const uint64_t FRAC = (1ull << 52) - 1, HID = 1ull << 52;
+  const uint64_t ma = (ua & FRAC) | HID, mb = (ub & FRAC) | HID;
+  const uint64_t d = mb << 11;
+  // seed: y0 = r * 2^87 with r the FP32 reciprocal of dt = d >> 40 (exponent -24,
+  // or exactly 2^-23 when dt = 2^23, where 2^127 / d rounds to the clamp)
+  const uint32_t rb = ddiv_rcp_bits((uint32_t)(d >> 40));
+  const uint64_t y0 = ((rb >> 23) & 0xFFu) == 103u ? ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u) << 40) : ~0ull;
+  const uint64_t y = ddiv_newton(d, ddiv_newton(d, y0));
+  // quotient of X = ma 2^53 by mb
+  uint64_t q = ddiv_mulhi(ma << 11, y) >> 10;
+  int64_t r = (int64_t)((ma << 53) - q * mb);
+  if (r < 0) {
+    q -= 1;
+    r += (int64_t)mb;
+  } else if (r >= (int64_t)mb) {
+    q += 1;
+    r -= (int64_t)mb;
+  }
+  uint64_t sig, inc;
+  int ebias;
+  if (q >= (1ull << 53)) {
+    sig = q >> 1;
+    const uint64_t round = q & 1ull, sticky = r != 0 ? 1ull : 0ull;
+    inc = round & (sticky | (sig & 1ull));
+    ebias = E;
+  } else {
+    sig = q;
+    const uint64_t twor = (uint64_t)r << 1;
+    inc = (twor > mb || (twor == mb && (sig & 1ull))) ? 1ull : 0ull;
+    ebias = E - 1;
+  }
+  // (ebias - 1) << 52 plus the 53-bit significand (hidden bit included);
+  // a rounding carry to 2^53 moves into the exponent by itself
+  const uint64_t mag = ((uint64_t)(ebias - 1) << 52) + sig + inc;
+  return ddiv_from_bits(mag | ((ua ^ ub) & (1ull << 63)));
+}
+
+}  // namespace amrs

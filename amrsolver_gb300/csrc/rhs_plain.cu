@@ -16,6 +16,7 @@
 // with explicit fused multiply-adds (weno5js_cd): the same function in
 // exact arithmetic, a quarter of the divisions, rounding differences only.
 #include "amrs_kernels.h"
+#include "ddiv.cuh"
 
 namespace amrs {
 
@@ -148,7 +149,9 @@ __global__ void __launch_bounds__(256) weno_flux_lambda_kernel(BoxTable tb, Face
 // WENO5-JS (src/rhs/High_resolution.h:124-159), beta[1] with the fourth power.
 // Operation order of the reference; a sum x + 2^k*y (power-of-two factor,
 // exact product) is one fma, which rounds exactly like the reference's
-// separate multiply and add.
+// separate multiply and add.  The four divisions are correctly rounded on
+// the integer pipe (ddiv_rn): the same quotients as the reference's, at a
+// fraction of the FP64 issue slots.
 __device__ __forceinline__ double weno5js(const double s0, const double s1, const double s2, const double s3,
                                           const double s4) {
   const double eps = 1e-40;
@@ -164,10 +167,10 @@ __device__ __forceinline__ double weno5js(const double s0, const double s1, cons
   const double beta1 = fma(0.25, g * g * g * g, (13.0 / 12.0) * c * c);
   const double beta2 = fma(0.25, f * f, (13.0 / 12.0) * d * d);
   const double e0 = eps + beta0, e1 = eps + beta1, e2 = eps + beta2;
-  const double alpha0 = 0.1 / (e0 * e0);
-  const double alpha1 = 0.6 / (e1 * e1);
-  const double alpha2 = 0.3 / (e2 * e2);
-  const double sum = 1.0 / (alpha0 + alpha1 + alpha2);
+  const double alpha0 = ddiv_rn(0.1, e0 * e0);
+  const double alpha1 = ddiv_rn(0.6, e1 * e1);
+  const double alpha2 = ddiv_rn(0.3, e2 * e2);
+  const double sum = ddiv_rn(1.0, alpha0 + alpha1 + alpha2);
   const double vl0 = fma(2.0, s0, -(7.0 * s1)) + 11.0 * s2;  // 2 s0 - 7 s1 + 11 s2
   const double vl1 = fma(2.0, s3, -s1 + 5.0 * s2);          // -s1 + 5 s2 + 2 s3
   const double vl2 = fma(2.0, s2, 5.0 * s3) - s4;           // 2 s2 + 5 s3 - s4

@@ -1,5 +1,6 @@
 // Ghost fill and time-step reduction kernels.
 #include "amrs_kernels.h"
+#include "ddiv.cuh"
 #include "tma.cuh"
 
 namespace amrs {
@@ -687,6 +688,66 @@ __global__ void __launch_bounds__(256) fp64_probe_kernel(double* out, int iters,
 
 cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t st) {
   fp64_probe_kernel<<<blocks, 256, 0, st>>>(out, iters, 0.999);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------ division check ----
+// ddiv_rn against the hardware division over generated operands: index i
+// of the launch draws (a, b) from one of four families (WENO weights
+// c_k / (eps + beta)^2, 1 / sum, arbitrary bit patterns, random significands
+// at moderate exponents) with a counter-based generator; mismatching bit
+// patterns are counted and the first one is recorded.
+__device__ __forceinline__ unsigned long long splitmix(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+__global__ void __launch_bounds__(256) ddiv_check_kernel(unsigned long long seed, long long count,
+                                                         unsigned long long* bad, double* first) {
+  unsigned long long nbad = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long r1 = splitmix(seed ^ (2 * (unsigned long long)i)),
+                             r2 = splitmix(seed ^ (2 * (unsigned long long)i + 1));
+    double a, b;
+    switch ((int)(i & 3)) {
+      case 0: {  // c_k / (1e-40 + beta)^2, beta = 2^[-200, 200) x random significand
+        const double beta = __longlong_as_double((long long)((r2 & 0xFFFFFFFFFFFFFull) | ((823ull + (r2 >> 55)) << 52)));
+        const double e = 1e-40 + beta;
+        const double c[4] = {0.1, 0.6, 0.3, 1.0};
+        a = c[r1 & 3];
+        b = e * e;
+        break;
+      }
+      case 1:  // 1 / sum of weights: sums over 2^[-140, 300)
+        a = 1.0;
+        b = __longlong_as_double((long long)((r2 & 0xFFFFFFFFFFFFFull) | ((883ull + (r2 >> 55) % 440ull) << 52)));
+        break;
+      case 2:  // arbitrary bit patterns (also the fallback domain)
+        a = __longlong_as_double((long long)r1);
+        b = __longlong_as_double((long long)r2);
+        break;
+      default:  // random significands and signs, exponents within +-128
+        a = __longlong_as_double((long long)((r1 & 0x800FFFFFFFFFFFFFull) | ((960ull + (r1 >> 56) % 128ull) << 52)));
+        b = __longlong_as_double((long long)((r2 & 0x800FFFFFFFFFFFFFull) | ((960ull + (r2 >> 56) % 128ull) << 52)));
+    }
+    const double ref = a / b, got = ddiv_rn(a, b);
+    const bool nan2 = ref != ref && got != got;
+    if (__double_as_longlong(ref) != __double_as_longlong(got) && !nan2) {
+      if (atomicAdd(bad, 1ull) == 0ull) {
+        first[0] = a; first[1] = b; first[2] = ref; first[3] = got;
+      }
+      ++nbad;
+    }
+  }
+  (void)nbad;
+}
+
+cudaError_t launch_ddiv_check(unsigned long long seed, long long count, unsigned long long* bad, double* first,
+                              int nsm, cudaStream_t st) {
+  ddiv_check_kernel<<<nsm * 8, 256, 0, st>>>(seed, count, bad, first);
   return cudaGetLastError();
 }
 

@@ -439,6 +439,14 @@ amrs_status amrs_probe_fp64_tflops(amrs_handle* h, double* tflops);
  * the SM clock over it can relate the rate to the clock.
  * Host-synchronising. */
 amrs_status amrs_probe_fp64_tflops_timed(amrs_handle* h, double seconds, double* tflops, double* ms);
+/* Check of the library's integer-pipe FP64 division (used where the kernels
+ * divide; no counterpart in the reference): `count` operand pairs generated
+ * on the device from `seed` (WENO weight and normalisation ranges, arbitrary
+ * bit patterns, random significands) are divided both ways; *mismatches
+ * receives the number of results whose bits differ from the hardware
+ * division's, first[0..3] the first such (a, b, hardware, library).
+ * Host-synchronising. */
+amrs_status amrs_debug_ddiv_check(amrs_handle* h, uint64_t seed, int64_t count, int64_t* mismatches, double* first);
 /* Per-kernel timing of one RK stage of one box: CUDA events around the
  * kernels on `stream`, averaged over `reps`.  ms[0] primitives (plus the
  * WENO5 point fluxes), ms[1] viscous cell fluxes, ms[2] the Euler face

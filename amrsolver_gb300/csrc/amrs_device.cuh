@@ -11,6 +11,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "ddiv.cuh"
+
 namespace amrs {
 
 constexpr int URHO = 0, UMX = 1, UMY = 2, UMZ = 3, UET = 4, NCONS = 5;
@@ -66,12 +68,12 @@ __device__ __forceinline__ double add_source(const DClosures& c, const double* U
 // visc_const_t::visc / visc_suth_t::visc (src/cls/Closures.h:103-120)
 __device__ __forceinline__ double visc(const DClosures& c, double T) {
   if (c.visc_law == 0) return c.visc_ref;
-  return c.visc_ref * T * sqrt(T) / (c.Tvisc_ref + T);
+  return ddiv_rn(c.visc_ref * T * sqrt(T), c.Tvisc_ref + T);
 }
 // cond_const_t::cond / cond_suth_t::cond (src/cls/Closures.h:130-166)
 __device__ __forceinline__ double cond(const DClosures& c, double T) {
   if (c.cond_law == 0) return c.cond_ref;
-  return c.cond_ref * T * sqrt(T) / (c.Tcond_ref + T);
+  return ddiv_rn(c.cond_ref * T * sqrt(T), c.Tcond_ref + T);
 }
 
 // std::max / std::min semantics
@@ -81,7 +83,7 @@ __device__ __forceinline__ double rmin(double a, double b) { return (b < a) ? b 
 // cons2prim (src/rhs/CNS_hydro_K.h:15-34) plus QE = cv*T.
 __device__ __forceinline__ void cons2prim(const double u[5], double q[NQ], const DClosures& c) {
   double rho = rmax(1e-40, u[URHO]);
-  double rhoinv = 1.0 / rho;
+  double rhoinv = ddiv_rn(1.0, rho);
   double ux = u[UMX] * rhoinv;
   double uy = u[UMY] * rhoinv;
   double uz = u[UMZ] * rhoinv;
@@ -93,7 +95,7 @@ __device__ __forceinline__ void cons2prim(const double u[5], double q[NQ], const
   q[QV] = uy;
   q[QW] = uz;
   q[QPRES] = p;
-  q[QT] = p / (rho * c.Rspec);
+  q[QT] = ddiv_rn(p, rho * c.Rspec);
   q[QE] = c.cv * q[QT];
 }
 

@@ -24,10 +24,11 @@
 //   Q in [2^53, 2^54): 54 quotient bits, the last one is the rounding bit and
 //       R != 0 the sticky bit; Q in [2^52, 2^53): 53 bits, rounding decided
 //       by comparing 2R with mb.
-// Domain: both operands normal and finite, and a result exponent that is
-// normal with room for a rounding carry; anything else (zeros, subnormals,
-// infinities, NaNs, results that overflow or underflow) takes the
-// hardware division, so the function equals a / b for every input.
+// Domain: b normal and finite, and either a = +-0 (result +-0) or a normal
+// and finite with a result exponent that is normal with room for a rounding
+// carry; anything else (b zero, subnormal, infinite or NaN, a subnormal,
+// infinite or NaN, results that overflow or underflow) takes the hardware
+// division, so the function equals a / b for every input.
 #pragma once
 #include <stdint.h>
 
@@ -103,7 +104,8 @@ AMRS_HD double ddiv_rn(double a, double b) {
   const uint64_t ua = ddiv_bits(a), ub = ddiv_bits(b);
   const int ea = (int)((ua >> 52) & 0x7FF), eb = (int)((ub >> 52) & 0x7FF);
   const int E = ea - eb + 1023;  // biased exponent of the quotient when ma >= mb
-  if (ea == 0 || ea == 0x7FF || eb == 0 || eb == 0x7FF || E < 2 || E > 2045) return a / b;
+  const bool azero = (ua << 1) == 0;
+  if (eb == 0 || eb == 0x7FF || (!azero && (ea == 0 || ea == 0x7FF || E < 2 || E > 2045))) return a / b;
   const uint64_t FRAC = (1ull << 52) - 1, HID = 1ull << 52;
   const uint64_t ma = (ua & FRAC) | HID, mb = (ub & FRAC) | HID;
   const uint64_t d = mb << 11;
@@ -137,7 +139,7 @@ AMRS_HD double ddiv_rn(double a, double b) {
   }
   // (ebias - 1) << 52 plus the 53-bit significand (hidden bit included);
   // a rounding carry to 2^53 moves into the exponent by itself
-  const uint64_t mag = ((uint64_t)(ebias - 1) << 52) + sig + inc;
+  const uint64_t mag = azero ? 0ull : ((uint64_t)(ebias - 1) << 52) + sig + inc;
   return ddiv_from_bits(mag | ((ua ^ ub) & (1ull << 63)));
 }
 

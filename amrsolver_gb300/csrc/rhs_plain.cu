@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) weno_flux_lambda_kernel(BoxTable tb, Face
     const DArr U = R.slot[s_in];
     const long long o = U.off(i, j, k);
     const double gam = tb.cls[R.cl].gamma;
-    const double rhoinv = 1.0 / U.p[o];
+    const double rhoinv = ddiv_rn(1.0, U.p[o]);
     const double momx = U.p[o + U.ns], momy = U.p[o + 2 * U.ns], momz = U.p[o + 3 * U.ns];
     const double rhoet = U.p[o + 4 * U.ns];
     const double ux = momx * rhoinv, uy = momy * rhoinv, uz = momz * rhoinv;
@@ -328,15 +328,15 @@ __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, c
     auto Q = [&](long long off, int n) { return q.p[off + n * q.ns]; };
     const double c0 = sqrt(cl.gamma * cl.Rspec * Q(o, QT));
     const double cspeed = c0 + (d == 0 ? 2.e-40 : 1.e-40);
-    double dlft = 0.5 * (Q(o, QPRES) - Q(o - s, QPRES)) / cspeed - 0.5 * Q(o, QRHO) * (Q(o, QN) - Q(o - s, QN));
-    double drgt = 0.5 * (Q(o + s, QPRES) - Q(o, QPRES)) / cspeed - 0.5 * Q(o, QRHO) * (Q(o + s, QN) - Q(o, QN));
+    double dlft = ddiv_rn(0.5 * (Q(o, QPRES) - Q(o - s, QPRES)), cspeed) - 0.5 * Q(o, QRHO) * (Q(o, QN) - Q(o - s, QN));
+    double drgt = ddiv_rn(0.5 * (Q(o + s, QPRES) - Q(o, QPRES)), cspeed) - 0.5 * Q(o, QRHO) * (Q(o + s, QN) - Q(o, QN));
     const double d0 = mc_limiter(dlft, drgt);
     const double cs2 = cspeed * cspeed;
-    dlft = (Q(o, QRHO) - Q(o - s, QRHO)) - (Q(o, QPRES) - Q(o - s, QPRES)) / cs2;
-    drgt = (Q(o + s, QRHO) - Q(o, QRHO)) - (Q(o + s, QPRES) - Q(o, QPRES)) / cs2;
+    dlft = (Q(o, QRHO) - Q(o - s, QRHO)) - ddiv_rn(Q(o, QPRES) - Q(o - s, QPRES), cs2);
+    drgt = (Q(o + s, QRHO) - Q(o, QRHO)) - ddiv_rn(Q(o + s, QPRES) - Q(o, QPRES), cs2);
     const double d1 = mc_limiter(dlft, drgt);
-    dlft = 0.5 * (Q(o, QPRES) - Q(o - s, QPRES)) / cspeed + 0.5 * Q(o, QRHO) * (Q(o, QN) - Q(o - s, QN));
-    drgt = 0.5 * (Q(o + s, QPRES) - Q(o, QPRES)) / cspeed + 0.5 * Q(o, QRHO) * (Q(o + s, QN) - Q(o, QN));
+    dlft = ddiv_rn(0.5 * (Q(o, QPRES) - Q(o - s, QPRES)), cspeed) + 0.5 * Q(o, QRHO) * (Q(o, QN) - Q(o - s, QN));
+    drgt = ddiv_rn(0.5 * (Q(o + s, QPRES) - Q(o, QPRES)), cspeed) + 0.5 * Q(o, QRHO) * (Q(o + s, QN) - Q(o, QN));
     const double d2 = mc_limiter(dlft, drgt);
     const double d3 = mc_limiter(Q(o, QT1) - Q(o - s, QT1), Q(o + s, QT1) - Q(o, QT1));
     const double d4 = mc_limiter(Q(o, QT2) - Q(o - s, QT2), Q(o + s, QT2) - Q(o, QT2));
@@ -348,8 +348,8 @@ __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, c
     const double s02 = d0 + d2;
     const DArr S = ft.fr[b].slope[d];
     const long long os = S.off(i, j, k);
-    S.p[os + SL_A * S.ns] = s02 / csr + d1;
-    S.p[os + SL_B * S.ns] = (d2 - d0) / Q(o, QRHO);
+    S.p[os + SL_A * S.ns] = ddiv_rn(s02, csr) + d1;
+    S.p[os + SL_B * S.ns] = ddiv_rn(d2 - d0, Q(o, QRHO));
     S.p[os + SL_C * S.ns] = s02 * csr;
     S.p[os + SL_T1 * S.ns] = d3;
     S.p[os + SL_T2 * S.ns] = d4;
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, c
       // cns_riemann_z's left state takes its sound speed from q(i,j,k+1)
       // (src/rhs/Riemann.h:316): for the face above this cell, cell k + 2
       const double csl = sqrt(cl.gamma * cl.Rspec * Q(o + 2 * s, QT)) + 1.e-40;
-      S.p[os + SL_AL * S.ns] = s02 / csl + d1;
+      S.p[os + SL_AL * S.ns] = ddiv_rn(s02, csl) + d1;
       S.p[os + SL_CL * S.ns] = s02 * csl;
     }
   }
@@ -374,26 +374,26 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   const double clsqr = gamma * pr * rr;
   double wl = sqrt(clsql);
   double wr = sqrt(clsqr);
-  const double cleft = wl / rl;
-  const double cright = wr / rr;
+  const double cleft = ddiv_rn(wl, rl);
+  const double cright = ddiv_rn(wr, rr);
   const double ccsmall = small * (cleft + cright);
-  double pstar = (wl * pr + wr * pl - wr * wl * (ur - ul)) / (wl + wr);
+  double pstar = ddiv_rn(wl * pr + wr * pl - wr * wl * (ur - ul), wl + wr);
   pstar = rmax(pstar, smallp);
   double pstnm1 = pstar;
   double wlsq = (0.5 * (gamma - 1.) * (pstar + pl) + pstar) * rl;
   double wrsq = (0.5 * (gamma - 1.) * (pstar + pr) + pstar) * rr;
   wl = sqrt(wlsq);
   wr = sqrt(wrsq);
-  double ustarp = ul - (pstar - pl) / wl;
-  double ustarm = ur + (pstar - pr) / wr;
-  pstar = (wl * pr + wr * pl - wr * wl * (ur - ul)) / (wl + wr);
+  double ustarp = ul - ddiv_rn(pstar - pl, wl);
+  double ustarm = ur + ddiv_rn(pstar - pr, wr);
+  pstar = ddiv_rn(wl * pr + wr * pl - wr * wl * (ur - ul), wl + wr);
   pstar = rmax(pstar, smallp);
   double ustar = 0.0;
   for (int iter = 0; iter < 3; ++iter) {
     wlsq = (0.5 * (gamma - 1.) * (pstar + pl) + pstar) * rl;
     wrsq = (0.5 * (gamma - 1.) * (pstar + pr) + pstar) * rr;
-    wl = 1. / sqrt(wlsq);
-    wr = 1. / sqrt(wrsq);
+    wl = ddiv_rn(1., sqrt(wlsq));
+    wr = ddiv_rn(1., sqrt(wrsq));
     const double ustnm1 = ustarm;
     const double ustnp1 = ustarp;
     ustarm = ur - (pr - pstar) * wr;
@@ -404,7 +404,7 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
     double zm = fabs(ustarm - ustnm1);
     if (zm - weakwv * cright < 0.0) zm = dpditer * wr;
     const double zz = zp + zm;
-    const double denom = dpditer / rmax(zz, ccsmall);
+    const double denom = ddiv_rn(dpditer, rmax(zz, ccsmall));
     pstnm1 = pstar;
     pstar = pstar - denom * (ustarm - ustarp);
     pstar = rmax(pstar, smallp);
@@ -418,7 +418,7 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   } else {
     uo = 0.5 * (ur + ul);
     po = 0.5 * (pr + pl);
-    ro = 2. * (rl * rr) / (rl + rr);
+    ro = ddiv_rn(2. * (rl * rr), rl + rr);
     sgnm = 1.;
     utrans1 = 0.5 * (ut1l + ut1r);
     utrans2 = 0.5 * (ut2l + ut2r);
@@ -432,25 +432,25 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   // (same operations, same values, same selection, NaN included).
   auto mixed = [&](double spin, double spout, double rstar) {
     const double ss = rmax(spout - spin, spout + spin);
-    const double frac = 0.5 * (1. + (spin + spout) / rmax(ss, ccsmall));
+    const double frac = 0.5 * (1. + ddiv_rn(spin + spout, rmax(ss, ccsmall)));
     rgdnv = frac * rstar + (1. - frac) * ro;
     ugdnv = frac * ustar + (1. - frac) * uo;
     pgdnv = frac * pstar + (1. - frac) * po;
   };
   if (pstar >= po) {
     // shock: spout == spin, so the side state or the star state
-    const double spin = sqrt(wosq) / ro - suo;
+    const double spin = ddiv_rn(sqrt(wosq), ro) - suo;
     if (spin < 0.) {
       rgdnv = ro; ugdnv = uo; pgdnv = po;
     } else if (spin >= 0.) {
-      rgdnv = ro / (1. - ro * dpjmp / wosq); ugdnv = ustar; pgdnv = pstar;
+      rgdnv = ddiv_rn(ro, 1. - ddiv_rn(ro * dpjmp, wosq)); ugdnv = ustar; pgdnv = pstar;
     } else {
-      mixed(spin, spin, ro / (1. - ro * dpjmp / wosq));
+      mixed(spin, spin, ddiv_rn(ro, 1. - ddiv_rn(ro * dpjmp, wosq)));
     }
   } else {
-    const double rstar = ro / (1. - ro * dpjmp / wosq);
-    const double spout = sqrt(gamma * po / ro) - suo;
-    const double spin = sqrt(gamma * pstar / rstar) - suo;
+    const double rstar = ddiv_rn(ro, 1. - ddiv_rn(ro * dpjmp, wosq));
+    const double spout = sqrt(ddiv_rn(gamma * po, ro)) - suo;
+    const double spin = sqrt(ddiv_rn(gamma * pstar, rstar)) - suo;
     if (spout < 0.) {
       rgdnv = ro; ugdnv = uo; pgdnv = po;
     } else if (spin >= 0.) {
@@ -464,7 +464,7 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   flxut = rgdnv * ugdnv * utrans1;
   flxutt = rgdnv * ugdnv * utrans2;
   // (0.5*r)*k + x == fma(0.5, r*k, x): the halving is exact (normal range)
-  flxe = ugdnv * (fma(0.5, rgdnv * (ugdnv * ugdnv + utrans1 * utrans1 + utrans2 * utrans2), pgdnv / (gamma - 1.)) +
+  flxe = ugdnv * (fma(0.5, rgdnv * (ugdnv * ugdnv + utrans1 * utrans1 + utrans2 * utrans2), ddiv_rn(pgdnv, gamma - 1.)) +
                   pgdnv);
 }
 
@@ -564,7 +564,7 @@ __device__ __forceinline__ double discon_sensor(double pp, double pl, double pr)
   // src/rhs/CNS_hydro_K.h:39-44
   const double pjst = pr + 2.0 * pp + pl;
   const double ptvd = fabs(pr - pp) + fabs(pp - pl);
-  return fabs(2.0 * (pr - 2.0 * pp + pl) / (pjst + ptvd + 1.0e-40));
+  return fabs(ddiv_rn(2.0 * (pr - 2.0 * pp + pl), pjst + ptvd + 1.0e-40));
 }
 
 // Sensor and spectral radius on the valid box (src/rhs/CNS_hydro_K.h:46-75);
@@ -587,7 +587,7 @@ __global__ void __launch_bounds__(256) jst_sensor_kernel(BoxTable tb, FaceTable 
     FR.sen.p[os + FR.sen.ns] = discon_sensor(pp, P(o - q.js), P(o + q.js));
     FR.sen.p[os + 2 * FR.sen.ns] = discon_sensor(pp, P(o - q.ks), P(o + q.ks));
     const double ux = q.p[o + QU * q.ns], uy = q.p[o + QV * q.ns], uz = q.p[o + QW * q.ns];
-    const double cs = sqrt(tb.cls[R.cl].gamma * pp / q.p[o + QRHO * q.ns]);
+    const double cs = sqrt(ddiv_rn(tb.cls[R.cl].gamma * pp, q.p[o + QRHO * q.ns]));
     FR.lam.p[os] = fabs(ux) + cs;
     FR.lam.p[os + FR.lam.ns] = fabs(uy) + cs;
     FR.lam.p[os + 2 * FR.lam.ns] = fabs(uz) + cs;

@@ -729,9 +729,10 @@ __global__ void __launch_bounds__(256) ddiv_check_kernel(unsigned long long seed
         a = __longlong_as_double((long long)r1);
         b = __longlong_as_double((long long)r2);
         break;
-      default:  // random significands and signs, exponents within +-128
+      default:  // random significands and signs, exponents within +-128; one in 32 numerators +-0
         a = __longlong_as_double((long long)((r1 & 0x800FFFFFFFFFFFFFull) | ((960ull + (r1 >> 56) % 128ull) << 52)));
         b = __longlong_as_double((long long)((r2 & 0x800FFFFFFFFFFFFFull) | ((960ull + (r2 >> 56) % 128ull) << 52)));
+        if (((r1 >> 51) & 31ull) == 0ull) a = __longlong_as_double((long long)(r1 & 0x8000000000000000ull));
     }
     const double ref = a / b, got = ddiv_rn(a, b);
     const bool nan2 = ref != ref && got != got;

@@ -68,12 +68,12 @@ __device__ __forceinline__ double add_source(const DClosures& c, const double* U
 // visc_const_t::visc / visc_suth_t::visc (src/cls/Closures.h:103-120)
 __device__ __forceinline__ double visc(const DClosures& c, double T) {
   if (c.visc_law == 0) return c.visc_ref;
-  return ddiv_rn(c.visc_ref * T * sqrt(T), c.Tvisc_ref + T);
+  return ddiv_rn(c.visc_ref * T * dsqrt_rn(T), c.Tvisc_ref + T);
 }
 // cond_const_t::cond / cond_suth_t::cond (src/cls/Closures.h:130-166)
 __device__ __forceinline__ double cond(const DClosures& c, double T) {
   if (c.cond_law == 0) return c.cond_ref;
-  return ddiv_rn(c.cond_ref * T * sqrt(T), c.Tcond_ref + T);
+  return ddiv_rn(c.cond_ref * T * dsqrt_rn(T), c.Tcond_ref + T);
 }
 
 // std::max / std::min semantics

@@ -150,6 +150,9 @@ cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t s
 // ddiv_rn (ddiv.cuh) against the hardware division over `count` generated operand pairs
 cudaError_t launch_ddiv_check(unsigned long long seed, long long count, unsigned long long* bad, double* first,
                               int nsm, cudaStream_t st);
+// dsqrt_rn (ddiv.cuh) against the hardware square root over `count` generated operands
+cudaError_t launch_dsqrt_check(unsigned long long seed, long long count, unsigned long long* bad, double* first,
+                               int nsm, cudaStream_t st);
 // amrex::average_down of cell-centred data (coarse box lo, extents n, ratio r).
 cudaError_t launch_avgdown(const DArr& fine, const DArr& crse, const int lo[3], const int n[3], const int r[3],
                            int scomp, int ncomp, double volfrac, int nsm, cudaStream_t st);

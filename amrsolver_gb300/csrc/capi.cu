@@ -1882,8 +1882,10 @@ amrs_status amrs_probe_fp64_tflops_timed(amrs_handle* h, double seconds, double*
   return AMRS_OK;
 }
 
-// The integer-pipe division against the hardware one (see the header).
-amrs_status amrs_debug_ddiv_check(amrs_handle* h, uint64_t seed, int64_t count, int64_t* mismatches, double* first) {
+// The integer-pipe division (what = 0) or square root (what = 1) against the
+// hardware one (see the header).
+static amrs_status intpipe_check(amrs_handle* h, int what, uint64_t seed, int64_t count, int64_t* mismatches,
+                                 double* first) {
   if (!h || !mismatches || !first) return AMRS_ERR_NULL;
   if (count < 1 || count > (1ll << 40)) return AMRS_ERR_SIZE;
   CK(cudaSetDevice(h->device));
@@ -1893,7 +1895,8 @@ amrs_status amrs_debug_ddiv_check(amrs_handle* h, uint64_t seed, int64_t count, 
   cudaError_t e = cudaMalloc(&dfirst, 4 * sizeof(double));
   if (e == cudaSuccess) e = cudaMemset(bad, 0, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemset(dfirst, 0, 4 * sizeof(double));
-  if (e == cudaSuccess) e = launch_ddiv_check(seed, count, bad, dfirst, h->nsm, 0);
+  if (e == cudaSuccess)
+    e = what ? launch_dsqrt_check(seed, count, bad, dfirst, h->nsm, 0) : launch_ddiv_check(seed, count, bad, dfirst, h->nsm, 0);
   unsigned long long nb = 0;
   if (e == cudaSuccess) e = cudaMemcpy(&nb, bad, sizeof(nb), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(first, dfirst, 4 * sizeof(double), cudaMemcpyDeviceToHost);
@@ -1902,6 +1905,14 @@ amrs_status amrs_debug_ddiv_check(amrs_handle* h, uint64_t seed, int64_t count, 
   if (e != cudaSuccess) return cuda_fail(e, "amrs_debug_ddiv_check");
   *mismatches = (int64_t)nb;
   return AMRS_OK;
+}
+
+amrs_status amrs_debug_ddiv_check(amrs_handle* h, uint64_t seed, int64_t count, int64_t* mismatches, double* first) {
+  return intpipe_check(h, 0, seed, count, mismatches, first);
+}
+
+amrs_status amrs_debug_dsqrt_check(amrs_handle* h, uint64_t seed, int64_t count, int64_t* mismatches, double* first) {
+  return intpipe_check(h, 1, seed, count, mismatches, first);
 }
 
 // The same probe with a timed launch of about 0.2 s.

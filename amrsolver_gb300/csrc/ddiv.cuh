@@ -1,5 +1,5 @@
-// Correctly rounded FP64 division a / b (IEEE round to nearest, ties to
-// even) computed on the integer pipe.
+// Correctly rounded FP64 division a / b and square root sqrt(x) (IEEE round
+// to nearest, ties to even) computed on the integer pipe.
 //
 // Why: on this GPU the FP64 pipe issues 2 lanes per clock per SM and every
 // kernel of the path is bound by it; a hardware-style FP64 division
@@ -35,6 +35,7 @@
 #ifdef __CUDACC__
 #define AMRS_HD __host__ __device__ __forceinline__
 #else
+#include <math.h>
 #include <string.h>
 #define AMRS_HD inline
 #endif
@@ -141,6 +142,82 @@ AMRS_HD double ddiv_rn(double a, double b) {
   // a rounding carry to 2^53 moves into the exponent by itself
   const uint64_t mag = azero ? 0ull : ((uint64_t)(ebias - 1) << 52) + sig + inc;
   return ddiv_from_bits(mag | ((ua ^ ub) & (1ull << 63)));
+}
+
+// Correctly rounded reciprocal square root of a float holding an integer
+// v in [2^22, 2^24), returned as its bits.
+AMRS_HD uint32_t dsqrt_rsqrt_bits(uint32_t v) {
+  // v as a float without a conversion instruction: 2^23 + low bits, or
+  // 2^22 + low bits for v below 2^23
+  const uint32_t fb = (v >> 23) ? (0x4B000000u | (v & 0x7FFFFFu)) : (0x4A800000u | ((v << 1) & 0x7FFFFFu));
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(__frsqrt_rn(__uint_as_float(fb)));
+#else
+  float f;
+  memcpy(&f, &fb, 4);
+  // host: the nearest float to 1/sqrt(f), from a double evaluation rounded once
+  const float r = (float)(1.0 / sqrt((double)f));
+  uint32_t rb;
+  memcpy(&rb, &r, 4);
+  return rb;
+#endif
+}
+
+// One Newton-Raphson step of y ~ 2^95 / sqrt(n) (n in [2^62, 2^64)):
+// y <- y + y (1 - n y^2 / 2^190) / 2.
+AMRS_HD uint64_t dsqrt_newton(uint64_t n, uint64_t y) {
+  const uint64_t t = ddiv_mulhi(y, y);             // y^2 / 2^64
+  const uint64_t u = ddiv_mulhi(n, t);             // n y^2 / 2^128, ~2^62
+  const int64_t e = (int64_t)((1ull << 62) - u);   // 2^62 (1 - n y^2 / 2^190)
+  const uint64_t m = e < 0 ? (uint64_t)(-e) : (uint64_t)e;
+  const uint64_t lo = y * m, hi = ddiv_mulhi(y, m);
+  const uint64_t corr = (hi << 1) | (lo >> 63);    // y |e| / 2^63
+  if (e < 0) return y - corr;
+  const uint64_t s = y + corr;
+  return s < y ? ~0ull : s;
+}
+
+// sqrt(x), correctly rounded (IEEE round to nearest even), computed on the
+// integer pipe for positive normal x (and +-0); anything else takes the
+// hardware square root, so the function equals sqrt(x) for every input.
+// Method: x = M 2^(2k) with N = M 2^104 an integer in [2^104, 2^106); a
+// fixed-point reciprocal square root y ~ 2^95 / sqrt(N / 2^42) from a
+// correctly rounded FP32 rsqrt seed and two Newton-Raphson steps (relative
+// error < 2^-60); S~ = floor(sqrt(N)) within 1 from (N / 2^42) y / 2^74; the
+// exact remainder R = N - S^2 (|R| < 2^55, exact in 64-bit arithmetic) fixes
+// S and decides the rounding: up iff R > S (N is an integer, so it never
+// equals (S + 1/2)^2).
+AMRS_HD double dsqrt_rn(double x) {
+  const uint64_t ux = ddiv_bits(x);
+  const int ex = (int)(ux >> 52);  // sign bit included: negative x lands above 0x7FF
+  if ((ux << 1) == 0) return x;     // +-0
+  if (ex == 0 || ex >= 0x7FF) {
+#ifdef __CUDA_ARCH__
+    return sqrt(x);
+#else
+    return ::sqrt(x);
+#endif
+  }
+  const int e = ex - 1023;
+  const uint64_t mx = (ux & ((1ull << 52) - 1)) | (1ull << 52);
+  const uint64_t N_lo = (e & 1) ? (mx << 53) : (mx << 52);  // N mod 2^64
+  const uint64_t n64 = (e & 1) ? (mx << 11) : (mx << 10);   // N / 2^42, in [2^62, 2^64)
+  const uint32_t rb = dsqrt_rsqrt_bits((uint32_t)(n64 >> 40));
+  // rsqrt in (2^-12, 2^-11]: y0 = rsqrt * 2^75 (clamped when it is 2^-11 exactly)
+  const uint64_t y0 = ((rb >> 23) & 0xFFu) == 115u ? ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u) << 40) : ~0ull;
+  const uint64_t y = dsqrt_newton(n64, dsqrt_newton(n64, y0));
+  uint64_t S = ddiv_mulhi(n64, y) >> 10;
+  int64_t R = (int64_t)(N_lo - S * S);
+  if (R < 0) {
+    S -= 1;
+    R += (int64_t)(2 * S + 1);
+  } else if (R > (int64_t)(2 * S)) {
+    R -= (int64_t)(2 * S + 1);
+    S += 1;
+  }
+  const uint64_t inc = R > (int64_t)S ? 1ull : 0ull;
+  const int eb = (e >> 1) + 1023;  // floor(e / 2), biased
+  return ddiv_from_bits(((uint64_t)(eb - 1) << 52) + S + inc);
 }
 
 }  // namespace amrs

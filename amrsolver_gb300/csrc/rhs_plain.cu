@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(256) weno_flux_lambda_kernel(BoxTable tb, Face
     fx[0] = momx; fx[ns] = momx * ux + P; fx[2 * ns] = momy * ux; fx[3 * ns] = momz * ux; fx[4 * ns] = (rhoet + P) * ux;
     fy[0] = momy; fy[ns] = momx * uy; fy[2 * ns] = momy * uy + P; fy[3 * ns] = momz * uy; fy[4 * ns] = (rhoet + P) * uy;
     fz[0] = momz; fz[ns] = momx * uz; fz[2 * ns] = momy * uz; fz[3 * ns] = momz * uz + P; fz[4 * ns] = (rhoet + P) * uz;
-    const double cs = sqrt(gam * P * rhoinv);
+    const double cs = dsqrt_rn(gam * P * rhoinv);
     const long long ol = FR.lam.off(i, j, k);
     FR.lam.p[ol] = fabs(rmax(rmax(ux + cs, ux - cs), ux));
     FR.lam.p[ol + FR.lam.ns] = fabs(rmax(rmax(uy + cs, uy - cs), uy));
@@ -326,7 +326,7 @@ __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, c
     const long long o = q.off(i, j, k);
     const int QN = QU + d, QT1 = (d == 0) ? QV : QU, QT2 = (d == 2) ? QV : QW;
     auto Q = [&](long long off, int n) { return q.p[off + n * q.ns]; };
-    const double c0 = sqrt(cl.gamma * cl.Rspec * Q(o, QT));
+    const double c0 = dsqrt_rn(cl.gamma * cl.Rspec * Q(o, QT));
     const double cspeed = c0 + (d == 0 ? 2.e-40 : 1.e-40);
     double dlft = ddiv_rn(0.5 * (Q(o, QPRES) - Q(o - s, QPRES)), cspeed) - 0.5 * Q(o, QRHO) * (Q(o, QN) - Q(o - s, QN));
     double drgt = ddiv_rn(0.5 * (Q(o + s, QPRES) - Q(o, QPRES)), cspeed) - 0.5 * Q(o, QRHO) * (Q(o + s, QN) - Q(o, QN));
@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, c
     if (d == 2 && k <= R.hi[2]) {
       // cns_riemann_z's left state takes its sound speed from q(i,j,k+1)
       // (src/rhs/Riemann.h:316): for the face above this cell, cell k + 2
-      const double csl = sqrt(cl.gamma * cl.Rspec * Q(o + 2 * s, QT)) + 1.e-40;
+      const double csl = dsqrt_rn(cl.gamma * cl.Rspec * Q(o + 2 * s, QT)) + 1.e-40;
       S.p[os + SL_AL * S.ns] = ddiv_rn(s02, csl) + d1;
       S.p[os + SL_CL * S.ns] = s02 * csl;
     }
@@ -372,8 +372,8 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   const double small = 1.e-6;
   const double clsql = gamma * pl * rl;
   const double clsqr = gamma * pr * rr;
-  double wl = sqrt(clsql);
-  double wr = sqrt(clsqr);
+  double wl = dsqrt_rn(clsql);
+  double wr = dsqrt_rn(clsqr);
   const double cleft = ddiv_rn(wl, rl);
   const double cright = ddiv_rn(wr, rr);
   const double ccsmall = small * (cleft + cright);
@@ -382,8 +382,8 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   double pstnm1 = pstar;
   double wlsq = (0.5 * (gamma - 1.) * (pstar + pl) + pstar) * rl;
   double wrsq = (0.5 * (gamma - 1.) * (pstar + pr) + pstar) * rr;
-  wl = sqrt(wlsq);
-  wr = sqrt(wrsq);
+  wl = dsqrt_rn(wlsq);
+  wr = dsqrt_rn(wrsq);
   double ustarp = ul - ddiv_rn(pstar - pl, wl);
   double ustarm = ur + ddiv_rn(pstar - pr, wr);
   pstar = ddiv_rn(wl * pr + wr * pl - wr * wl * (ur - ul), wl + wr);
@@ -392,8 +392,8 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   for (int iter = 0; iter < 3; ++iter) {
     wlsq = (0.5 * (gamma - 1.) * (pstar + pl) + pstar) * rl;
     wrsq = (0.5 * (gamma - 1.) * (pstar + pr) + pstar) * rr;
-    wl = ddiv_rn(1., sqrt(wlsq));
-    wr = ddiv_rn(1., sqrt(wrsq));
+    wl = ddiv_rn(1., dsqrt_rn(wlsq));
+    wr = ddiv_rn(1., dsqrt_rn(wrsq));
     const double ustnm1 = ustarm;
     const double ustnp1 = ustarp;
     ustarm = ur - (pr - pstar) * wr;
@@ -439,7 +439,7 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   };
   if (pstar >= po) {
     // shock: spout == spin, so the side state or the star state
-    const double spin = ddiv_rn(sqrt(wosq), ro) - suo;
+    const double spin = ddiv_rn(dsqrt_rn(wosq), ro) - suo;
     if (spin < 0.) {
       rgdnv = ro; ugdnv = uo; pgdnv = po;
     } else if (spin >= 0.) {
@@ -449,8 +449,8 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
     }
   } else {
     const double rstar = ddiv_rn(ro, 1. - ddiv_rn(ro * dpjmp, wosq));
-    const double spout = sqrt(ddiv_rn(gamma * po, ro)) - suo;
-    const double spin = sqrt(ddiv_rn(gamma * pstar, rstar)) - suo;
+    const double spout = dsqrt_rn(ddiv_rn(gamma * po, ro)) - suo;
+    const double spin = dsqrt_rn(ddiv_rn(gamma * pstar, rstar)) - suo;
     if (spout < 0.) {
       rgdnv = ro; ugdnv = uo; pgdnv = po;
     } else if (spin >= 0.) {
@@ -587,7 +587,7 @@ __global__ void __launch_bounds__(256) jst_sensor_kernel(BoxTable tb, FaceTable 
     FR.sen.p[os + FR.sen.ns] = discon_sensor(pp, P(o - q.js), P(o + q.js));
     FR.sen.p[os + 2 * FR.sen.ns] = discon_sensor(pp, P(o - q.ks), P(o + q.ks));
     const double ux = q.p[o + QU * q.ns], uy = q.p[o + QV * q.ns], uz = q.p[o + QW * q.ns];
-    const double cs = sqrt(ddiv_rn(tb.cls[R.cl].gamma * pp, q.p[o + QRHO * q.ns]));
+    const double cs = dsqrt_rn(ddiv_rn(tb.cls[R.cl].gamma * pp, q.p[o + QRHO * q.ns]));
     FR.lam.p[os] = fabs(ux) + cs;
     FR.lam.p[os + FR.lam.ns] = fabs(uy) + cs;
     FR.lam.p[os + 2 * FR.lam.ns] = fabs(uz) + cs;

@@ -311,15 +311,15 @@ __global__ void __launch_bounds__(256) estdt_kernel(BoxTable tb, int s_in, long 
       const DClosures& cl = tb.cls[R.cl];
       const long long o = S.off(i, j, k);
       const double rho = S.p[o], mx = S.p[o + S.ns], my = S.p[o + 2 * S.ns], mz = S.p[o + 2 * S.ns];
-      const double rhoinv = 1.0 / rmax(rho, 1.0e-40);
+      const double rhoinv = ddiv_rn(1.0, rmax(rho, 1.0e-40));
       const double vx = mx * rhoinv, vy = my * rhoinv, vz = mz * rhoinv;
       const double ke = 0.5 * rho * (vx * vx + vy * vy + vz * vz);
       const double rhoei = (S.p[o + 4 * S.ns] - ke);
       const double p = (cl.gamma - 1.0) * rhoei;
-      const double cs = sqrt(cl.gamma * p * rhoinv);
-      const double dtx = R.dx[0] / (fabs(vx) + cs);
-      const double dty = R.dx[1] / (fabs(vy) + cs);
-      const double dtz = R.dx[2] / (fabs(vz) + cs);
+      const double cs = dsqrt_rn(cl.gamma * p * rhoinv);
+      const double dtx = ddiv_rn(R.dx[0], fabs(vx) + cs);
+      const double dty = ddiv_rn(R.dx[1], fabs(vy) + cs);
+      const double dtz = ddiv_rn(R.dx[2], fabs(vz) + cs);
       const double dt = rmin(dtx, rmin(dty, dtz));
       const unsigned long long bb = (unsigned long long)__double_as_longlong(dt);
       if (dt >= 0.0 && bb < best) best = bb;
@@ -532,13 +532,13 @@ __global__ void __launch_bounds__(256) prim_stats_kernel(BoxTable tb, const long
       mn[n] = fmin(mn[n], q[n]);
       mx[n] = fmax(mx[n], q[n]);
     }
-    const double sos = sqrt(cl.gamma * cl.Rspec * q[QT]);
+    const double sos = dsqrt_rn(cl.gamma * cl.Rspec * q[QT]);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const double a0 = fabs(q[QU + d] + sos), a1 = fabs(q[QU + d] - sos);
       t[3 * d] = fmax(t[3 * d], a0);
       t[3 * d + 1] = fmax(t[3 * d + 1], a1);
-      t[3 * d + 2] = fmax(t[3 * d + 2], fmax(a0, a1) * dt / dxs[d]);
+      t[3 * d + 2] = fmax(t[3 * d + 2], ddiv_rn(fmax(a0, a1) * dt, dxs[d]));
     }
   }
 #pragma unroll
@@ -706,7 +706,6 @@ __device__ __forceinline__ unsigned long long splitmix(unsigned long long x) {
 
 __global__ void __launch_bounds__(256) ddiv_check_kernel(unsigned long long seed, long long count,
                                                          unsigned long long* bad, double* first) {
-  unsigned long long nbad = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
        i += (long long)gridDim.x * blockDim.x) {
     const unsigned long long r1 = splitmix(seed ^ (2 * (unsigned long long)i)),
@@ -740,15 +739,47 @@ __global__ void __launch_bounds__(256) ddiv_check_kernel(unsigned long long seed
       if (atomicAdd(bad, 1ull) == 0ull) {
         first[0] = a; first[1] = b; first[2] = ref; first[3] = got;
       }
-      ++nbad;
     }
   }
-  (void)nbad;
+}
+
+// dsqrt_rn against the hardware square root: arbitrary bit patterns,
+// positive doubles over the whole exponent range, squares of random doubles
+// and their neighbours.
+__global__ void __launch_bounds__(256) dsqrt_check_kernel(unsigned long long seed, long long count,
+                                                          unsigned long long* bad, double* first) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long r1 = splitmix(seed ^ (2 * (unsigned long long)i)),
+                             r2 = splitmix(seed ^ (2 * (unsigned long long)i + 1));
+    double x;
+    switch ((int)(i % 3)) {
+      case 0: x = __longlong_as_double((long long)r1); break;
+      case 1: x = __longlong_as_double((long long)(r1 & 0x7FFFFFFFFFFFFFFFull)); break;
+      default: {
+        const double r = __longlong_as_double((long long)((r1 & 0xFFFFFFFFFFFFFull) | ((600ull + r2 % 800ull) << 52)));
+        x = __longlong_as_double(__double_as_longlong(r * r) + (long long)((r2 >> 32) % 5ull) - 2);
+      }
+    }
+    const double ref = sqrt(x), got = dsqrt_rn(x);
+    const bool nan2 = ref != ref && got != got;
+    if (__double_as_longlong(ref) != __double_as_longlong(got) && !nan2) {
+      if (atomicAdd(bad, 1ull) == 0ull) {
+        first[0] = x; first[1] = 0.0; first[2] = ref; first[3] = got;
+      }
+    }
+  }
 }
 
 cudaError_t launch_ddiv_check(unsigned long long seed, long long count, unsigned long long* bad, double* first,
                               int nsm, cudaStream_t st) {
   ddiv_check_kernel<<<nsm * 8, 256, 0, st>>>(seed, count, bad, first);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dsqrt_check(unsigned long long seed, long long count, unsigned long long* bad, double* first,
+                               int nsm, cudaStream_t st) {
+  dsqrt_check_kernel<<<nsm * 8, 256, 0, st>>>(seed, count, bad, first);
   return cudaGetLastError();
 }
 

@@ -447,6 +447,11 @@ amrs_status amrs_probe_fp64_tflops_timed(amrs_handle* h, double seconds, double*
  * division's, first[0..3] the first such (a, b, hardware, library).
  * Host-synchronising. */
 amrs_status amrs_debug_ddiv_check(amrs_handle* h, uint64_t seed, int64_t count, int64_t* mismatches, double* first);
+/* The same for the library's integer-pipe FP64 square root: `count`
+ * arguments (arbitrary bit patterns, positive doubles over the whole
+ * exponent range, squares and their neighbours) against the hardware square
+ * root; first[0] = x, first[2] = hardware, first[3] = library. */
+amrs_status amrs_debug_dsqrt_check(amrs_handle* h, uint64_t seed, int64_t count, int64_t* mismatches, double* first);
 /* Per-kernel timing of one RK stage of one box: CUDA events around the
  * kernels on `stream`, averaged over `reps`.  ms[0] primitives (plus the
  * WENO5 point fluxes), ms[1] viscous cell fluxes, ms[2] the Euler face

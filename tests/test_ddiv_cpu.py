@@ -1,9 +1,12 @@
-"""The integer-pipe division (amrsolver_gb300/csrc/ddiv.cuh) on the host:
-compiled with g++ and compared bit for bit with the host's IEEE division
-over random operands (the WENO weight and normalisation ranges, arbitrary
-bit patterns, significands near all-ones and powers of two, quotients next
-to rounding boundaries) and special values.  The device build of the same
-header is checked against CUDA's division in tests/test_gpu_ddiv.py."""
+"""The integer-pipe division and square root (amrsolver_gb300/csrc/ddiv.cuh)
+on the host: compiled with g++ and compared bit for bit with the host's
+IEEE division and square root over random operands (for the division: the
+WENO weight and normalisation ranges, arbitrary bit patterns, significands
+near all-ones and powers of two, quotients next to rounding boundaries; for
+the square root: arbitrary bits, the whole exponent range, squares and
+their neighbours) and special values.  The device build of the same header
+is checked against CUDA's division and square root in
+tests/test_gpu_ddiv.py."""
 import os
 import subprocess
 
@@ -13,14 +16,24 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 @pytest.fixture(scope="module")
-def exe(tmp_path_factory):
-    out = str(tmp_path_factory.mktemp("ddiv") / "ddiv_check")
-    subprocess.check_call(["g++", "-O2", "-std=c++17", "-o", out, os.path.join(HERE, "cpp", "ddiv_check.cpp")])
+def exes(tmp_path_factory):
+    d = tmp_path_factory.mktemp("ddiv")
+    out = {}
+    for name in ("ddiv_check", "dsqrt_check"):
+        out[name] = str(d / name)
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-o", out[name], os.path.join(HERE, "cpp", name + ".cpp")])
     return out
 
 
 @pytest.mark.parametrize("seed", [11, 12])
-def test_ddiv_matches_ieee_division(exe, seed):
-    r = subprocess.run([exe, "10000000", str(seed)], capture_output=True, text=True)
+def test_ddiv_matches_ieee_division(exes, seed):
+    r = subprocess.run([exes["ddiv_check"], "10000000", str(seed)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout
+    assert "mismatches 0 checked" in r.stdout
+
+
+@pytest.mark.parametrize("seed", [13, 14])
+def test_dsqrt_matches_ieee_sqrt(exes, seed):
+    r = subprocess.run([exes["dsqrt_check"], "10000000", str(seed)], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout
     assert "mismatches 0 checked" in r.stdout

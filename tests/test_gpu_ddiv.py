@@ -1,8 +1,11 @@
-"""The integer-pipe FP64 division (amrsolver_gb300/csrc/ddiv.cuh) on the
-device against CUDA's own division: 4e9 generated operand pairs (the WENO
-weight and normalisation ranges, arbitrary bit patterns, random significands
-and signs), every result bit for bit.  The kernels that divide use it, so
-this equality is what keeps them equal to the reference's CPU build."""
+"""The integer-pipe FP64 division and square root
+(amrsolver_gb300/csrc/ddiv.cuh) on the device against CUDA's own: 4e9
+generated operand pairs for the division (the WENO weight and normalisation
+ranges, arbitrary bit patterns, random significands and signs, zero
+numerators) and 2e9 arguments for the square root (arbitrary bits, the whole
+exponent range, squares and their neighbours), every result bit for bit.
+The kernels that divide or take roots use them, so this equality is what
+keeps them equal to the reference's CPU build."""
 import pytest
 import torch
 
@@ -22,4 +25,14 @@ def test_ddiv_equals_hardware_division():
         assert bad == 0, ("division differs", seed, first)
         total += 1_000_000_000
     assert total >= 4_000_000_000
+    h.close()
+
+
+def test_dsqrt_equals_hardware_sqrt():
+    assert torch.cuda.is_available(), "GPU test needs a CUDA device"
+    capi.load(build_if_missing=True)
+    h = capi.Handle(P.Scheme(), P.Closures.nondimensional(1e-3))
+    for seed in (5, 6):
+        bad, first = h.ddiv_check(seed, 1_000_000_000, sqrt=True)
+        assert bad == 0, ("square root differs", seed, first)
     h.close()

@@ -70,20 +70,36 @@ AMRS_HD double ddiv_from_bits(uint64_t u) {
 #endif
 }
 
-// Correctly rounded reciprocal of a float holding an integer in [2^23, 2^24),
-// returned as its bits.
-AMRS_HD uint32_t ddiv_rcp_bits(uint32_t dt) {
+// Seeds of the Newton iterations.  They need about 22 correct bits, not
+// correct rounding: on the device the approximate FP32 reciprocal and
+// reciprocal square root (rcp.approx / rsqrt.approx, within 1 ulp and
+// 2^-22.9 relative), which run on the special-function unit and use no FP64
+// slot.  The host build perturbs the correctly rounded value by up to
+// +-2 ulps, so the host checks cover seeds at least that far off.
+AMRS_HD uint32_t ddiv_seed_perturb(uint32_t rb, uint32_t v) {
 #ifdef __CUDA_ARCH__
-  const float f = __uint_as_float(0x4B000000u | (dt & 0x7FFFFFu));  // == dt exactly
-  return __float_as_uint(__frcp_rn(f));
+  (void)v;
+  return rb;
+#else
+  return rb + (uint32_t)((int)((v ^ (v >> 7) ^ (v >> 13)) % 5u) - 2);
+#endif
+}
+
+// Reciprocal of a float holding an integer dt in [2^23, 2^24) (relative
+// error below 2^-22.5), returned as its bits.
+AMRS_HD uint32_t ddiv_rcp_bits(uint32_t dt) {
+  const uint32_t fb = 0x4B000000u | (dt & 0x7FFFFFu);  // the float equal to dt
+#ifdef __CUDA_ARCH__
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(__uint_as_float(fb)));
+  return __float_as_uint(r);
 #else
   float f, r;
-  const uint32_t fb = 0x4B000000u | (dt & 0x7FFFFFu);
   memcpy(&f, &fb, 4);
   r = 1.0f / f;
   uint32_t rb;
   memcpy(&rb, &r, 4);
-  return rb;
+  return ddiv_seed_perturb(rb, dt);
 #endif
 }
 
@@ -110,10 +126,12 @@ AMRS_HD double ddiv_rn(double a, double b) {
   const uint64_t FRAC = (1ull << 52) - 1, HID = 1ull << 52;
   const uint64_t ma = (ua & FRAC) | HID, mb = (ub & FRAC) | HID;
   const uint64_t d = mb << 11;
-  // seed: y0 = r * 2^87 with r the FP32 reciprocal of dt = d >> 40 (exponent -24,
-  // or exactly 2^-23 when dt = 2^23, where 2^127 / d rounds to the clamp)
+  // seed: y0 = r * 2^87 with r ~ 1/dt, dt = d >> 40: r = m 2^(er - 23) gives
+  // y0 = m << (er + 64); r lies near (2^-24, 2^-23], an approximate r may sit
+  // just outside, and a y0 of 2^64 or more is clamped
   const uint32_t rb = ddiv_rcp_bits((uint32_t)(d >> 40));
-  const uint64_t y0 = ((rb >> 23) & 0xFFu) == 103u ? ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u) << 40) : ~0ull;
+  const int rsh = (int)((rb >> 23) & 0xFFu) - 127 + 64;
+  const uint64_t y0 = rsh >= 41 ? ~0ull : ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u) << rsh);
   const uint64_t y = ddiv_newton(d, ddiv_newton(d, y0));
   // quotient of X = ma 2^53 by mb
   uint64_t q = ddiv_mulhi(ma << 11, y) >> 10;
@@ -144,22 +162,23 @@ AMRS_HD double ddiv_rn(double a, double b) {
   return ddiv_from_bits(mag | ((ua ^ ub) & (1ull << 63)));
 }
 
-// Correctly rounded reciprocal square root of a float holding an integer
-// v in [2^22, 2^24), returned as its bits.
+// Reciprocal square root of a float holding an integer v in [2^22, 2^24)
+// (relative error below 2^-22.5), returned as its bits.
 AMRS_HD uint32_t dsqrt_rsqrt_bits(uint32_t v) {
   // v as a float without a conversion instruction: 2^23 + low bits, or
   // 2^22 + low bits for v below 2^23
   const uint32_t fb = (v >> 23) ? (0x4B000000u | (v & 0x7FFFFFu)) : (0x4A800000u | ((v << 1) & 0x7FFFFFu));
 #ifdef __CUDA_ARCH__
-  return __float_as_uint(__frsqrt_rn(__uint_as_float(fb)));
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(__uint_as_float(fb)));
+  return __float_as_uint(r);
 #else
   float f;
   memcpy(&f, &fb, 4);
-  // host: the nearest float to 1/sqrt(f), from a double evaluation rounded once
   const float r = (float)(1.0 / sqrt((double)f));
   uint32_t rb;
   memcpy(&rb, &r, 4);
-  return rb;
+  return ddiv_seed_perturb(rb, v);
 #endif
 }
 
@@ -203,8 +222,10 @@ AMRS_HD double dsqrt_rn(double x) {
   const uint64_t N_lo = (e & 1) ? (mx << 53) : (mx << 52);  // N mod 2^64
   const uint64_t n64 = (e & 1) ? (mx << 11) : (mx << 10);   // N / 2^42, in [2^62, 2^64)
   const uint32_t rb = dsqrt_rsqrt_bits((uint32_t)(n64 >> 40));
-  // rsqrt in (2^-12, 2^-11]: y0 = rsqrt * 2^75 (clamped when it is 2^-11 exactly)
-  const uint64_t y0 = ((rb >> 23) & 0xFFu) == 115u ? ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u) << 40) : ~0ull;
+  // y0 = rsqrt * 2^75 = m << (er + 52) for rsqrt = m 2^(er - 23) near (2^-12, 2^-11];
+  // an approximate value may sit just outside, and 2^64 or more is clamped
+  const int rsh = (int)((rb >> 23) & 0xFFu) - 127 + 52;
+  const uint64_t y0 = rsh >= 41 ? ~0ull : ((uint64_t)((rb & 0x7FFFFFu) | 0x800000u) << rsh);
   const uint64_t y = dsqrt_newton(n64, dsqrt_newton(n64, y0));
   uint64_t S = ddiv_mulhi(n64, y) >> 10;
   int64_t R = (int64_t)(N_lo - S * S);

@@ -732,6 +732,10 @@ __global__ void __launch_bounds__(256) ddiv_check_kernel(unsigned long long seed
         a = __longlong_as_double((long long)((r1 & 0x800FFFFFFFFFFFFFull) | ((960ull + (r1 >> 56) % 128ull) << 52)));
         b = __longlong_as_double((long long)((r2 & 0x800FFFFFFFFFFFFFull) | ((960ull + (r2 >> 56) % 128ull) << 52)));
         if (((r1 >> 51) & 31ull) == 0ull) a = __longlong_as_double((long long)(r1 & 0x8000000000000000ull));
+        // one in 4 divisors with a significand near 2 (the reciprocal seed
+        // then sits at the edge of its binade)
+        if (((r2 >> 40) & 3ull) == 0ull)
+          b = __longlong_as_double(__double_as_longlong(b) | 0x000FFFFFFF000000ll);
     }
     const double ref = a / b, got = ddiv_rn(a, b);
     const bool nan2 = ref != ref && got != got;
@@ -753,9 +757,13 @@ __global__ void __launch_bounds__(256) dsqrt_check_kernel(unsigned long long see
     const unsigned long long r1 = splitmix(seed ^ (2 * (unsigned long long)i)),
                              r2 = splitmix(seed ^ (2 * (unsigned long long)i + 1));
     double x;
-    switch ((int)(i % 3)) {
+    switch ((int)(i % 4)) {
       case 0: x = __longlong_as_double((long long)r1); break;
       case 1: x = __longlong_as_double((long long)(r1 & 0x7FFFFFFFFFFFFFFFull)); break;
+      case 2:  // significands near 1 and near 2, both exponent parities
+        x = __longlong_as_double((long long)((((r1 & 1ull) ? (0xFFFFFFFFFFFFFull - (r2 & 0xFFFFFFull)) : (r2 & 0xFFFFFFull))) |
+                                             ((1ull + r1 % 2046ull) << 52)));
+        break;
       default: {
         const double r = __longlong_as_double((long long)((r1 & 0xFFFFFFFFFFFFFull) | ((600ull + r2 % 800ull) << 52)));
         x = __longlong_as_double(__double_as_longlong(r * r) + (long long)((r2 >> 32) % 5ull) - 2);

@@ -52,8 +52,8 @@ int main(int argc, char** argv) {
       a = from_bits((rnd() & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(900 + rnd() % 250) << 52));
       b = from_bits((rnd() & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(900 + rnd() % 250) << 52));
     } else if (kind == 4) {  // significands near all-ones / power of two
-      const uint64_t fa = (rnd() & 1) ? (0xFFFFFFFFFFFFFull - (rnd() & 0xFF)) : (rnd() & 0xFF);
-      const uint64_t fb = (rnd() & 1) ? (0xFFFFFFFFFFFFFull - (rnd() & 0xFF)) : (rnd() & 0xFF);
+      const uint64_t fa = (rnd() & 1) ? (0xFFFFFFFFFFFFFull - (rnd() & 0xFFFFFF)) : (rnd() & 0xFFFFFF);
+      const uint64_t fb = (rnd() & 1) ? (0xFFFFFFFFFFFFFull - (rnd() & 0xFFFFFF)) : (rnd() & 0xFFFFFF);
       a = from_bits(fa | ((uint64_t)(1000 + rnd() % 40) << 52));
       b = from_bits(fb | ((uint64_t)(1000 + rnd() % 40) << 52));
     } else {  // quotients landing next to the rounding boundaries: a = q b +- a few ulps

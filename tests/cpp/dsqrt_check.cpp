@@ -39,7 +39,7 @@ int main(int argc, char** argv) {
     if (kind == 0) x = from_bits(rnd());
     else if (kind == 1) x = from_bits(rnd() & 0x7FFFFFFFFFFFFFFFull);
     else if (kind == 2) {
-      const uint64_t f = (rnd() & 1) ? (0xFFFFFFFFFFFFFull - (rnd() & 0xFFF)) : (rnd() & 0xFFF);
+      const uint64_t f = (rnd() & 1) ? (0xFFFFFFFFFFFFFull - (rnd() & 0xFFFFFF)) : (rnd() & 0xFFFFFF);
       x = from_bits(f | ((uint64_t)(1 + rnd() % 2046) << 52));
     } else {
       const double r = from_bits((rnd() & 0xFFFFFFFFFFFFFull) | ((uint64_t)(600 + rnd() % 800) << 52));

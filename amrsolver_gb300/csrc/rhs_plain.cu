@@ -363,7 +363,10 @@ __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, c
   }
 }
 
-// Two-shock approximate Riemann solver (src/rhs/Riemann.h:123-249).
+// Two-shock approximate Riemann solver (src/rhs/Riemann.h:123-249).  Its
+// three pressure iterations are one serial chain per face, so it keeps the
+// hardware division and square root (shorter latency than the integer-pipe
+// forms, which pay off where many independent quotients overlap).
 __device__ void riemann_prob(const double gamma, const double smallp, const double rl, const double ul,
                              const double pl, const double ut1l, const double ut2l, const double rr, const double ur,
                              const double pr, const double ut1r, const double ut2r, double& flxrho, double& flxu,
@@ -372,28 +375,28 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   const double small = 1.e-6;
   const double clsql = gamma * pl * rl;
   const double clsqr = gamma * pr * rr;
-  double wl = dsqrt_rn(clsql);
-  double wr = dsqrt_rn(clsqr);
-  const double cleft = ddiv_rn(wl, rl);
-  const double cright = ddiv_rn(wr, rr);
+  double wl = sqrt(clsql);
+  double wr = sqrt(clsqr);
+  const double cleft = wl / rl;
+  const double cright = wr / rr;
   const double ccsmall = small * (cleft + cright);
-  double pstar = ddiv_rn(wl * pr + wr * pl - wr * wl * (ur - ul), wl + wr);
+  double pstar = (wl * pr + wr * pl - wr * wl * (ur - ul)) / (wl + wr);
   pstar = rmax(pstar, smallp);
   double pstnm1 = pstar;
   double wlsq = (0.5 * (gamma - 1.) * (pstar + pl) + pstar) * rl;
   double wrsq = (0.5 * (gamma - 1.) * (pstar + pr) + pstar) * rr;
-  wl = dsqrt_rn(wlsq);
-  wr = dsqrt_rn(wrsq);
-  double ustarp = ul - ddiv_rn(pstar - pl, wl);
-  double ustarm = ur + ddiv_rn(pstar - pr, wr);
-  pstar = ddiv_rn(wl * pr + wr * pl - wr * wl * (ur - ul), wl + wr);
+  wl = sqrt(wlsq);
+  wr = sqrt(wrsq);
+  double ustarp = ul - (pstar - pl) / wl;
+  double ustarm = ur + (pstar - pr) / wr;
+  pstar = (wl * pr + wr * pl - wr * wl * (ur - ul)) / (wl + wr);
   pstar = rmax(pstar, smallp);
   double ustar = 0.0;
   for (int iter = 0; iter < 3; ++iter) {
     wlsq = (0.5 * (gamma - 1.) * (pstar + pl) + pstar) * rl;
     wrsq = (0.5 * (gamma - 1.) * (pstar + pr) + pstar) * rr;
-    wl = ddiv_rn(1., dsqrt_rn(wlsq));
-    wr = ddiv_rn(1., dsqrt_rn(wrsq));
+    wl = 1. / sqrt(wlsq);
+    wr = 1. / sqrt(wrsq);
     const double ustnm1 = ustarm;
     const double ustnp1 = ustarp;
     ustarm = ur - (pr - pstar) * wr;
@@ -404,7 +407,7 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
     double zm = fabs(ustarm - ustnm1);
     if (zm - weakwv * cright < 0.0) zm = dpditer * wr;
     const double zz = zp + zm;
-    const double denom = ddiv_rn(dpditer, rmax(zz, ccsmall));
+    const double denom = dpditer / rmax(zz, ccsmall);
     pstnm1 = pstar;
     pstar = pstar - denom * (ustarm - ustarp);
     pstar = rmax(pstar, smallp);
@@ -418,7 +421,7 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   } else {
     uo = 0.5 * (ur + ul);
     po = 0.5 * (pr + pl);
-    ro = ddiv_rn(2. * (rl * rr), rl + rr);
+    ro = 2. * (rl * rr) / (rl + rr);
     sgnm = 1.;
     utrans1 = 0.5 * (ut1l + ut1r);
     utrans2 = 0.5 * (ut2l + ut2r);
@@ -432,25 +435,25 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   // (same operations, same values, same selection, NaN included).
   auto mixed = [&](double spin, double spout, double rstar) {
     const double ss = rmax(spout - spin, spout + spin);
-    const double frac = 0.5 * (1. + ddiv_rn(spin + spout, rmax(ss, ccsmall)));
+    const double frac = 0.5 * (1. + (spin + spout) / rmax(ss, ccsmall));
     rgdnv = frac * rstar + (1. - frac) * ro;
     ugdnv = frac * ustar + (1. - frac) * uo;
     pgdnv = frac * pstar + (1. - frac) * po;
   };
   if (pstar >= po) {
     // shock: spout == spin, so the side state or the star state
-    const double spin = ddiv_rn(dsqrt_rn(wosq), ro) - suo;
+    const double spin = sqrt(wosq) / ro - suo;
     if (spin < 0.) {
       rgdnv = ro; ugdnv = uo; pgdnv = po;
     } else if (spin >= 0.) {
-      rgdnv = ddiv_rn(ro, 1. - ddiv_rn(ro * dpjmp, wosq)); ugdnv = ustar; pgdnv = pstar;
+      rgdnv = ro / (1. - ro * dpjmp / wosq); ugdnv = ustar; pgdnv = pstar;
     } else {
-      mixed(spin, spin, ddiv_rn(ro, 1. - ddiv_rn(ro * dpjmp, wosq)));
+      mixed(spin, spin, ro / (1. - ro * dpjmp / wosq));
     }
   } else {
-    const double rstar = ddiv_rn(ro, 1. - ddiv_rn(ro * dpjmp, wosq));
-    const double spout = dsqrt_rn(ddiv_rn(gamma * po, ro)) - suo;
-    const double spin = dsqrt_rn(ddiv_rn(gamma * pstar, rstar)) - suo;
+    const double rstar = ro / (1. - ro * dpjmp / wosq);
+    const double spout = sqrt(gamma * po / ro) - suo;
+    const double spin = sqrt(gamma * pstar / rstar) - suo;
     if (spout < 0.) {
       rgdnv = ro; ugdnv = uo; pgdnv = po;
     } else if (spin >= 0.) {
@@ -464,7 +467,7 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   flxut = rgdnv * ugdnv * utrans1;
   flxutt = rgdnv * ugdnv * utrans2;
   // (0.5*r)*k + x == fma(0.5, r*k, x): the halving is exact (normal range)
-  flxe = ugdnv * (fma(0.5, rgdnv * (ugdnv * ugdnv + utrans1 * utrans1 + utrans2 * utrans2), ddiv_rn(pgdnv, gamma - 1.)) +
+  flxe = ugdnv * (fma(0.5, rgdnv * (ugdnv * ugdnv + utrans1 * utrans1 + utrans2 * utrans2), pgdnv / (gamma - 1.)) +
                   pgdnv);
 }
 

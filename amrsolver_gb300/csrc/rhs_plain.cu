@@ -326,7 +326,7 @@ __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, c
     const long long o = q.off(i, j, k);
     const int QN = QU + d, QT1 = (d == 0) ? QV : QU, QT2 = (d == 2) ? QV : QW;
     auto Q = [&](long long off, int n) { return q.p[off + n * q.ns]; };
-    const double c0 = dsqrt_rn(cl.gamma * cl.Rspec * Q(o, QT));
+    const double c0 = sqrt(cl.gamma * cl.Rspec * Q(o, QT));
     const double cspeed = c0 + (d == 0 ? 2.e-40 : 1.e-40);
     double dlft = ddiv_rn(0.5 * (Q(o, QPRES) - Q(o - s, QPRES)), cspeed) - 0.5 * Q(o, QRHO) * (Q(o, QN) - Q(o - s, QN));
     double drgt = ddiv_rn(0.5 * (Q(o + s, QPRES) - Q(o, QPRES)), cspeed) - 0.5 * Q(o, QRHO) * (Q(o + s, QN) - Q(o, QN));
@@ -356,17 +356,27 @@ __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, c
     if (d == 2 && k <= R.hi[2]) {
       // cns_riemann_z's left state takes its sound speed from q(i,j,k+1)
       // (src/rhs/Riemann.h:316): for the face above this cell, cell k + 2
-      const double csl = dsqrt_rn(cl.gamma * cl.Rspec * Q(o + 2 * s, QT)) + 1.e-40;
+      const double csl = sqrt(cl.gamma * cl.Rspec * Q(o + 2 * s, QT)) + 1.e-40;
       S.p[os + SL_AL * S.ns] = ddiv_rn(s02, csl) + d1;
       S.p[os + SL_CL * S.ns] = s02 * csl;
     }
   }
 }
 
+// Division of the two-shock solver: IDIV picks the integer-pipe form
+// (ddiv_rn) or the hardware one; both give the same correctly rounded bits.
+template <bool IDIV>
+__device__ __forceinline__ double rdiv(double a, double b) {
+  return IDIV ? ddiv_rn(a, b) : a / b;
+}
+
 // Two-shock approximate Riemann solver (src/rhs/Riemann.h:123-249).  Its
-// three pressure iterations are one serial chain per face, so it keeps the
-// hardware division and square root (shorter latency than the integer-pipe
-// forms, which pay off where many independent quotients overlap).
+// pressure iterations are one serial chain per face, so the choice of
+// division is the caller's: the MUSCL face kernel runs faster with the
+// integer-pipe division, the WENO5-Riemann kernel (whose reconstructions
+// already load the integer pipe) with the hardware one; the square roots are
+// the hardware's in both (their integer form lengthens the chain).
+template <bool IDIV>
 __device__ void riemann_prob(const double gamma, const double smallp, const double rl, const double ul,
                              const double pl, const double ut1l, const double ut2l, const double rr, const double ur,
                              const double pr, const double ut1r, const double ut2r, double& flxrho, double& flxu,
@@ -377,26 +387,26 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   const double clsqr = gamma * pr * rr;
   double wl = sqrt(clsql);
   double wr = sqrt(clsqr);
-  const double cleft = wl / rl;
-  const double cright = wr / rr;
+  const double cleft = rdiv<IDIV>(wl, rl);
+  const double cright = rdiv<IDIV>(wr, rr);
   const double ccsmall = small * (cleft + cright);
-  double pstar = (wl * pr + wr * pl - wr * wl * (ur - ul)) / (wl + wr);
+  double pstar = rdiv<IDIV>(wl * pr + wr * pl - wr * wl * (ur - ul), wl + wr);
   pstar = rmax(pstar, smallp);
   double pstnm1 = pstar;
   double wlsq = (0.5 * (gamma - 1.) * (pstar + pl) + pstar) * rl;
   double wrsq = (0.5 * (gamma - 1.) * (pstar + pr) + pstar) * rr;
   wl = sqrt(wlsq);
   wr = sqrt(wrsq);
-  double ustarp = ul - (pstar - pl) / wl;
-  double ustarm = ur + (pstar - pr) / wr;
-  pstar = (wl * pr + wr * pl - wr * wl * (ur - ul)) / (wl + wr);
+  double ustarp = ul - rdiv<IDIV>(pstar - pl, wl);
+  double ustarm = ur + rdiv<IDIV>(pstar - pr, wr);
+  pstar = rdiv<IDIV>(wl * pr + wr * pl - wr * wl * (ur - ul), wl + wr);
   pstar = rmax(pstar, smallp);
   double ustar = 0.0;
   for (int iter = 0; iter < 3; ++iter) {
     wlsq = (0.5 * (gamma - 1.) * (pstar + pl) + pstar) * rl;
     wrsq = (0.5 * (gamma - 1.) * (pstar + pr) + pstar) * rr;
-    wl = 1. / sqrt(wlsq);
-    wr = 1. / sqrt(wrsq);
+    wl = rdiv<IDIV>(1., sqrt(wlsq));
+    wr = rdiv<IDIV>(1., sqrt(wrsq));
     const double ustnm1 = ustarm;
     const double ustnp1 = ustarp;
     ustarm = ur - (pr - pstar) * wr;
@@ -407,7 +417,7 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
     double zm = fabs(ustarm - ustnm1);
     if (zm - weakwv * cright < 0.0) zm = dpditer * wr;
     const double zz = zp + zm;
-    const double denom = dpditer / rmax(zz, ccsmall);
+    const double denom = rdiv<IDIV>(dpditer, rmax(zz, ccsmall));
     pstnm1 = pstar;
     pstar = pstar - denom * (ustarm - ustarp);
     pstar = rmax(pstar, smallp);
@@ -421,7 +431,7 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   } else {
     uo = 0.5 * (ur + ul);
     po = 0.5 * (pr + pl);
-    ro = 2. * (rl * rr) / (rl + rr);
+    ro = rdiv<IDIV>(2. * (rl * rr), rl + rr);
     sgnm = 1.;
     utrans1 = 0.5 * (ut1l + ut1r);
     utrans2 = 0.5 * (ut2l + ut2r);
@@ -435,25 +445,25 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   // (same operations, same values, same selection, NaN included).
   auto mixed = [&](double spin, double spout, double rstar) {
     const double ss = rmax(spout - spin, spout + spin);
-    const double frac = 0.5 * (1. + (spin + spout) / rmax(ss, ccsmall));
+    const double frac = 0.5 * (1. + rdiv<IDIV>(spin + spout, rmax(ss, ccsmall)));
     rgdnv = frac * rstar + (1. - frac) * ro;
     ugdnv = frac * ustar + (1. - frac) * uo;
     pgdnv = frac * pstar + (1. - frac) * po;
   };
   if (pstar >= po) {
     // shock: spout == spin, so the side state or the star state
-    const double spin = sqrt(wosq) / ro - suo;
+    const double spin = rdiv<IDIV>(sqrt(wosq), ro) - suo;
     if (spin < 0.) {
       rgdnv = ro; ugdnv = uo; pgdnv = po;
     } else if (spin >= 0.) {
-      rgdnv = ro / (1. - ro * dpjmp / wosq); ugdnv = ustar; pgdnv = pstar;
+      rgdnv = rdiv<IDIV>(ro, 1. - rdiv<IDIV>(ro * dpjmp, wosq)); ugdnv = ustar; pgdnv = pstar;
     } else {
-      mixed(spin, spin, ro / (1. - ro * dpjmp / wosq));
+      mixed(spin, spin, rdiv<IDIV>(ro, 1. - rdiv<IDIV>(ro * dpjmp, wosq)));
     }
   } else {
-    const double rstar = ro / (1. - ro * dpjmp / wosq);
-    const double spout = sqrt(gamma * po / ro) - suo;
-    const double spin = sqrt(gamma * pstar / rstar) - suo;
+    const double rstar = rdiv<IDIV>(ro, 1. - rdiv<IDIV>(ro * dpjmp, wosq));
+    const double spout = sqrt(rdiv<IDIV>(gamma * po, ro)) - suo;
+    const double spin = sqrt(rdiv<IDIV>(gamma * pstar, rstar)) - suo;
     if (spout < 0.) {
       rgdnv = ro; ugdnv = uo; pgdnv = po;
     } else if (spin >= 0.) {
@@ -467,7 +477,7 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   flxut = rgdnv * ugdnv * utrans1;
   flxutt = rgdnv * ugdnv * utrans2;
   // (0.5*r)*k + x == fma(0.5, r*k, x): the halving is exact (normal range)
-  flxe = ugdnv * (fma(0.5, rgdnv * (ugdnv * ugdnv + utrans1 * utrans1 + utrans2 * utrans2), pgdnv / (gamma - 1.)) +
+  flxe = ugdnv * (fma(0.5, rgdnv * (ugdnv * ugdnv + utrans1 * utrans1 + utrans2 * utrans2), rdiv<IDIV>(pgdnv, gamma - 1.)) +
                   pgdnv);
 }
 
@@ -506,7 +516,7 @@ __global__ void __launch_bounds__(256) riemann_face_kernel(BoxTable tb, FaceTabl
     const double ut1r = fma(-0.5, D(os, SL_T1), Q(oq, QT1));
     const double ut2r = fma(-0.5, D(os, SL_T2), Q(oq, QT2));
     double frho, fu, fut, futt, fe;
-    riemann_prob(gam, 1.0e-40, rl, ul, pl, ut1l, ut2l, rr, ur, pr, ut1r, ut2r, frho, fu, fut, futt, fe);
+    riemann_prob<true>(gam, 1.0e-40, rl, ul, pl, ut1l, ut2l, rr, ur, pr, ut1r, ut2r, frho, fu, fut, futt, fe);
     const DArr Fd = ft.fr[f.b].f[d];
     const long long of = Fd.off(f.i, f.j, f.k);
     Fd.p[of + URHO * Fd.ns] = frho;
@@ -550,8 +560,8 @@ __global__ void __launch_bounds__(256) weno_riemann_face_kernel(BoxTable tb, Fac
       rgt[m] = weno5js(v[5], v[4], v[3], v[2], v[1]);
     }
     double frho, fu, fut, futt, fe;
-    riemann_prob(cl.gamma, 1.0e-40, rmax(lft[0], 1.0e-40), lft[1], rmax(lft[2], 1.0e-40), lft[3], lft[4],
-                 rmax(rgt[0], 1.0e-40), rgt[1], rmax(rgt[2], 1.0e-40), rgt[3], rgt[4], frho, fu, fut, futt, fe);
+    riemann_prob<false>(cl.gamma, 1.0e-40, rmax(lft[0], 1.0e-40), lft[1], rmax(lft[2], 1.0e-40), lft[3], lft[4],
+                        rmax(rgt[0], 1.0e-40), rgt[1], rmax(rgt[2], 1.0e-40), rgt[3], rgt[4], frho, fu, fut, futt, fe);
     const DArr Fd = ft.fr[f.b].f[d];
     const long long of = Fd.off(f.i, f.j, f.k);
     Fd.p[of + URHO * Fd.ns] = frho;

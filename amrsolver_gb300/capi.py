@@ -116,6 +116,7 @@ SIGNATURES = {
     "amrs_boxlist_set_schedule": (_S, [_P, ctypes.c_int32]),
     "amrs_boxlist_face_grid": (ctypes.c_int32, [_P]),
     "amrs_boxlist_get_tiles": (_S, [_P, _P]),
+    "amrs_plot_derive_box": (_S, [ctypes.POINTER(CClosures), ctypes.POINTER(CBox), Array4, Array4, _P]),
     "amrs_boxlist_prim_stats": (_S, [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.c_double, _P, _P]),
     "amrs_prim_stats_box": (_S, [_P, ctypes.POINTER(CBox), ctypes.POINTER(ctypes.c_double), Array4, ctypes.c_double,
                                  _P, _P]),
@@ -569,3 +570,15 @@ class BoxList:
         check(self._L.amrs_boxlist_totals(self.bl, slot, float(scale), ctypes.c_void_p(out.data_ptr()),
                                           _stream_ptr(stream)), "amrs_boxlist_totals")
         return out
+
+
+def plot_derive(closures, U, lo, out, ng=NGHOST, stream=None):
+    """Derived plot variables (pressure, temperature, x/y/z velocity) of the
+    valid cells of one box's state `U` (ghost depth `ng`) into the cuda tensor
+    `out` (5, nz, ny, nx): amrs_plot_derive_box."""
+    nz, ny, nx = (s - 2 * ng for s in U.shape[1:])
+    bx = c_box(lo, (nx, ny, nz))
+    cl = c_closures(closures)
+    check(load().amrs_plot_derive_box(ctypes.byref(cl), ctypes.byref(bx), array4(U, lo, ng), array4(out, lo, 0),
+                                      _stream_ptr(stream)), "amrs_plot_derive_box")
+    return out

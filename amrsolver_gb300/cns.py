@@ -160,6 +160,15 @@ class CNSLevel:
         d["totals"] = self.totals().tolist()
         return d
 
+    def write_plotfile(self, path, step=0, derive=None, prob_lo=(0.0, 0.0, 0.0)):
+        """CNS::writePlotFile of this single-box level (src/CNS.cpp:644-874):
+        the state and the derived quantities `derive` (default all of
+        pressure, temperature, x/y/z_velocity) at the current time."""
+        from . import plotfile
+        box = (self.lo, self.n)
+        return plotfile.write_plotfile(path, [box], [self.S], self.closures, self.dx, prob_lo, box, self.time, step,
+                                       plotfile.DERIVED_NAMES if derive is None else derive)
+
     def run(self, stop_time, max_step, cfl=None, dt=None):
         """The reference's main loop (src/main.cpp:66-75) for one level."""
         steps = 0

@@ -153,6 +153,9 @@ cudaError_t launch_ddiv_check(unsigned long long seed, long long count, unsigned
 // dsqrt_rn (ddiv.cuh) against the hardware square root over `count` generated operands
 cudaError_t launch_dsqrt_check(unsigned long long seed, long long count, unsigned long long* bad, double* first,
                                int nsm, cudaStream_t st);
+// derived plot variables (pressure, temperature, velocities) of one box's valid cells
+cudaError_t launch_plot_derive(const DArr& U, const DArr& O, const int lo[3], const int n[3], double gamma, double cv,
+                               int nsm, cudaStream_t st);
 // amrex::average_down of cell-centred data (coarse box lo, extents n, ratio r).
 cudaError_t launch_avgdown(const DArr& fine, const DArr& crse, const int lo[3], const int n[3], const int r[3],
                            int scomp, int ncomp, double volfrac, int nsm, cudaStream_t st);

@@ -950,6 +950,22 @@ amrs_status amrs_average_down(const amrs_box* crse_box, const int32_t ratio[3], 
   return AMRS_OK;
 }
 
+amrs_status amrs_plot_derive_box(const amrs_closures* closures, const amrs_box* bx, amrs_array4 state, amrs_array4 out,
+                                 void* stream) {
+  if (!closures || !bx) return AMRS_ERR_NULL;
+  if (!box_ok(*bx)) return AMRS_ERR_BOX;
+  if (!covers(state, *bx, 0, NCONS) || !covers(out, *bx, 0, 5)) return AMRS_ERR_LAYOUT;
+  if (!(closures->cv > 0.0)) return AMRS_ERR_SCHEME;
+  int dev = 0, nsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int lo[3] = {bx->lo[0], bx->lo[1], bx->lo[2]};
+  const int n[3] = {bn(*bx, 0), bn(*bx, 1), bn(*bx, 2)};
+  CK(launch_plot_derive(to_darr(state), to_darr(out), lo, n, closures->gamma, closures->cv, nsm,
+                        static_cast<cudaStream_t>(stream)));
+  return AMRS_OK;
+}
+
 amrs_status amrs_est_timestep_box(amrs_handle* h, const amrs_box* bx, const double dx[3], double cfl,
                                   amrs_array4 state, double* dt_device, void* stream) {
   if (!h || !bx || !dx || !dt_device) return AMRS_ERR_NULL;

@@ -791,6 +791,40 @@ cudaError_t launch_dsqrt_check(unsigned long long seed, long long count, unsigne
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------- plot fields ----
+// The derived plot variables of CNS (src/set/CNS_setup.cpp:153-176) over the
+// valid cells of one box, in the operation order of their derive functions
+// (src/cls/CNS_K.h:76-129): pressure (derpres), temperature (dertemp, from
+// the internal energy and cv, not from p / (rho R)) and the three
+// velocities (dervel: momentum / density).  out: 5 components in that order.
+__global__ void __launch_bounds__(256) plot_derive_kernel(DArr U, DArr O, int lo0, int lo1, int lo2, int nx,
+                                                          int ny, long long total, double gamma, double cv) {
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+       g += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(g % nx) + lo0;
+    const long long t = g / nx;
+    const int j = (int)(t % ny) + lo1, k = (int)(t / ny) + lo2;
+    const double rho = U(i, j, k, URHO), mx = U(i, j, k, UMX), my = U(i, j, k, UMY), mz = U(i, j, k, UMZ);
+    const double rhoinv = ddiv_rn(1.0, rho);
+    const double rhoeint = U(i, j, k, UET) - 0.5 * rhoinv * (mx * mx + my * my + mz * mz);
+    O(i, j, k, 0) = (gamma - 1.0) * rhoeint;
+    O(i, j, k, 1) = ddiv_rn(rhoeint * rhoinv, cv);
+    O(i, j, k, 2) = ddiv_rn(mx, rho);
+    O(i, j, k, 3) = ddiv_rn(my, rho);
+    O(i, j, k, 4) = ddiv_rn(mz, rho);
+  }
+}
+
+cudaError_t launch_plot_derive(const DArr& U, const DArr& O, const int lo[3], const int n[3], double gamma, double cv,
+                               int nsm, cudaStream_t st) {
+  const long long total = (long long)n[0] * n[1] * n[2];
+  long long blocks = (total + 255) / 256;
+  if (blocks > (long long)nsm * 8) blocks = (long long)nsm * 8;
+  if (blocks < 1) blocks = 1;
+  plot_derive_kernel<<<(int)blocks, 256, 0, st>>>(U, O, lo[0], lo[1], lo[2], n[0], n[1], total, gamma, cv);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------ average_down ----
 // amrex::average_down of cell-centred data on a Cartesian grid (called by
 // CNS::avgDown, src/CNS.cpp:513-530): each coarse cell of the box becomes

@@ -230,6 +230,15 @@ amrs_status amrs_fill_halo_box_bcnormal(const amrs_box* domain, const int32_t bc
  * result to *dt_device (device pointer) without a host sync. */
 amrs_status amrs_est_timestep_box(amrs_handle* h, const amrs_box* bx, const double dx[3], double cfl,
                                   amrs_array4 state, double* dt_device, void* stream);
+/* The derived plot variables of the reference's plotfiles
+ * (src/set/CNS_setup.cpp:153-176, written by CNS::writePlotFile,
+ * src/CNS.cpp:644-874) over the valid cells of `bx`: out components 0..4 =
+ * pressure (derpres), temperature (dertemp: internal energy / (rho cv)), x, y
+ * and z velocity (dervel: momentum / density), in the operation order of
+ * src/cls/CNS_K.h:76-129.  Runs on the current device; asynchronous on
+ * `stream`. */
+amrs_status amrs_plot_derive_box(const amrs_closures* closures, const amrs_box* bx, amrs_array4 state, amrs_array4 out,
+                                 void* stream);
 /* amrs_boxlist_prim_stats for one box's state (valid cells of `state`, the
  * same 21 doubles into `out`, device memory).  Asynchronous on `stream`. */
 amrs_status amrs_prim_stats_box(amrs_handle* h, const amrs_box* bx, const double dx[3], amrs_array4 state, double dt,

@@ -1329,6 +1329,31 @@ int orc_prim_stats(const OrcClosures* c, const int* lo, const int* hi, const dou
   return 0;
 }
 
+// The derived plot variables of CNS::writePlotFile (src/set/CNS_setup.cpp:
+// 153-176) over the valid cells of one ghosted box, in the operation order
+// of derpres, dertemp and dervel (src/cls/CNS_K.h:76-129).  out (valid box,
+// 5 components): pressure, temperature, x, y, z velocity.
+int orc_plot_derive(const OrcClosures* c, const int* lo, const int* hi, const double* U, double* out) {
+  if (!c || !lo || !hi || !U || !out) return 1;
+  const Box b = to_box(lo, hi);
+  Arr<double> u = make_arr<double>(const_cast<double*>(U), b, NGHOST);
+  Arr<double> o = make_arr<double>(out, b, 0);
+  const double gamma = c->gamma, cv = c->cv;
+  for (int k = b.lo[2]; k <= b.hi[2]; ++k)
+    for (int j = b.lo[1]; j <= b.hi[1]; ++j)
+      for (int i = b.lo[0]; i <= b.hi[0]; ++i) {
+        const double rhoinv = 1.0 / u(i, j, k, URHO);
+        const double mx = u(i, j, k, UMX), my = u(i, j, k, UMY), mz = u(i, j, k, UMZ);
+        const double rhoeint = u(i, j, k, UET) - 0.5 * rhoinv * (mx * mx + my * my + mz * mz);
+        o(i, j, k, 0) = (gamma - 1.0) * rhoeint;
+        o(i, j, k, 1) = (rhoeint * rhoinv) / cv;
+        o(i, j, k, 2) = u(i, j, k, UMX) / u(i, j, k, URHO);
+        o(i, j, k, 3) = u(i, j, k, UMY) / u(i, j, k, URHO);
+        o(i, j, k, 4) = u(i, j, k, UMZ) / u(i, j, k, URHO);
+      }
+  return 0;
+}
+
 // Number of stages of an RK variant, or -1 if the reference rejects it.
 int orc_rk_nstages(int order_rk, int stages_rk) {
   StageProg st[8];

@@ -102,6 +102,9 @@ class Oracle:
             L.orc_compute_rhs_count.argtypes = [ctypes.POINTER(CScheme), ctypes.POINTER(CClosures), ip,
                                                 ip, dp, dp, ctypes.POINTER(ctypes.c_longlong)]
             L.orc_compute_rhs_count.restype = ctypes.c_int
+        if hasattr(L, "orc_plot_derive"):
+            L.orc_plot_derive.argtypes = [ctypes.POINTER(CClosures), ip, ip, dp, dp]
+            L.orc_plot_derive.restype = ctypes.c_int
         if hasattr(L, "orc_prim_stats"):
             L.orc_prim_stats.argtypes = [ctypes.POINTER(CClosures), ip, ip, dp, dp, ctypes.c_double, dp]
             L.orc_prim_stats.restype = ctypes.c_int
@@ -197,6 +200,18 @@ class Oracle:
                                      float(dt), _ptr(out))
         if rc:
             raise RuntimeError("orc_prim_stats failed: %d" % rc)
+        return out
+
+    def plot_derive(self, closures, U, lo=(0, 0, 0)):
+        """Derived plot variables (pressure, temperature, x/y/z velocity) of
+        one ghosted box's valid cells: (5, nz, ny, nx)."""
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        nz, ny, nx = (s - 2 * NG for s in U.shape[1:])
+        hi = (lo[0] + nx - 1, lo[1] + ny - 1, lo[2] + nz - 1)
+        out = np.empty((5, nz, ny, nx))
+        rc = self.lib.orc_plot_derive(ctypes.byref(c_closures(closures)), _i3(lo), _i3(hi), _ptr(U), _ptr(out))
+        if rc:
+            raise RuntimeError("orc_plot_derive failed: %d" % rc)
         return out
 
     def fill_halo(self, U, bc_lo, bc_hi, lo=(0, 0, 0)):

@@ -362,4 +362,38 @@ int orc_prim_stats(const OrcClosures* c, const int* lo, const int* hi, const dou
   return 0;
 }
 
+// The reference's own derive functions of its plotfiles (derpres, dertemp,
+// dervel: src/cls/CNS_K.h:76-129, registered at src/set/CNS_setup.cpp:153-176)
+// on one ghosted box's valid cells; out as orc_plot_derive's.
+int orc_plot_derive(const OrcClosures* c, const int* lo, const int* hi, const double* U, double* out) {
+  if (int rc = set_closures(c)) return rc;
+  Box bx(IntVect(lo[0], lo[1], lo[2]), IntVect(hi[0], hi[1], hi[2]));
+  Box gb = grow(bx, NGHOST);
+  Array4<const Real> u(const_cast<double*>(U), {gb.lo[0], gb.lo[1], gb.lo[2]},
+                       {gb.hi[0] + 1, gb.hi[1] + 1, gb.hi[2] + 1}, NCONS);
+  FArrayBox dat(bx, NCONS), der(bx, 5);
+  Array4<Real> d = dat.array();
+  for (int n = 0; n < NCONS; ++n)
+    for (int k = bx.lo[2]; k <= bx.hi[2]; ++k)
+      for (int j = bx.lo[1]; j <= bx.hi[1]; ++j)
+        for (int i = bx.lo[0]; i <= bx.hi[0]; ++i) d(i, j, k, n) = u(i, j, k, n);
+  Geometry geom;
+  derpres(bx, der, 0, 1, dat, geom, 0.0, nullptr, 0);
+  dertemp(bx, der, 1, 1, dat, geom, 0.0, nullptr, 0);
+  for (int v = 0; v < 3; ++v) {
+    // dervel reads (density, momentum component) as its components 0 and 1
+    FArrayBox dv(bx, 2);
+    Array4<Real> a = dv.array();
+    for (int k = bx.lo[2]; k <= bx.hi[2]; ++k)
+      for (int j = bx.lo[1]; j <= bx.hi[1]; ++j)
+        for (int i = bx.lo[0]; i <= bx.hi[0]; ++i) {
+          a(i, j, k, 0) = u(i, j, k, URHO);
+          a(i, j, k, 1) = u(i, j, k, UMX + v);
+        }
+    dervel(bx, der, 2 + v, 1, dv, geom, 0.0, nullptr, 0);
+  }
+  std::memcpy(out, der.data.data(), der.data.size() * sizeof(double));
+  return 0;
+}
+
 }  // extern "C"

@@ -105,3 +105,14 @@ def test_prim_stats_bitexact(orc, seed):
     b = REF.prim_stats(CL, U, dx, dt, lo=lo)
     np.testing.assert_array_equal(a, b)
     assert np.all(a[:6] <= a[6:12]) and np.all(a[12:] > 0)
+
+
+@pytest.mark.parametrize("seed", [4, 5])
+def test_plot_derive_bitexact(orc, seed):
+    """The plotfile's derived variables: the reference's own derpres, dertemp
+    and dervel (src/cls/CNS_K.h:76-129) against the restatement."""
+    rng = np.random.default_rng(seed)
+    n = tuple(int(v) for v in rng.integers(3, 8, 3))
+    U = P.random_state(n, seed=seed + 70, amp=0.3)
+    lo = tuple(int(v) for v in rng.integers(-4, 4, 3))
+    np.testing.assert_array_equal(orc.plot_derive(CL, U, lo=lo), REF.plot_derive(CL, U, lo=lo))

@@ -17,15 +17,15 @@ __device__ __forceinline__ void cons2prim_vjp(const BoxRec& R, const DClosures& 
   const double rho = Q.p[oq + QRHO * Q.ns], u = Q.p[oq + QU * Q.ns], v = Q.p[oq + QV * Q.ns],
                w = Q.p[oq + QW * Q.ns], T = Q.p[oq + QT * Q.ns];
   double rb = qb[QRHO], ub = qb[QU], vb = qb[QV], wb = qb[QW];
-  const double pb = qb[QPRES] + qb[QT] / (rho * cl.Rspec);
-  rb += -qb[QT] * T / rho;
+  const double pb = qb[QPRES] + ddiv_rn(qb[QT], (rho * cl.Rspec));
+  rb += ddiv_rn(-qb[QT] * T, rho);
   const double eib = (cl.gamma - 1.0) * pb;  // d/d rhoei
   const double keb = -eib;                   // d/d rhoke
   rb += 0.5 * (u * u + v * v + w * w) * keb;
   ub += rho * u * keb;
   vb += rho * v * keb;
   wb += rho * w * keb;
-  const double rinv = 1.0 / rho;
+  const double rinv = ddiv_rn(1.0, rho);
   rb += -(ub * u + vb * v + wb * w) * rinv;
   const DArr U = R.slot[0];
   const double rho_raw = U(i, j, k, URHO);
@@ -59,13 +59,13 @@ __device__ __forceinline__ void weno5js_grad(const double s[5], double gr[5], do
   const double DP = (t0 + t1 + t2) * (e0 * q0);
   double w0, w1, w2, we0, we1, we2;  // w_k and w_k / e_k
   if (DP > 1e-300 && DP < 1e300) {
-    const double r = 1.0 / DP, rP = r * (e0 * q0);
+    const double r = ddiv_rn(1.0, DP), rP = r * (e0 * q0);
     w0 = t0 * rP; w1 = t1 * rP; w2 = t2 * rP;
     we0 = (t0 * q0) * r; we1 = (t1 * q1) * r; we2 = (t2 * q2) * r;
   } else {
-    const double ie0 = 1.0 / e0, ie1 = 1.0 / e1, ie2 = 1.0 / e2;
+    const double ie0 = ddiv_rn(1.0, e0), ie1 = ddiv_rn(1.0, e1), ie2 = ddiv_rn(1.0, e2);
     const double a0 = 0.1 * ie0 * ie0, a1 = 0.6 * ie1 * ie1, a2 = 0.3 * ie2 * ie2;
-    const double iA = 1.0 / (a0 + a1 + a2);
+    const double iA = ddiv_rn(1.0, (a0 + a1 + a2));
     w0 = a0 * iA; w1 = a1 * iA; w2 = a2 * iA;
     we0 = w0 * ie0; we1 = w1 * ie1; we2 = w2 * ie2;
   }

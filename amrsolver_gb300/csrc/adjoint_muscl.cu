@@ -161,9 +161,9 @@ __global__ void __launch_bounds__(256) muscl_vjp_slope_kernel(BoxTable tb, FaceR
     const double d1l = Q(o, QT1) - Q(o - s, QT1), d1r = Q(o + s, QT1) - Q(o, QT1);
     const double d2l = Q(o, QT2) - Q(o - s, QT2), d2r = Q(o + s, QT2) - Q(o, QT2);
     const double cs2 = cs * cs;
-    const double l0 = 0.5 * dpl / cs - 0.5 * rc * dul, r0 = 0.5 * dpr / cs - 0.5 * rc * dur;
-    const double l1 = drl - dpl / cs2, r1 = drr - dpr / cs2;
-    const double l2 = 0.5 * dpl / cs + 0.5 * rc * dul, r2 = 0.5 * dpr / cs + 0.5 * rc * dur;
+    const double l0 = ddiv_rn(0.5 * dpl, cs) - 0.5 * rc * dul, r0 = ddiv_rn(0.5 * dpr, cs) - 0.5 * rc * dur;
+    const double l1 = drl - ddiv_rn(dpl, cs2), r1 = drr - ddiv_rn(dpr, cs2);
+    const double l2 = ddiv_rn(0.5 * dpl, cs) + 0.5 * rc * dul, r2 = ddiv_rn(0.5 * dpr, cs) + 0.5 * rc * dur;
     auto mc = [](double a, double b) {
       const double dcen = 0.5 * (a + b);
       const double dsgn = copysign(1.0, dcen);
@@ -198,17 +198,17 @@ __global__ void __launch_bounds__(256) muscl_vjp_slope_kernel(BoxTable tb, FaceR
       Bb += f[6 * n]; d3b += f[8 * n]; d4b += f[9 * n];
     }
     // A = s02/csr + d1, B = (d2 - d0)/rho, C = s02*csr (z: A_L, C_L with csl)
-    double s02b = Ab / csr + Cb * csr;
-    double csrb = -Ab * (s02 / csr) / csr + Cb * s02;
+    double s02b = ddiv_rn(Ab, csr) + Cb * csr;
+    double csrb = ddiv_rn(-Ab * (ddiv_rn(s02, csr)), csr) + Cb * s02;
     double d1b = Ab + ALb;
-    double d0b = -Bb / rc, d2b = Bb / rc;
-    double rcb = -Bb * ((d2 - d0) / rc) / rc;
+    double d0b = ddiv_rn(-Bb, rc), d2b = ddiv_rn(Bb, rc);
+    double rcb = ddiv_rn(-Bb * (ddiv_rn((d2 - d0), rc)), rc);
     double csl = 0.0, c0l = 0.0, cslb = 0.0;
     if (d == 2 && c <= R.hi[2]) {
       c0l = sqrt(gR * Q(o + 2 * s, QT));
       csl = c0l + 1.e-40;
-      s02b += ALb / csl + CLb * csl;
-      cslb = -ALb * (s02 / csl) / csl + CLb * s02;
+      s02b += ddiv_rn(ALb, csl) + CLb * csl;
+      cslb = ddiv_rn(-ALb * (ddiv_rn(s02, csl)), csl) + CLb * s02;
     }
     d0b += s02b;
     d2b += s02b;
@@ -222,15 +222,15 @@ __global__ void __launch_bounds__(256) muscl_vjp_slope_kernel(BoxTable tb, FaceR
     mc_vjp(d2l, d2r, d4b, l4b, r4b);
     // characteristic differences
     double csb = 0.0;
-    double dplb = 0.5 * (l0b + l2b) / cs - l1b / cs2, dprb = 0.5 * (r0b + r2b) / cs - r1b / cs2;
-    csb += -0.5 * (l0b + l2b) * dpl / cs2 - 0.5 * (r0b + r2b) * dpr / cs2;
-    csb += 2.0 * (l1b * dpl + r1b * dpr) / (cs2 * cs);
+    double dplb = ddiv_rn(0.5 * (l0b + l2b), cs) - ddiv_rn(l1b, cs2), dprb = ddiv_rn(0.5 * (r0b + r2b), cs) - ddiv_rn(r1b, cs2);
+    csb += ddiv_rn(-0.5 * (l0b + l2b) * dpl, cs2) - ddiv_rn(0.5 * (r0b + r2b) * dpr, cs2);
+    csb += ddiv_rn(2.0 * (l1b * dpl + r1b * dpr), (cs2 * cs));
     const double dulb = 0.5 * rc * (l2b - l0b), durb = 0.5 * rc * (r2b - r0b);
     rcb += 0.5 * ((l2b - l0b) * dul + (r2b - r0b) * dur);
     const double drlb = l1b, drrb = r1b;
     // c0 = sqrt(gamma R T)
     const double c0b = csb + csrb;
-    double Tb = (c0 > 0.0) ? c0b * gR / (2.0 * c0) : 0.0;
+    double Tb = (c0 > 0.0) ? ddiv_rn(c0b * gR, (2.0 * c0)) : 0.0;
     // Qbar at c-1 (m), c (z), c+1 (p), NQA order (rho, u, v, w, T, p)
     double qm[NQA] = {0, 0, 0, 0, 0, 0}, qz[NQA], qp[NQA] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(256) muscl_vjp_slope_kernel(BoxTable tb, FaceR
       w[(NQA + m) * n] = qz[m];
       w[(2 * NQA + m) * n] = qp[m];
     }
-    w[(3 * NQA) * n] = (d == 2 && c <= R.hi[2] && c0l > 0.0) ? cslb * gR / (2.0 * c0l) : 0.0;
+    w[(3 * NQA) * n] = (d == 2 && c <= R.hi[2] && c0l > 0.0) ? ddiv_rn(cslb * gR, (2.0 * c0l)) : 0.0;
   }
 }
 

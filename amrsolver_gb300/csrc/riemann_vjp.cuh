@@ -29,8 +29,8 @@ struct RPPar {
 
 AMRS_HD void rp_iter_fwd(const RPPar& q, double P, double Pm, double UM, double UP, double& Pn,
                                             double& UMn, double& UPn) {
-  const double wl = 1. / sqrt((q.hg * (P + q.pl) + P) * q.rl);
-  const double wr = 1. / sqrt((q.hg * (P + q.pr) + P) * q.rr);
+  const double wl = ddiv_rn(1., sqrt((q.hg * (P + q.pl) + P) * q.rl));
+  const double wr = ddiv_rn(1., sqrt((q.hg * (P + q.pr) + P) * q.rr));
   UMn = q.ur - (q.pr - P) * wr;
   UPn = q.ul + (q.pl - P) * wl;
   const double dpd = fabs(Pm - P);
@@ -39,7 +39,7 @@ AMRS_HD void rp_iter_fwd(const RPPar& q, double P, double Pm, double UM, double 
   double zm = fabs(UMn - UM);
   if (zm - 1.e-3 * q.cright < 0.0) zm = dpd * wr;
   const double zz = zp + zm;
-  const double denom = dpd / ((zz < q.ccs) ? q.ccs : zz);
+  const double denom = ddiv_rn(dpd, ((zz < q.ccs) ? q.ccs : zz));
   const double pn = P - denom * (UMn - UPn);
   Pn = (pn < q.smallp) ? q.smallp : pn;
 }
@@ -54,7 +54,7 @@ AMRS_HD void rp_iter_vjp(const RPPar& q, double P, double Pm, double UM, double 
                                             double& UMb, double& UPb, RPBar& g) {
   const double al = q.hg * (P + q.pl) + P, ar = q.hg * (P + q.pr) + P;
   const double sl = sqrt(al * q.rl), sr = sqrt(ar * q.rr);
-  const double wl = 1. / sl, wr = 1. / sr;
+  const double wl = ddiv_rn(1., sl), wr = ddiv_rn(1., sr);
   const double UMn = q.ur - (q.pr - P) * wr;
   const double UPn = q.ul + (q.pl - P) * wl;
   const double draw = Pm - P, dpd = fabs(draw);
@@ -67,7 +67,7 @@ AMRS_HD void rp_iter_vjp(const RPPar& q, double P, double Pm, double UM, double 
   const double zz = zp + zm;
   const bool bz = zz < q.ccs;
   const double den = bz ? q.ccs : zz;
-  const double denom = dpd / den;
+  const double denom = ddiv_rn(dpd, den);
   const double pn = P - denom * (UMn - UPn);
   const bool bpn = pn < q.smallp;
   // reverse
@@ -78,8 +78,8 @@ AMRS_HD void rp_iter_vjp(const RPPar& q, double P, double Pm, double UM, double 
   const double denomb = -pnb * (UMn - UPn);
   UMnbar += -pnb * denom;
   UPnbar += pnb * denom;
-  dpdb += denomb / den;
-  const double denb = -denomb * denom / den;
+  dpdb += ddiv_rn(denomb, den);
+  const double denb = ddiv_rn(-denomb * denom, den);
   if (bz) g.ccs += denb;
   const double zzb = bz ? 0.0 : denb;
   if (bp) { dpdb += zzb * wl; wlb += zzb * dpd; }
@@ -100,7 +100,7 @@ AMRS_HD void rp_iter_vjp(const RPPar& q, double P, double Pm, double UM, double 
   wlb += UPnbar * (q.pl - P);
   // w = 1/sqrt(a r), a = hg (P + p) + P
   const double slb = -wlb * wl * wl, srb = -wrb * wr * wr;
-  const double wlsqb = slb / (2.0 * sl), wrsqb = srb / (2.0 * sr);
+  const double wlsqb = ddiv_rn(slb, (2.0 * sl)), wrsqb = ddiv_rn(srb, (2.0 * sr));
   g.rl += wlsqb * al;
   g.rr += wrsqb * ar;
   const double alb = wlsqb * q.rl, arb = wrsqb * q.rr;
@@ -122,19 +122,19 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
   // ---- forward
   const double clsql = gamma * pl * rl, clsqr = gamma * pr * rr;
   const double wl0 = sqrt(clsql), wr0 = sqrt(clsqr);
-  const double cleft = wl0 / rl, cright = wr0 / rr;
+  const double cleft = ddiv_rn(wl0, rl), cright = ddiv_rn(wr0, rr);
   const double ccs = small * (cleft + cright);
   const double dU = ur - ul;
   const double D0 = wl0 + wr0;
-  const double ps0 = (wl0 * pr + wr0 * pl - wr0 * wl0 * dU) / D0;
+  const double ps0 = ddiv_rn((wl0 * pr + wr0 * pl - wr0 * wl0 * dU), D0);
   const bool m0 = !(ps0 < smallp);
   const double p0 = m0 ? ps0 : smallp;
   const double a1l = hg * (p0 + pl) + p0, a1r = hg * (p0 + pr) + p0;
   const double wl1 = sqrt(a1l * rl), wr1 = sqrt(a1r * rr);
-  const double usp0 = ul - (p0 - pl) / wl1;
-  const double usm0 = ur + (p0 - pr) / wr1;
+  const double usp0 = ul - ddiv_rn((p0 - pl), wl1);
+  const double usm0 = ur + ddiv_rn((p0 - pr), wr1);
   const double D1 = wl1 + wr1;
-  const double ps1 = (wl1 * pr + wr1 * pl - wr1 * wl1 * dU) / D1;
+  const double ps1 = ddiv_rn((wl1 * pr + wr1 * pl - wr1 * wl1 * dU), D1);
   const bool m1 = !(ps1 < smallp);
   const double p1 = m1 ? ps1 : smallp;
   const RPPar q{pl, pr, ul, ur, rl, rr, hg, cleft, cright, ccs, smallp};
@@ -152,25 +152,25 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
   if (side == 0) { ro = rl; uo = ul; po = pl; sgnm = 1.; utr1 = ut1l; utr2 = ut2l; }
   else if (side == 1) { ro = rr; uo = ur; po = pr; sgnm = -1.; utr1 = ut1r; utr2 = ut2r; }
   else {
-    uo = 0.5 * (ur + ul); po = 0.5 * (pr + pl); ro = 2. * (rl * rr) / (rl + rr); sgnm = 1.;
+    uo = 0.5 * (ur + ul); po = 0.5 * (pr + pl); ro = ddiv_rn(2. * (rl * rr), (rl + rr)); sgnm = 1.;
     utr1 = 0.5 * (ut1l + ut1r); utr2 = 0.5 * (ut2l + ut2r);
   }
   const double aw = hg * (pstar + po) + pstar;
   const double wosq = aw * ro;
   const double dpjmp = pstar - po;
-  const double tt = ro * dpjmp, uu = tt / wosq, dd = 1. - uu;
-  const double rstar = ro / dd;
+  const double tt = ro * dpjmp, uu = ddiv_rn(tt, wosq), dd = 1. - uu;
+  const double rstar = ddiv_rn(ro, dd);
   const double suo = sgnm * uo;
   // kind: 0 side state, 1 star state, 2 mixed (rarefaction fan)
   int kind;
   double spin = 0.0, spout = 0.0, co = 0.0, cstar = 0.0;
   if (pstar >= po) {
-    spin = sqrt(wosq) / ro - suo;
+    spin = ddiv_rn(sqrt(wosq), ro) - suo;
     kind = (spin < 0.) ? 0 : ((spin >= 0.) ? 1 : 2);
     spout = spin;
   } else {
-    co = sqrt(gamma * po / ro);
-    cstar = sqrt(gamma * pstar / rstar);
+    co = sqrt(ddiv_rn(gamma * po, ro));
+    cstar = sqrt(ddiv_rn(gamma * pstar, rstar));
     spout = co - suo;
     spin = cstar - suo;
     kind = (spout < 0.) ? 0 : ((spin >= 0.) ? 1 : 2);
@@ -183,7 +183,7 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
     ssv = bab ? b : a;
     bss = ssv < ccs;
     den2 = bss ? ccs : ssv;
-    frac = 0.5 * (1. + (spin + spout) / den2);
+    frac = 0.5 * (1. + ddiv_rn((spin + spout), den2));
   }
   double rg, ug, pg;
   if (kind == 0) { rg = ro; ug = uo; pg = po; }
@@ -195,13 +195,13 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
   }
   // ---- reverse of the fluxes
   const double K = ug * ug + utr1 * utr1 + utr2 * utr2;
-  const double E = 0.5 * rg * K + pg / (gamma - 1.) + pg;
+  const double E = 0.5 * rg * K + ddiv_rn(pg, (gamma - 1.)) + pg;
   double rgb = fb[0] * ug + fb[1] * ug * ug + fb[2] * ug * utr1 + fb[3] * ug * utr2 + fb[4] * ug * 0.5 * K;
   double ugb = fb[0] * rg + fb[1] * 2.0 * rg * ug + fb[2] * rg * utr1 + fb[3] * rg * utr2 +
                fb[4] * (E + ug * rg * ug);
   double t1b = fb[2] * rg * ug + fb[4] * ug * rg * utr1;
   double t2b = fb[3] * rg * ug + fb[4] * ug * rg * utr2;
-  double pgb = fb[1] + fb[4] * ug * (1.0 / (gamma - 1.) + 1.0);
+  double pgb = fb[1] + fb[4] * ug * (ddiv_rn(1.0, (gamma - 1.)) + 1.0);
   // ---- reverse of the selection
   double rob = 0.0, uob = 0.0, pob = 0.0, rstarb = 0.0, ustarb = 0.0, pstarb = 0.0, ccsb = 0.0;
   if (kind == 0) { rob += rgb; uob += ugb; pob += pgb; }
@@ -211,8 +211,8 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
     ustarb += frac * ugb; uob += (1. - frac) * ugb;
     pstarb += frac * pgb; pob += (1. - frac) * pgb;
     const double fracb = rgb * (rstar - ro) + ugb * (ustar - uo) + pgb * (pstar - po);
-    const double qb = 0.5 * fracb / den2;
-    const double den2b = -0.5 * fracb * (spin + spout) / (den2 * den2);
+    const double qb = ddiv_rn(0.5 * fracb, den2);
+    const double den2b = ddiv_rn(-0.5 * fracb * (spin + spout), (den2 * den2));
     double ab = 0.0, bb = 0.0;
     if (bss) ccsb += den2b;
     else if (bab) bb += den2b;
@@ -224,21 +224,21 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
       const double cob = spoutb, cstarb = spinb;
       const double suob = -spoutb - spinb;
       uob += suob * sgnm;
-      const double xb = cob / (2.0 * co);
-      pob += xb * gamma / ro;
-      rob += -xb * gamma * po / (ro * ro);
-      const double yb = cstarb / (2.0 * cstar);
-      pstarb += yb * gamma / rstar;
-      rstarb += -yb * gamma * pstar / (rstar * rstar);
+      const double xb = ddiv_rn(cob, (2.0 * co));
+      pob += ddiv_rn(xb * gamma, ro);
+      rob += ddiv_rn(-xb * gamma * po, (ro * ro));
+      const double yb = ddiv_rn(cstarb, (2.0 * cstar));
+      pstarb += ddiv_rn(yb * gamma, rstar);
+      rstarb += ddiv_rn(-yb * gamma * pstar, (rstar * rstar));
     }
   }
   // rstar = ro / (1 - ro dpjmp / wosq), wosq = (hg (pstar + po) + pstar) ro
   {
-    rob += rstarb / dd;
-    const double ddb = -rstarb * rstar / dd;
+    rob += ddiv_rn(rstarb, dd);
+    const double ddb = ddiv_rn(-rstarb * rstar, dd);
     const double uub = -ddb;
-    const double ttb = uub / wosq;
-    const double wosqb = -uub * uu / wosq;
+    const double ttb = ddiv_rn(uub, wosq);
+    const double wosqb = ddiv_rn(-uub * uu, wosq);
     rob += ttb * dpjmp;
     const double dpb = ttb * ro;
     pstarb += dpb;
@@ -255,8 +255,8 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
     inb[6] += 0.5 * uob; inb[1] += 0.5 * uob;
     inb[7] += 0.5 * pob; inb[2] += 0.5 * pob;
     const double s = rl + rr;
-    inb[0] += rob * 2.0 * rr * rr / (s * s);
-    inb[5] += rob * 2.0 * rl * rl / (s * s);
+    inb[0] += ddiv_rn(rob * 2.0 * rr * rr, (s * s));
+    inb[5] += ddiv_rn(rob * 2.0 * rl * rl, (s * s));
     inb[3] += 0.5 * t1b; inb[8] += 0.5 * t1b;
     inb[4] += 0.5 * t2b; inb[9] += 0.5 * t2b;
   }
@@ -274,22 +274,22 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
   double p0b = Pmnb;
   {
     const double ps1b = m1 ? Pnb : 0.0;
-    const double N1b = ps1b / D1, D1b = -ps1b * ps1 / D1;
+    const double N1b = ddiv_rn(ps1b, D1), D1b = ddiv_rn(-ps1b * ps1, D1);
     double wl1b = N1b * (pr - wr1 * dU) + D1b, wr1b = N1b * (pl - wl1 * dU) + D1b;
     g.pr += N1b * wl1;
     g.pl += N1b * wr1;
     dUb += -N1b * wr1 * wl1;
     // usm0 = ur + (p0 - pr)/wr1;  usp0 = ul - (p0 - pl)/wl1
     g.ur += UMnb;
-    p0b += UMnb / wr1;
-    g.pr -= UMnb / wr1;
-    wr1b += -UMnb * (p0 - pr) / (wr1 * wr1);
+    p0b += ddiv_rn(UMnb, wr1);
+    g.pr -= ddiv_rn(UMnb, wr1);
+    wr1b += ddiv_rn(-UMnb * (p0 - pr), (wr1 * wr1));
     g.ul += UPnb;
-    p0b -= UPnb / wl1;
-    g.pl += UPnb / wl1;
-    wl1b += UPnb * (p0 - pl) / (wl1 * wl1);
+    p0b -= ddiv_rn(UPnb, wl1);
+    g.pl += ddiv_rn(UPnb, wl1);
+    wl1b += ddiv_rn(UPnb * (p0 - pl), (wl1 * wl1));
     // w1 = sqrt(a1 r), a1 = hg (p0 + p) + p0
-    const double wlsqb = wl1b / (2.0 * wl1), wrsqb = wr1b / (2.0 * wr1);
+    const double wlsqb = ddiv_rn(wl1b, (2.0 * wl1)), wrsqb = ddiv_rn(wr1b, (2.0 * wr1));
     g.rl += wlsqb * a1l;
     g.rr += wrsqb * a1r;
     const double alb = wlsqb * rl, arb = wrsqb * rr;
@@ -299,7 +299,7 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
   }
   {
     const double ps0b = m0 ? p0b : 0.0;
-    const double N0b = ps0b / D0, D0b = -ps0b * ps0 / D0;
+    const double N0b = ddiv_rn(ps0b, D0), D0b = ddiv_rn(-ps0b * ps0, D0);
     wl0b += N0b * (pr - wr0 * dU) + D0b;
     wr0b += N0b * (pl - wl0 * dU) + D0b;
     g.pr += N0b * wl0;
@@ -309,16 +309,16 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
   // ccs = small (cleft + cright), cleft = wl0 / rl, cright = wr0 / rr
   {
     const double cb = small * (ccsb + g.ccs);
-    wl0b += cb / rl;
-    g.rl += -cb * cleft / rl;
-    wr0b += cb / rr;
-    g.rr += -cb * cright / rr;
+    wl0b += ddiv_rn(cb, rl);
+    g.rl += ddiv_rn(-cb * cleft, rl);
+    wr0b += ddiv_rn(cb, rr);
+    g.rr += ddiv_rn(-cb * cright, rr);
   }
   g.ur += dUb;
   g.ul -= dUb;
   // w0 = sqrt(gamma p r)
   {
-    const double lb = wl0b / (2.0 * wl0), rb2 = wr0b / (2.0 * wr0);
+    const double lb = ddiv_rn(wl0b, (2.0 * wl0)), rb2 = ddiv_rn(wr0b, (2.0 * wr0));
     g.pl += lb * gamma * rl;
     g.rl += lb * gamma * pl;
     g.pr += rb2 * gamma * rr;

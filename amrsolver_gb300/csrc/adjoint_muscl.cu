@@ -55,7 +55,11 @@ struct SBuf {
   int mx, my;
 };
 
-__global__ void __launch_bounds__(256) muscl_vjp_face_kernel(BoxTable tb, FaceRec fr, DArr vbar, FBuf fs, int d,
+// Two CTAs per SM (128 registers): the reverse solver is a long dependent
+// chain per face, and 16 warps hide its latency better than 8 with all the
+// registers it would otherwise take (measured: 7.97 against 8.97 ms per
+// SSPRK3 step VJP at 64^3).
+__global__ void __launch_bounds__(256, 2) muscl_vjp_face_kernel(BoxTable tb, FaceRec fr, DArr vbar, FBuf fs, int d,
                                                              long long total) {
   const BoxRec& R = tb.box[0];
   const DArr q = R.q;

@@ -34,7 +34,10 @@ __device__ __forceinline__ double vget_r(const DArr& v, const BoxRec& R, int i, 
   return v(i, j, k, n);
 }
 
-__global__ void __launch_bounds__(256) wr_vjp_face_kernel(BoxTable tb, DArr vbar, RBuf rb, int d, long long total) {
+// Three CTAs per SM (85 registers, the rest spilled): 24 warps hide the
+// latency of the reverse solver's chain (measured: 11.96 against 13.96 ms
+// per SSPRK3 step VJP at 64^3 with the unconstrained 255 registers).
+__global__ void __launch_bounds__(256, 3) wr_vjp_face_kernel(BoxTable tb, DArr vbar, RBuf rb, int d, long long total) {
   const BoxRec& R = tb.box[0];
   const DArr q = R.q;
   const DClosures& cl = tb.cls[R.cl];

@@ -141,6 +141,8 @@ SIGNATURES = {
                                    ctypes.POINTER(ctypes.c_double)]),
     "amrs_debug_dsqrt_check": (_S, [_P, ctypes.c_uint64, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64),
                                     ctypes.POINTER(ctypes.c_double)]),
+    "amrs_debug_dmul_check": (_S, [_P, ctypes.c_uint64, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64),
+                                   ctypes.POINTER(ctypes.c_double)]),
     "amrs_probe_fp64_tflops_timed": (_S, [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_double)]),
     "amrs_debug_wait_timeout": (_S, [_P, ctypes.c_int32, _P]),
@@ -363,13 +365,14 @@ class Handle:
                                              int(reps), _stream_ptr(stream), ms), "amrs_profile_stage_box")
         return tuple(ms)
 
-    def ddiv_check(self, seed, count, sqrt=False):
+    def ddiv_check(self, seed, count, sqrt=False, mul=False):
         """(mismatches, first mismatch (a, b, hardware, library)) of the
-        integer-pipe division (or square root) against the hardware one on
-        the device."""
+        integer-pipe division (or square root, or product) against the
+        hardware one on the device."""
         nb = ctypes.c_int64()
         first = (ctypes.c_double * 4)()
-        fn = self._L.amrs_debug_dsqrt_check if sqrt else self._L.amrs_debug_ddiv_check
+        fn = (self._L.amrs_debug_dmul_check if mul else
+              self._L.amrs_debug_dsqrt_check if sqrt else self._L.amrs_debug_ddiv_check)
         check(fn(self.h, int(seed), int(count), ctypes.byref(nb), first), "amrs_debug_ddiv_check")
         return nb.value, tuple(first)
 

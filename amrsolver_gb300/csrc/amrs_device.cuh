@@ -81,29 +81,64 @@ __device__ __forceinline__ double rmax(double a, double b) { return (a < b) ? b 
 __device__ __forceinline__ double rmin(double a, double b) { return (b < a) ? b : a; }
 
 // cons2prim (src/rhs/CNS_hydro_K.h:15-34) plus QE = cv*T.
+// A product on the FP64 pipe (a * b) or, with I, the same correctly rounded
+// product formed on the integer pipe (dmul_rn).  The kernels of this path
+// are bound by the FP64 pipe while their integer pipe idles; the masks below
+// (one per routine, chosen by measurement) move part of their products
+// across without changing a bit of any result.
+template <bool I>
+__device__ __forceinline__ double kmul(double a, double b) {
+  return I ? dmul_rn(a, b) : a * b;
+}
+
+// cons2prim products on the integer pipe: bit 0 the velocities, 1 their
+// squares, 2 the kinetic-energy scalings, 3 pressure, rho R and e.
+#ifndef AMRS_C2P_IMUL
+#define AMRS_C2P_IMUL 0x02
+#endif
+#ifndef AMRS_VISC_IMUL
+#define AMRS_VISC_IMUL 0x17
+#endif
+#ifndef AMRS_PROG_IMUL
+#define AMRS_PROG_IMUL 0x0
+#endif
 __device__ __forceinline__ void cons2prim(const double u[5], double q[NQ], const DClosures& c) {
   double rho = rmax(1e-40, u[URHO]);
+  constexpr int M = AMRS_C2P_IMUL;
   double rhoinv = ddiv_rn(1.0, rho);
-  double ux = u[UMX] * rhoinv;
-  double uy = u[UMY] * rhoinv;
-  double uz = u[UMZ] * rhoinv;
-  double rhoke = 0.5 * rho * (ux * ux + uy * uy + uz * uz);
+  double ux = kmul<M & 1>(u[UMX], rhoinv);
+  double uy = kmul<M & 1>(u[UMY], rhoinv);
+  double uz = kmul<M & 1>(u[UMZ], rhoinv);
+  double rhoke = kmul<(M >> 2) & 1>(kmul<(M >> 2) & 1>(0.5, rho),
+                                    kmul<(M >> 1) & 1>(ux, ux) + kmul<(M >> 1) & 1>(uy, uy) +
+                                        kmul<(M >> 1) & 1>(uz, uz));
   double rhoei = (u[UET] - rhoke);
-  double p = (c.gamma - 1.0) * rhoei;
+  double p = kmul<(M >> 3) & 1>(c.gamma - 1.0, rhoei);
   q[QRHO] = rho;
   q[QU] = ux;
   q[QV] = uy;
   q[QW] = uz;
   q[QPRES] = p;
-  q[QT] = ddiv_rn(p, rho * c.Rspec);
-  q[QE] = c.cv * q[QT];
+  q[QT] = ddiv_rn(p, kmul<(M >> 3) & 1>(rho, c.Rspec));
+  q[QE] = kmul<(M >> 3) & 1>(c.cv, q[QT]);
 }
 
 // One KEEP pair term (src/rhs/CentralKEEP.h:19-36 helpers, :76-83 body),
 // already multiplied by its coefficient: the contribution of pair
 // (point 1 = larger index, point 2 = smaller index) to the face flux in
 // direction d.  q1/q2 give rho,u,v,w,T,p,e.
-template <int D>
+//
+// IM selects, bit by bit, the products formed on the integer pipe
+// (dmul_rn, the same correctly rounded product): 0 P, 1-3 the three
+// products of s3, 4-7 the momentum and energy cubic products, 8-9 the two
+// products of pu, 10-14 the coefficient scalings of the five components,
+// 15 P s3.  The FP64 pipe is the bound of the kernels calling this, and the
+// integer pipe is otherwise idle in them, so moving part of the products
+// there shortens the FP64 stream without changing a bit of the result.
+#ifndef AMRS_KEEP_IMUL
+#define AMRS_KEEP_IMUL 0x7C00
+#endif
+template <int D, int IM = AMRS_KEEP_IMUL>
 __device__ __forceinline__ void keep_pair(const double* q1, const double* q2, double coef, double T[5]) {
   constexpr int QN = QU + D;
   const double rhoS = q1[QRHO] + q2[QRHO];
@@ -119,19 +154,20 @@ __device__ __forceinline__ void keep_pair(const double* q1, const double* q2, do
   // So coef*(...) == (coef/8)*(...) with the eighths taken out, and no
   // FP64 instruction is spent on a power-of-two scaling.
   const double c8 = 0.125 * coef, c4 = 0.25 * coef;
-  const double P = rhoS * unS;
-  const double s3 = q1[QU] * q2[QU] + q1[QV] * q2[QV] + q1[QW] * q2[QW];
-  const double cx = P * (q1[QU] + q2[QU]);
-  const double cy = P * (q1[QV] + q2[QV]);
-  const double cz = P * (q1[QW] + q2[QW]);
-  const double ce = P * (q1[QE] + q2[QE]);
+  const double P = kmul<(IM >> 0) & 1>(rhoS, unS);
+  const double s3 = kmul<(IM >> 1) & 1>(q1[QU], q2[QU]) + kmul<(IM >> 2) & 1>(q1[QV], q2[QV]) +
+                    kmul<(IM >> 3) & 1>(q1[QW], q2[QW]);
+  const double cx = kmul<(IM >> 4) & 1>(P, q1[QU] + q2[QU]);
+  const double cy = kmul<(IM >> 5) & 1>(P, q1[QV] + q2[QV]);
+  const double cz = kmul<(IM >> 6) & 1>(P, q1[QW] + q2[QW]);
+  const double ce = kmul<(IM >> 7) & 1>(P, q1[QE] + q2[QE]);
   const double psum = q1[QPRES] + q2[QPRES];
-  const double pu = q1[QPRES] * q2[QN] + q2[QPRES] * q1[QN];
-  T[URHO] = c4 * P;
-  T[UMX] = c8 * (D == 0 ? fma(4.0, psum, cx) : cx);
-  T[UMY] = c8 * (D == 1 ? fma(4.0, psum, cy) : cy);
-  T[UMZ] = c8 * (D == 2 ? fma(4.0, psum, cz) : cz);
-  T[UET] = c8 * fma(4.0, pu, P * s3 + ce);
+  const double pu = kmul<(IM >> 8) & 1>(q1[QPRES], q2[QN]) + kmul<(IM >> 9) & 1>(q2[QPRES], q1[QN]);
+  T[URHO] = kmul<(IM >> 10) & 1>(c4, P);
+  T[UMX] = kmul<(IM >> 11) & 1>(c8, D == 0 ? fma(4.0, psum, cx) : cx);
+  T[UMY] = kmul<(IM >> 12) & 1>(c8, D == 1 ? fma(4.0, psum, cy) : cy);
+  T[UMZ] = kmul<(IM >> 13) & 1>(c8, D == 2 ? fma(4.0, psum, cz) : cz);
+  T[UET] = kmul<(IM >> 14) & 1>(c8, fma(4.0, pu, kmul<(IM >> 15) & 1>(P, s3) + ce));
 }
 
 // Cell-centred viscous fluxes (src/rhs/CNS_hydro_K.h:108-172) from the
@@ -144,19 +180,23 @@ __device__ __forceinline__ void viscous_cell_dy(const double* qc, const double* 
                                                 const double dy[4], const double* qzm, const double* qzp,
                                                 const double dxinv[3], const DClosures& c, double f[NVF]) {
   // (a-b)*0.5*dxinv == (a-b)*(0.5*dxinv) exactly: the 0.5 scalings are exact.
+  // Products on the integer pipe (AMRS_VISC_IMUL): bit 0 the x derivative
+  // scalings, 2 the z ones (the y ones are formed by the callers), 3 the
+  // r1_3*div terms, 4 the stress scalings by mu, 5 the energy-flux products.
+  constexpr int M = AMRS_VISC_IMUL;
   const double hx = 0.5 * dxinv[0], hz = 0.5 * dxinv[2];
   const double ux = qc[QU];
-  const double dudx = (qxp[QU] - qxm[QU]) * hx;
-  const double dvdx = (qxp[QV] - qxm[QV]) * hx;
-  const double dwdx = (qxp[QW] - qxm[QW]) * hx;
-  const double dTdx = (qxp[QT] - qxm[QT]) * hx;
+  const double dudx = kmul<M & 1>(qxp[QU] - qxm[QU], hx);
+  const double dvdx = kmul<M & 1>(qxp[QV] - qxm[QV], hx);
+  const double dwdx = kmul<M & 1>(qxp[QW] - qxm[QW], hx);
+  const double dTdx = kmul<M & 1>(qxp[QT] - qxm[QT], hx);
   const double uy = qc[QV];
   const double dudy = dy[0], dvdy = dy[1], dwdy = dy[2], dTdy = dy[3];
   const double uz = qc[QW];
-  const double dudz = (qzp[QU] - qzm[QU]) * hz;
-  const double dvdz = (qzp[QV] - qzm[QV]) * hz;
-  const double dwdz = (qzp[QW] - qzm[QW]) * hz;
-  const double dTdz = (qzp[QT] - qzm[QT]) * hz;
+  const double dudz = kmul<(M >> 2) & 1>(qzp[QU] - qzm[QU], hz);
+  const double dvdz = kmul<(M >> 2) & 1>(qzp[QV] - qzm[QV], hz);
+  const double dwdz = kmul<(M >> 2) & 1>(qzp[QW] - qzm[QW], hz);
+  const double dTdz = kmul<(M >> 2) & 1>(qzp[QT] - qzm[QT], hz);
   const double div = dudx + dvdy + dwdz;
   const double mu = visc(c, qc[QT]);
   const double lambda = cond(c, qc[QT]);
@@ -165,34 +205,36 @@ __device__ __forceinline__ void viscous_cell_dy(const double* qc, const double* 
   // exact, so (-2mu)*d == -(2mu*d) and a + (-t)*u == a - t*u to the bit:
   // the negated stresses n.. are formed directly and the sums add them,
   // with no separate negations.
+  constexpr bool MD = (M >> 3) & 1, MS = (M >> 4) & 1, ME = (M >> 5) & 1;
   const double nmu = -mu, nmu2 = -2.0 * mu, nlam = -lambda;
-  const double nxx = nmu2 * (dudx - r1_3 * div);
-  const double nxy = nmu * (dudy + dvdx);
-  const double nxz = nmu * (dudz + dwdx);
-  const double nyy = nmu2 * (dvdy - r1_3 * div);
-  const double nyz = nmu * (dvdz + dwdy);
-  const double nzz = nmu2 * (dwdz - r1_3 * div);
+  const double nxx = kmul<MS>(nmu2, dudx - kmul<MD>(r1_3, div));
+  const double nxy = kmul<MS>(nmu, dudy + dvdx);
+  const double nxz = kmul<MS>(nmu, dudz + dwdx);
+  const double nyy = kmul<MS>(nmu2, dvdy - kmul<MD>(r1_3, div));
+  const double nyz = kmul<MS>(nmu, dvdz + dwdy);
+  const double nzz = kmul<MS>(nmu2, dwdz - kmul<MD>(r1_3, div));
   f[0] = nxx;
   f[1] = nxy;
   f[2] = nxz;
-  f[3] = nlam * dTdx + nxx * ux + nxy * uy + nxz * uz;
+  f[3] = kmul<ME>(nlam, dTdx) + kmul<ME>(nxx, ux) + kmul<ME>(nxy, uy) + kmul<ME>(nxz, uz);
   f[4] = nxy;
   f[5] = nyy;
   f[6] = nyz;
-  f[7] = nlam * dTdy + nxy * ux + nyy * uy + nyz * uz;
+  f[7] = kmul<ME>(nlam, dTdy) + kmul<ME>(nxy, ux) + kmul<ME>(nyy, uy) + kmul<ME>(nyz, uz);
   f[8] = nxz;
   f[9] = nyz;
   f[10] = nzz;
-  f[11] = nlam * dTdz + nxz * ux + nyz * uy + nzz * uz;
+  f[11] = kmul<ME>(nlam, dTdz) + kmul<ME>(nxz, ux) + kmul<ME>(nyz, uy) + kmul<ME>(nzz, uz);
 }
 
 __device__ __forceinline__ void viscous_cell(const double* qc, const double* qxm, const double* qxp,
                                              const double* qym, const double* qyp, const double* qzm,
                                              const double* qzp, const double dxinv[3], const DClosures& c,
                                              double f[NVF]) {
+  constexpr bool MY = (AMRS_VISC_IMUL >> 1) & 1;
   const double hy = 0.5 * dxinv[1];
-  const double dy[4] = {(qyp[QU] - qym[QU]) * hy, (qyp[QV] - qym[QV]) * hy, (qyp[QW] - qym[QW]) * hy,
-                        (qyp[QT] - qym[QT]) * hy};
+  const double dy[4] = {kmul<MY>(qyp[QU] - qym[QU], hy), kmul<MY>(qyp[QV] - qym[QV], hy),
+                        kmul<MY>(qyp[QW] - qym[QW], hy), kmul<MY>(qyp[QT] - qym[QT], hy)};
   viscous_cell_dy(qc, qxm, qxp, dy, qzm, qzp, dxinv, c, f);
 }
 
@@ -253,9 +295,10 @@ __device__ __forceinline__ void apply_prog(const DProg& p, double reg[3]) {
   for (int o = 0; o < 3; ++o) {
     if (o >= p.nops) break;
     const DOp& q = p.ops[o];
-    if (q.kind == 0) reg[q.dst] = q.a * reg[q.x] + q.b * reg[q.y];
-    else if (q.kind == 1) reg[q.dst] = reg[q.dst] + q.a * reg[q.x];
-    else if (q.kind == 2) reg[q.dst] = reg[q.x] + q.a * reg[q.dst];
+    constexpr bool M = AMRS_PROG_IMUL & 1;
+    if (q.kind == 0) reg[q.dst] = kmul<M>(q.a, reg[q.x]) + kmul<M>(q.b, reg[q.y]);
+    else if (q.kind == 1) reg[q.dst] = reg[q.dst] + kmul<M>(q.a, reg[q.x]);
+    else if (q.kind == 2) reg[q.dst] = reg[q.x] + kmul<M>(q.a, reg[q.dst]);
     else reg[q.dst] = reg[q.x];
   }
 }

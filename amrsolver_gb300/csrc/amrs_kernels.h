@@ -151,6 +151,8 @@ cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t s
 cudaError_t launch_ddiv_check(unsigned long long seed, long long count, unsigned long long* bad, double* first,
                               int nsm, cudaStream_t st);
 // dsqrt_rn (ddiv.cuh) against the hardware square root over `count` generated operands
+cudaError_t launch_dmul_check(unsigned long long seed, long long count, unsigned long long* bad, double* first,
+                              int nsm, cudaStream_t st);
 cudaError_t launch_dsqrt_check(unsigned long long seed, long long count, unsigned long long* bad, double* first,
                                int nsm, cudaStream_t st);
 // derived plot variables (pressure, temperature, velocities) of one box's valid cells

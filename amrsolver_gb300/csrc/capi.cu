@@ -1898,8 +1898,8 @@ amrs_status amrs_probe_fp64_tflops_timed(amrs_handle* h, double seconds, double*
   return AMRS_OK;
 }
 
-// The integer-pipe division (what = 0) or square root (what = 1) against the
-// hardware one (see the header).
+// The integer-pipe division (what = 0), square root (what = 1) or product
+// (what = 2) against the hardware one (see the header).
 static amrs_status intpipe_check(amrs_handle* h, int what, uint64_t seed, int64_t count, int64_t* mismatches,
                                  double* first) {
   if (!h || !mismatches || !first) return AMRS_ERR_NULL;
@@ -1912,7 +1912,9 @@ static amrs_status intpipe_check(amrs_handle* h, int what, uint64_t seed, int64_
   if (e == cudaSuccess) e = cudaMemset(bad, 0, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemset(dfirst, 0, 4 * sizeof(double));
   if (e == cudaSuccess)
-    e = what ? launch_dsqrt_check(seed, count, bad, dfirst, h->nsm, 0) : launch_ddiv_check(seed, count, bad, dfirst, h->nsm, 0);
+    e = what == 2 ? launch_dmul_check(seed, count, bad, dfirst, h->nsm, 0)
+                  : (what ? launch_dsqrt_check(seed, count, bad, dfirst, h->nsm, 0)
+                          : launch_ddiv_check(seed, count, bad, dfirst, h->nsm, 0));
   unsigned long long nb = 0;
   if (e == cudaSuccess) e = cudaMemcpy(&nb, bad, sizeof(nb), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(first, dfirst, 4 * sizeof(double), cudaMemcpyDeviceToHost);
@@ -1929,6 +1931,10 @@ amrs_status amrs_debug_ddiv_check(amrs_handle* h, uint64_t seed, int64_t count, 
 
 amrs_status amrs_debug_dsqrt_check(amrs_handle* h, uint64_t seed, int64_t count, int64_t* mismatches, double* first) {
   return intpipe_check(h, 1, seed, count, mismatches, first);
+}
+
+amrs_status amrs_debug_dmul_check(amrs_handle* h, uint64_t seed, int64_t count, int64_t* mismatches, double* first) {
+  return intpipe_check(h, 2, seed, count, mismatches, first);
 }
 
 // The same probe with a timed launch of about 0.2 s.

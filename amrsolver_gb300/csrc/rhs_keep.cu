@@ -100,6 +100,12 @@ __global__ void __launch_bounds__(256) visc_cell_kernel(BoxTable tb) {
 }
 
 // ------------------------------------------------ fused face kernel -----
+// Products of the divergence epilogue on the integer pipe, one bit per
+// direction (see kmul).
+#ifndef AMRS_DIV_IMUL
+#define AMRS_DIV_IMUL 0x4
+#endif
+
 template <int ORDER> struct KeepCfg {
   static constexpr int H = ORDER / 2;
   static constexpr int QS_CAP = (ORDER == 6) ? 544 : 480;  // (tx+6)*(ty+2H) capacity
@@ -281,7 +287,8 @@ keep_face_kernel(BoxTable tb, int s_in, int s_s1, int s_out, DProg prog_in, int 
         for (int n = 0; n < 5; ++n) {
           const double* fx = fsx + n * C::F_CAP + cb * (TX + 1) + ca;
           const double* fy = fsy + n * C::F_CAP + cb * TX + ca;
-          double ds = dxi0 * (fx[0] - fx[1]) + dxi1 * (fy[0] - fy[TX]) + dxi2 * (fzprev[n] - fznew[n]);
+          double ds = kmul<AMRS_DIV_IMUL & 1>(dxi0, fx[0] - fx[1]) + kmul<(AMRS_DIV_IMUL >> 1) & 1>(dxi1, fy[0] - fy[TX]) +
+                      kmul<(AMRS_DIV_IMUL >> 2) & 1>(dxi2, fzprev[n] - fznew[n]);
           if (src) ds = add_source(tb.cls[R.cl], Uin.p, oin, Uin.ns, n, ds);
           if (rhs_only) {
             Uo.p[oo + n * Uo.ns] = ds;

@@ -111,6 +111,9 @@ __global__ void __launch_bounds__(256) keep_faces_plain_kernel(BoxTable tb, Face
 
 // ------------------------------------------------------------- WENO5 ----
 // Physical Euler fluxes + max eigenvalue: src/rhs/High_resolution.h:83-121.
+#ifndef AMRS_WPF_IMUL
+#define AMRS_WPF_IMUL 0x0B
+#endif
 __global__ void __launch_bounds__(256) weno_flux_lambda_kernel(BoxTable tb, FaceTable ft, int s_in, long long total) {
   if (list_idle(tb)) return;
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
@@ -126,19 +129,29 @@ __global__ void __launch_bounds__(256) weno_flux_lambda_kernel(BoxTable tb, Face
     const double rhoinv = ddiv_rn(1.0, U.p[o]);
     const double momx = U.p[o + U.ns], momy = U.p[o + 2 * U.ns], momz = U.p[o + 3 * U.ns];
     const double rhoet = U.p[o + 4 * U.ns];
-    const double ux = momx * rhoinv, uy = momy * rhoinv, uz = momz * rhoinv;
-    const double rhoekin = 0.5 * rhoinv * (momx * momx + momy * momy + momz * momz);
+    // products on the integer pipe (kmul), by bit of AMRS_WPF_IMUL: 0 the
+    // velocities, 1 the kinetic energy, 2 the pressure, 3 the fluxes, 4 the
+    // sound speed's argument
+    constexpr int M = AMRS_WPF_IMUL;
+    constexpr bool M0 = M & 1, M1 = (M >> 1) & 1, M2 = (M >> 2) & 1, M3 = (M >> 3) & 1, M4 = (M >> 4) & 1;
+    const double ux = kmul<M0>(momx, rhoinv), uy = kmul<M0>(momy, rhoinv), uz = kmul<M0>(momz, rhoinv);
+    const double rhoekin = kmul<M1>(kmul<M1>(0.5, rhoinv), kmul<M1>(momx, momx) + kmul<M1>(momy, momy) +
+                                                               kmul<M1>(momz, momz));
     const double rhoeint = rhoet - rhoekin;
-    const double P = (gam - 1.0) * rhoeint;
+    const double P = kmul<M2>(gam - 1.0, rhoeint);
     const long long op = FR.pf[0].off(i, j, k);
     const long long ns = FR.pf[0].ns;
     double* fx = FR.pf[0].p + op;
     double* fy = FR.pf[1].p + op;
     double* fz = FR.pf[2].p + op;
-    fx[0] = momx; fx[ns] = momx * ux + P; fx[2 * ns] = momy * ux; fx[3 * ns] = momz * ux; fx[4 * ns] = (rhoet + P) * ux;
-    fy[0] = momy; fy[ns] = momx * uy; fy[2 * ns] = momy * uy + P; fy[3 * ns] = momz * uy; fy[4 * ns] = (rhoet + P) * uy;
-    fz[0] = momz; fz[ns] = momx * uz; fz[2 * ns] = momy * uz; fz[3 * ns] = momz * uz + P; fz[4 * ns] = (rhoet + P) * uz;
-    const double cs = dsqrt_rn(gam * P * rhoinv);
+    const double rhoh = rhoet + P;
+    fx[0] = momx; fx[ns] = kmul<M3>(momx, ux) + P; fx[2 * ns] = kmul<M3>(momy, ux); fx[3 * ns] = kmul<M3>(momz, ux);
+    fx[4 * ns] = kmul<M3>(rhoh, ux);
+    fy[0] = momy; fy[ns] = kmul<M3>(momx, uy); fy[2 * ns] = kmul<M3>(momy, uy) + P; fy[3 * ns] = kmul<M3>(momz, uy);
+    fy[4 * ns] = kmul<M3>(rhoh, uy);
+    fz[0] = momz; fz[ns] = kmul<M3>(momx, uz); fz[2 * ns] = kmul<M3>(momy, uz); fz[3 * ns] = kmul<M3>(momz, uz) + P;
+    fz[4 * ns] = kmul<M3>(rhoh, uz);
+    const double cs = dsqrt_rn(kmul<M4>(kmul<M4>(gam, P), rhoinv));
     const long long ol = FR.lam.off(i, j, k);
     FR.lam.p[ol] = fabs(rmax(rmax(ux + cs, ux - cs), ux));
     FR.lam.p[ol + FR.lam.ns] = fabs(rmax(rmax(uy + cs, uy - cs), uy));
@@ -152,29 +165,44 @@ __global__ void __launch_bounds__(256) weno_flux_lambda_kernel(BoxTable tb, Face
 // separate multiply and add.  The four divisions are correctly rounded on
 // the integer pipe (ddiv_rn): the same quotients as the reference's, at a
 // fraction of the FP64 issue slots.
+// Products formed on the integer pipe (kmul), by bit: 0 the shared 3 s2,
+// 1 the (13/12) x^2 terms, 2 the quarter-scaled squares b^2 and f^2, 3 the
+// fourth power of beta1, 4 the squares of eps + beta, 5 the stencil
+// coefficients 7, 11, 5, 6 the final scaling, 7 the weight products,
+// 8 the LLF halves (0.5 me) U of the face kernel; bit 9 takes the maximum
+// wave speed of the face kernel as an integer maximum of the bit patterns.
+#ifndef AMRS_WENO_IMUL
+#define AMRS_WENO_IMUL 0x263
+#endif
 __device__ __forceinline__ double weno5js(const double s0, const double s1, const double s2, const double s3,
                                           const double s4) {
+  constexpr int M = AMRS_WENO_IMUL;
+  constexpr bool M0 = M & 1, M1 = (M >> 1) & 1, M2 = (M >> 2) & 1, M3 = (M >> 3) & 1, M4 = (M >> 4) & 1,
+                 M5 = (M >> 5) & 1, M6 = (M >> 6) & 1, M7 = (M >> 7) & 1;
   const double eps = 1e-40;
+  const double s2x3 = kmul<M0>(3.0, s2);
   const double a = fma(-2.0, s1, s0) + s2;         // s0 - 2 s1 + s2
-  const double b = fma(-4.0, s1, s0) + 3.0 * s2;   // s0 - 4 s1 + 3 s2
+  const double b = fma(-4.0, s1, s0) + s2x3;       // s0 - 4 s1 + 3 s2
   const double c = fma(-2.0, s2, s1) + s3;         // s1 - 2 s2 + s3
   const double g = s1 - s3;
   const double d = fma(-2.0, s3, s2) + s4;         // s2 - 2 s3 + s4
-  const double f = fma(-4.0, s3, 3.0 * s2) + s4;   // 3 s2 - 4 s3 + s4
+  const double f = fma(-4.0, s3, s2x3) + s4;       // 3 s2 - 4 s3 + s4
   // 0.25*b*b == 0.25*(b*b) and 0.25*g*g*g*g == 0.25*(((g*g)*g)*g): the
   // quarter scales exactly, so x + 0.25*y is one fma(0.25, y, x) (normal range)
-  const double beta0 = fma(0.25, b * b, (13.0 / 12.0) * a * a);
-  const double beta1 = fma(0.25, g * g * g * g, (13.0 / 12.0) * c * c);
-  const double beta2 = fma(0.25, f * f, (13.0 / 12.0) * d * d);
+  constexpr double c1312 = 13.0 / 12.0;
+  const double beta0 = fma(0.25, kmul<M2>(b, b), kmul<M1>(kmul<M1>(c1312, a), a));
+  const double beta1 = fma(0.25, kmul<M3>(kmul<M3>(kmul<M3>(g, g), g), g), kmul<M1>(kmul<M1>(c1312, c), c));
+  const double beta2 = fma(0.25, kmul<M2>(f, f), kmul<M1>(kmul<M1>(c1312, d), d));
   const double e0 = eps + beta0, e1 = eps + beta1, e2 = eps + beta2;
-  const double alpha0 = ddiv_rn(0.1, e0 * e0);
-  const double alpha1 = ddiv_rn(0.6, e1 * e1);
-  const double alpha2 = ddiv_rn(0.3, e2 * e2);
+  const double alpha0 = ddiv_rn(0.1, kmul<M4>(e0, e0));
+  const double alpha1 = ddiv_rn(0.6, kmul<M4>(e1, e1));
+  const double alpha2 = ddiv_rn(0.3, kmul<M4>(e2, e2));
   const double sum = ddiv_rn(1.0, alpha0 + alpha1 + alpha2);
-  const double vl0 = fma(2.0, s0, -(7.0 * s1)) + 11.0 * s2;  // 2 s0 - 7 s1 + 11 s2
-  const double vl1 = fma(2.0, s3, -s1 + 5.0 * s2);          // -s1 + 5 s2 + 2 s3
-  const double vl2 = fma(2.0, s2, 5.0 * s3) - s4;           // 2 s2 + 5 s3 - s4
-  return (1.0 / 6.0) * sum * (alpha0 * vl0 + alpha1 * vl1 + alpha2 * vl2);
+  const double vl0 = fma(2.0, s0, -kmul<M5>(7.0, s1)) + kmul<M5>(11.0, s2);  // 2 s0 - 7 s1 + 11 s2
+  const double vl1 = fma(2.0, s3, -s1 + kmul<M5>(5.0, s2));                  // -s1 + 5 s2 + 2 s3
+  const double vl2 = fma(2.0, s2, kmul<M5>(5.0, s3)) - s4;                   // 2 s2 + 5 s3 - s4
+  return kmul<M6>(kmul<M6>(1.0 / 6.0, sum),
+                  kmul<M7>(alpha0, vl0) + kmul<M7>(alpha1, vl1) + kmul<M7>(alpha2, vl2));
 }
 
 // The same reconstruction with its weights over a common denominator, for
@@ -235,15 +263,16 @@ __global__ void __launch_bounds__(256) weno_face_kernel(BoxTable tb, FaceTable f
     const long long su = (f.d == 0) ? 1 : (f.d == 1 ? U.js : U.ks);
     const long long ol = L.off(f.i, f.j, f.k) + f.d * L.ns;
     double me;
-    if (REF_ORDER) {
+    if (REF_ORDER && !((AMRS_WENO_IMUL >> 9) & 1)) {
       me = rmax(L.p[ol - 3 * st], L.p[ol - 2 * st]);
       me = rmax(me, L.p[ol - st]);
       me = rmax(me, L.p[ol]);
       me = rmax(me, L.p[ol + st]);
       me = rmax(me, L.p[ol + 2 * st]);
     } else {
-      // lambda >= 0: the integer order of the bit patterns is the order of
-      // the values, and the maximum needs no FP64 instruction
+      // lambda = |u| + c > 0: the integer order of the bit patterns is the
+      // order of the values, and the maximum (the same value as the
+      // reference's chain of rmax) needs no FP64 instruction
       long long m = __double_as_longlong(L.p[ol - 3 * st]);
 #pragma unroll
       for (int q = -2; q <= 2; ++q) m = max(m, __double_as_longlong(L.p[ol + q * st]));
@@ -275,7 +304,7 @@ __global__ void __launch_bounds__(256) weno_face_kernel(BoxTable tb, FaceTable f
         double h[6], p[6];
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
-          h[q] = hme * U.p[ou + (q - 3) * su + n * U.ns];
+          h[q] = kmul<(AMRS_WENO_IMUL >> 8) & 1>(hme, U.p[ou + (q - 3) * su + n * U.ns]);
           p[q] = PF.p[opf + (q - 3) * su + n * PF.ns];
         }
         double flx = weno5js(fma(0.5, p[0], h[0]), fma(0.5, p[1], h[1]), fma(0.5, p[2], h[2]),

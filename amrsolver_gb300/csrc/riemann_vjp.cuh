@@ -6,6 +6,8 @@
 #pragma once
 #include <cmath>
 
+#include "ddiv.cuh"
+
 #if defined(__CUDACC__)
 #define AMRS_HD __host__ __device__ __forceinline__
 #else

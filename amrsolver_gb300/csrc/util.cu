@@ -779,6 +779,76 @@ __global__ void __launch_bounds__(256) dsqrt_check_kernel(unsigned long long see
   }
 }
 
+// dmul_rn against the hardware product: arbitrary bit patterns, random
+// significands and signs at moderate exponents, short significands whose
+// products fall on rounding ties, exponent sums at the edges of the integer
+// path's domain (underflow, overflow), zeros, subnormals and specials, and
+// the kernels' constant factors (1/6, -1/48, 1/3, 13/12, 3, 5, 7, 11) against
+// random values.
+__global__ void __launch_bounds__(256) dmul_check_kernel(unsigned long long seed, long long count,
+                                                         unsigned long long* bad, double* first) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long r1 = splitmix(seed ^ (2 * (unsigned long long)i)),
+                             r2 = splitmix(seed ^ (2 * (unsigned long long)i + 1));
+    const unsigned long long SGN = 1ull << 63, FR = 0xFFFFFFFFFFFFFull;
+    double a, b;
+    switch ((int)(i % 6)) {
+      case 0:
+        a = __longlong_as_double((long long)r1);
+        b = __longlong_as_double((long long)r2);
+        break;
+      case 1:
+        a = __longlong_as_double((long long)((r1 & (SGN | FR)) | ((900ull + (r1 >> 52) % 250ull) << 52)));
+        b = __longlong_as_double((long long)((r2 & (SGN | FR)) | ((900ull + (r2 >> 52) % 250ull) << 52)));
+        break;
+      case 2: {  // 20..33-bit significands whose products need 53 or 54 bits
+        const int wa = 20 + (int)(r1 % 14ull), wb = 54 - wa + (int)((r2 >> 60) % 3ull) - 1;
+        const unsigned long long sa = ((r1 >> 8) & ((1ull << (wa - 1)) - 1)) | (1ull << (wa - 1));
+        const unsigned long long sb = ((r2 >> 8) & ((1ull << (wb - 1)) - 1)) | (1ull << (wb - 1));
+        a = __longlong_as_double((long long)((r1 & SGN) | ((sa << (53 - wa)) & FR) | ((1000ull + (r2 & 31ull)) << 52)));
+        b = __longlong_as_double((long long)((r2 & SGN) | ((sb << (53 - wb)) & FR) | ((1000ull + ((r1 >> 3) & 31ull)) << 52)));
+        break;
+      }
+      case 3: {  // exponent sums next to underflow and overflow
+        const int ea = 1 + (int)(r1 % 2046ull);
+        const int target = (r2 & 1ull) ? (int)((r2 >> 1) % 6ull) - 3 : 2043 + (int)((r2 >> 1) % 6ull);
+        int eb = target - ea + 1023;
+        eb = eb < 0 ? 0 : (eb > 2046 ? 2046 : eb);
+        a = __longlong_as_double((long long)((r1 & (SGN | FR)) | ((unsigned long long)ea << 52)));
+        b = __longlong_as_double((long long)((r2 & (SGN | FR)) | ((unsigned long long)eb << 52)));
+        break;
+      }
+      case 4: {  // zeros, subnormals, infinities and NaNs against random values
+        const unsigned long long sp[6] = {0ull, SGN, 0x7FF0000000000000ull, 0x7FF8000000000000ull, r1 & FR,
+                                          r1 & (SGN | FR)};
+        a = __longlong_as_double((long long)sp[(r1 >> 58) % 6ull]);
+        b = __longlong_as_double((long long)((r2 & (SGN | FR)) | (((r2 >> 52) % 2048ull) << 52)));
+        if (r2 & 1ull) { const double t = a; a = b; b = t; }
+        break;
+      }
+      default: {  // the kernels' constant factors
+        const double cst[8] = {0.125 * (4.0 / 3.0), 0.125 * (-2.0 / 12.0), 1.0 / 3.0, 13.0 / 12.0, 3.0, 5.0, 7.0, 11.0};
+        a = cst[r1 & 7ull];
+        b = __longlong_as_double((long long)((r2 & (SGN | FR)) | ((700ull + (r2 >> 52) % 650ull) << 52)));
+      }
+    }
+    const double ref = __dmul_rn(a, b), got = dmul_rn(a, b);
+    const bool nan2 = ref != ref && got != got;
+    if (__double_as_longlong(ref) != __double_as_longlong(got) && !nan2) {
+      if (atomicAdd(bad, 1ull) == 0ull) {
+        first[0] = a; first[1] = b; first[2] = ref; first[3] = got;
+      }
+    }
+  }
+}
+
+cudaError_t launch_dmul_check(unsigned long long seed, long long count, unsigned long long* bad, double* first,
+                              int nsm, cudaStream_t st) {
+  dmul_check_kernel<<<nsm * 8, 256, 0, st>>>(seed, count, bad, first);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_ddiv_check(unsigned long long seed, long long count, unsigned long long* bad, double* first,
                               int nsm, cudaStream_t st) {
   ddiv_check_kernel<<<nsm * 8, 256, 0, st>>>(seed, count, bad, first);

@@ -461,6 +461,13 @@ amrs_status amrs_debug_ddiv_check(amrs_handle* h, uint64_t seed, int64_t count, 
  * exponent range, squares and their neighbours) against the hardware square
  * root; first[0] = x, first[2] = hardware, first[3] = library. */
 amrs_status amrs_debug_dsqrt_check(amrs_handle* h, uint64_t seed, int64_t count, int64_t* mismatches, double* first);
+/* The same for the library's integer-pipe FP64 product (used for part of the
+ * products of the FP64-bound kernels): `count` operand pairs (arbitrary bit
+ * patterns, random significands, short significands whose products fall on
+ * rounding ties, exponents at the edges of underflow and overflow, zeros,
+ * subnormals and specials, the kernels' constant factors) against the
+ * hardware product; first[0..3] = (a, b, hardware, library). */
+amrs_status amrs_debug_dmul_check(amrs_handle* h, uint64_t seed, int64_t count, int64_t* mismatches, double* first);
 /* Per-kernel timing of one RK stage of one box: CUDA events around the
  * kernels on `stream`, averaged over `reps`.  ms[0] primitives (plus the
  * WENO5 point fluxes), ms[1] viscous cell fluxes, ms[2] the Euler face

@@ -1,11 +1,13 @@
-"""The integer-pipe FP64 division and square root
+"""The integer-pipe FP64 division, square root and product
 (amrsolver_gb300/csrc/ddiv.cuh) on the device against CUDA's own: 4e9
 generated operand pairs for the division (the WENO weight and normalisation
 ranges, arbitrary bit patterns, random significands and signs, zero
-numerators) and 2e9 arguments for the square root (arbitrary bits, the whole
-exponent range, squares and their neighbours), every result bit for bit.
-The kernels that divide or take roots use them, so this equality is what
-keeps them equal to the reference's CPU build."""
+numerators), 2e9 arguments for the square root (arbitrary bits, the whole
+exponent range, squares and their neighbours) and 3e9 operand pairs for the
+product (arbitrary bits, rounding ties, the edges of underflow and overflow,
+zeros, subnormals and specials, the kernels' constant factors), every result
+bit for bit.  The kernels use them in place of the hardware operations, so
+this equality is what keeps them equal to the reference's CPU build."""
 import pytest
 import torch
 
@@ -35,4 +37,14 @@ def test_dsqrt_equals_hardware_sqrt():
     for seed in (5, 6):
         bad, first = h.ddiv_check(seed, 1_000_000_000, sqrt=True)
         assert bad == 0, ("square root differs", seed, first)
+    h.close()
+
+
+def test_dmul_equals_hardware_product():
+    assert torch.cuda.is_available(), "GPU test needs a CUDA device"
+    capi.load(build_if_missing=True)
+    h = capi.Handle(P.Scheme(), P.Closures.nondimensional(1e-3))
+    for seed in (7, 8, 9):
+        bad, first = h.ddiv_check(seed, 1_000_000_000, mul=True)
+        assert bad == 0, ("product differs", seed, first)
     h.close()

@@ -143,6 +143,7 @@ SIGNATURES = {
                                     ctypes.POINTER(ctypes.c_double)]),
     "amrs_debug_dmul_check": (_S, [_P, ctypes.c_uint64, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64),
                                    ctypes.POINTER(ctypes.c_double)]),
+    "amrs_probe_intpipe": (_S, [_P, ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]),
     "amrs_probe_fp64_tflops_timed": (_S, [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_double)]),
     "amrs_debug_wait_timeout": (_S, [_P, ctypes.c_int32, _P]),
@@ -375,6 +376,14 @@ class Handle:
               self._L.amrs_debug_dsqrt_check if sqrt else self._L.amrs_debug_ddiv_check)
         check(fn(self.h, int(seed), int(count), ctypes.byref(nb), first), "amrs_debug_ddiv_check")
         return nb.value, tuple(first)
+
+    def probe_intpipe(self, mode):
+        """ms of the overlap probe (amrs_probe_intpipe): 16 FMA chains per
+        thread plus four chains of no (0), hardware (1) or integer-pipe (2)
+        products."""
+        ms = ctypes.c_double()
+        check(self._L.amrs_probe_intpipe(self.h, int(mode), ctypes.byref(ms)), "amrs_probe_intpipe")
+        return ms.value
 
     def set_check_nonfinite(self, on=True):
         """Opt in (or out) of the non-finite check after every stage and RHS;

@@ -55,6 +55,11 @@ struct SBuf {
   int mx, my;
 };
 
+// Resident CTAs per SM asked of the slope and gather reverse kernels.
+#ifndef AMRS_MVJP_CTAS
+#define AMRS_MVJP_CTAS 4
+#endif
+
 // Two CTAs per SM (128 registers): the reverse solver is a long dependent
 // chain per face, and 16 warps hide its latency better than 8 with all the
 // registers it would otherwise take (measured: 7.97 against 8.97 ms per
@@ -137,7 +142,7 @@ __device__ __forceinline__ void mc_vjp(double l, double r, double db, double& lb
   }
 }
 
-__global__ void __launch_bounds__(256) muscl_vjp_slope_kernel(BoxTable tb, FaceRec fr, FBuf fs, SBuf ss, int d,
+__global__ void __launch_bounds__(256, AMRS_MVJP_CTAS) muscl_vjp_slope_kernel(BoxTable tb, FaceRec fr, FBuf fs, SBuf ss, int d,
                                                               long long total) {
   const BoxRec& R = tb.box[0];
   const DArr q = R.q;
@@ -257,7 +262,7 @@ __global__ void __launch_bounds__(256) muscl_vjp_slope_kernel(BoxTable tb, FaceR
   }
 }
 
-__global__ void __launch_bounds__(256) muscl_vjp_gather_kernel(BoxTable tb, DArr ubar, SBuf s0, SBuf s1, SBuf s2,
+__global__ void __launch_bounds__(256, AMRS_MVJP_CTAS) muscl_vjp_gather_kernel(BoxTable tb, DArr ubar, SBuf s0, SBuf s1, SBuf s2,
                                                                long long total) {
   const BoxRec& R = tb.box[0];
   const DClosures& cl = tb.cls[R.cl];

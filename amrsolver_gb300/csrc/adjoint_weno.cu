@@ -87,8 +87,8 @@ __global__ void __launch_bounds__(256) weno_vjp_face_kernel(BoxTable tb, FaceRec
       weno5js_grad(sm5, gm);
 #pragma unroll
       for (int q = 0; q < 6; ++q) {
-        const double a = (q < 5) ? fbn * gp[q] : 0.0;       // cotangent of s+_q
-        const double b = (q > 0) ? fbn * gm[5 - q] : 0.0;   // cotangent of s-_{5-q}
+        const double a = (q < 5) ? kmul<(AMRS_WGRAD_IMUL >> 8) & 1>(fbn, gp[q]) : 0.0;      // cotangent of s+_q
+        const double b = (q > 0) ? kmul<(AMRS_WGRAD_IMUL >> 8) & 1>(fbn, gm[5 - q]) : 0.0;  // cotangent of s-_{5-q}
         const double dlt = a - b;
         fb.p[g + (q * WSLOT + n) * fb.nf] = 0.5 * (a + b);
         fb.p[g + (q * WSLOT + 5 + n) * fb.nf] = 0.5 * me * dlt;

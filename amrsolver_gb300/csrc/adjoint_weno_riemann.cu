@@ -17,6 +17,11 @@
 #include "amrs_kernels.h"
 #include "riemann_vjp.cuh"
 
+// Integer-pipe products of the WENO5 gradients here (see weno5js_grad).
+#ifndef AMRS_WRGRAD_IMUL
+#define AMRS_WRGRAD_IMUL 0x40
+#endif
+
 namespace amrs {
 
 namespace {
@@ -60,8 +65,8 @@ __global__ void __launch_bounds__(256, 3) wr_vjp_face_kernel(BoxTable tb, DArr v
       for (int s = 0; s < 6; ++s) v[s] = q.p[o + (s - 3) * sq + comp[m] * q.ns];
       const double sl[5] = {v[0], v[1], v[2], v[3], v[4]};
       const double sr[5] = {v[5], v[4], v[3], v[2], v[1]};
-      weno5js_grad(sl, gl[m], &lraw[m]);
-      weno5js_grad(sr, gr[m], &rraw[m]);
+      weno5js_grad<AMRS_WRGRAD_IMUL>(sl, gl[m], &lraw[m]);
+      weno5js_grad<AMRS_WRGRAD_IMUL>(sr, gr[m], &rraw[m]);
     }
     in[0] = (lraw[0] < 1.0e-40) ? 1.0e-40 : lraw[0];
     in[1] = lraw[1];

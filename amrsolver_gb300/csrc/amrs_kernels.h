@@ -147,6 +147,7 @@ cudaError_t launch_bcnormal_box(const DArr& u, const int lo[3], const int hi[3],
 cudaError_t launch_bcnormal_list(const BoxTable& tb, int slot, const LevelDomain& dom, const DBcNormal& bn, int nsm,
                                  cudaStream_t st);
 cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t st);
+cudaError_t launch_intpipe_probe(int mode, double* out, int blocks, int iters, cudaStream_t st);
 // ddiv_rn (ddiv.cuh) against the hardware division over `count` generated operand pairs
 cudaError_t launch_ddiv_check(unsigned long long seed, long long count, unsigned long long* bad, double* first,
                               int nsm, cudaStream_t st);

@@ -1898,6 +1898,31 @@ amrs_status amrs_probe_fp64_tflops_timed(amrs_handle* h, double seconds, double*
   return AMRS_OK;
 }
 
+amrs_status amrs_probe_intpipe(amrs_handle* h, int32_t mode, double* ms_out) {
+  if (!h || !ms_out) return AMRS_ERR_NULL;
+  if (mode < 0 || mode > 2) return AMRS_ERR_SIZE;
+  CK(cudaSetDevice(h->device));
+  const int blocks = 2 * h->nsm, iters = 8000;
+  double* buf = nullptr;
+  CK(cudaMalloc(&buf, sizeof(double) * blocks * 256));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaError_t e = launch_intpipe_probe(mode, buf, blocks, iters, 0);  // warm-up
+  if (e == cudaSuccess) e = cudaEventRecord(e0, 0);
+  for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = launch_intpipe_probe(mode, buf, blocks, iters, 0);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, 0);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  if (e != cudaSuccess) return cuda_fail(e, "amrs_probe_intpipe");
+  *ms_out = ms / 3.0;
+  return AMRS_OK;
+}
+
 // The integer-pipe division (what = 0), square root (what = 1) or product
 // (what = 2) against the hardware one (see the header).
 static amrs_status intpipe_check(amrs_handle* h, int what, uint64_t seed, int64_t count, int64_t* mismatches,

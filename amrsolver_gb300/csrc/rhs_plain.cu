@@ -174,9 +174,14 @@ __global__ void __launch_bounds__(256) weno_flux_lambda_kernel(BoxTable tb, Face
 #ifndef AMRS_WENO_IMUL
 #define AMRS_WENO_IMUL 0x263
 #endif
+// The same for the reconstructions of the WENO5-Riemann face kernel, whose
+// serial solver leaves less room on the integer pipe.
+#ifndef AMRS_WRREC_IMUL
+#define AMRS_WRREC_IMUL 0x001
+#endif
+template <int M = AMRS_WENO_IMUL>
 __device__ __forceinline__ double weno5js(const double s0, const double s1, const double s2, const double s3,
                                           const double s4) {
-  constexpr int M = AMRS_WENO_IMUL;
   constexpr bool M0 = M & 1, M1 = (M >> 1) & 1, M2 = (M >> 2) & 1, M3 = (M >> 3) & 1, M4 = (M >> 4) & 1,
                  M5 = (M >> 5) & 1, M6 = (M >> 6) & 1, M7 = (M >> 7) & 1;
   const double eps = 1e-40;
@@ -318,6 +323,22 @@ __global__ void __launch_bounds__(256) weno_face_kernel(BoxTable tb, FaceTable f
 }
 
 // ----------------------------------------------------------- Riemann ----
+// Square roots of the solver and the slopes: integer-pipe (dsqrt_rn) or
+// hardware, the same correctly rounded value.
+#ifndef AMRS_RS_ISQRT
+#define AMRS_RS_ISQRT 0
+#endif
+#ifndef AMRS_SLOPE_ISQRT
+#define AMRS_SLOPE_ISQRT 1
+#endif
+#ifndef AMRS_WR_IDIV
+#define AMRS_WR_IDIV 0
+#endif
+template <bool I>
+__device__ __forceinline__ double rsqrt_(double x) {
+  return I ? dsqrt_rn(x) : sqrt(x);
+}
+
 __device__ __forceinline__ double mc_limiter(double dlft, double drgt) {
   // src/rhs/Riemann.h:9-17
   const double dcen = 0.5 * (dlft + drgt);
@@ -355,7 +376,7 @@ __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, c
     const long long o = q.off(i, j, k);
     const int QN = QU + d, QT1 = (d == 0) ? QV : QU, QT2 = (d == 2) ? QV : QW;
     auto Q = [&](long long off, int n) { return q.p[off + n * q.ns]; };
-    const double c0 = sqrt(cl.gamma * cl.Rspec * Q(o, QT));
+    const double c0 = rsqrt_<AMRS_SLOPE_ISQRT>(cl.gamma * cl.Rspec * Q(o, QT));
     const double cspeed = c0 + (d == 0 ? 2.e-40 : 1.e-40);
     double dlft = ddiv_rn(0.5 * (Q(o, QPRES) - Q(o - s, QPRES)), cspeed) - 0.5 * Q(o, QRHO) * (Q(o, QN) - Q(o - s, QN));
     double drgt = ddiv_rn(0.5 * (Q(o + s, QPRES) - Q(o, QPRES)), cspeed) - 0.5 * Q(o, QRHO) * (Q(o + s, QN) - Q(o, QN));
@@ -385,7 +406,7 @@ __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, c
     if (d == 2 && k <= R.hi[2]) {
       // cns_riemann_z's left state takes its sound speed from q(i,j,k+1)
       // (src/rhs/Riemann.h:316): for the face above this cell, cell k + 2
-      const double csl = sqrt(cl.gamma * cl.Rspec * Q(o + 2 * s, QT)) + 1.e-40;
+      const double csl = rsqrt_<AMRS_SLOPE_ISQRT>(cl.gamma * cl.Rspec * Q(o + 2 * s, QT)) + 1.e-40;
       S.p[os + SL_AL * S.ns] = ddiv_rn(s02, csl) + d1;
       S.p[os + SL_CL * S.ns] = s02 * csl;
     }
@@ -414,8 +435,8 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   const double small = 1.e-6;
   const double clsql = gamma * pl * rl;
   const double clsqr = gamma * pr * rr;
-  double wl = sqrt(clsql);
-  double wr = sqrt(clsqr);
+  double wl = rsqrt_<AMRS_RS_ISQRT>(clsql);
+  double wr = rsqrt_<AMRS_RS_ISQRT>(clsqr);
   const double cleft = rdiv<IDIV>(wl, rl);
   const double cright = rdiv<IDIV>(wr, rr);
   const double ccsmall = small * (cleft + cright);
@@ -424,8 +445,8 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   double pstnm1 = pstar;
   double wlsq = (0.5 * (gamma - 1.) * (pstar + pl) + pstar) * rl;
   double wrsq = (0.5 * (gamma - 1.) * (pstar + pr) + pstar) * rr;
-  wl = sqrt(wlsq);
-  wr = sqrt(wrsq);
+  wl = rsqrt_<AMRS_RS_ISQRT>(wlsq);
+  wr = rsqrt_<AMRS_RS_ISQRT>(wrsq);
   double ustarp = ul - rdiv<IDIV>(pstar - pl, wl);
   double ustarm = ur + rdiv<IDIV>(pstar - pr, wr);
   pstar = rdiv<IDIV>(wl * pr + wr * pl - wr * wl * (ur - ul), wl + wr);
@@ -434,8 +455,8 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   for (int iter = 0; iter < 3; ++iter) {
     wlsq = (0.5 * (gamma - 1.) * (pstar + pl) + pstar) * rl;
     wrsq = (0.5 * (gamma - 1.) * (pstar + pr) + pstar) * rr;
-    wl = rdiv<IDIV>(1., sqrt(wlsq));
-    wr = rdiv<IDIV>(1., sqrt(wrsq));
+    wl = rdiv<IDIV>(1., rsqrt_<AMRS_RS_ISQRT>(wlsq));
+    wr = rdiv<IDIV>(1., rsqrt_<AMRS_RS_ISQRT>(wrsq));
     const double ustnm1 = ustarm;
     const double ustnp1 = ustarp;
     ustarm = ur - (pr - pstar) * wr;
@@ -481,7 +502,7 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   };
   if (pstar >= po) {
     // shock: spout == spin, so the side state or the star state
-    const double spin = rdiv<IDIV>(sqrt(wosq), ro) - suo;
+    const double spin = rdiv<IDIV>(rsqrt_<AMRS_RS_ISQRT>(wosq), ro) - suo;
     if (spin < 0.) {
       rgdnv = ro; ugdnv = uo; pgdnv = po;
     } else if (spin >= 0.) {
@@ -491,8 +512,8 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
     }
   } else {
     const double rstar = rdiv<IDIV>(ro, 1. - rdiv<IDIV>(ro * dpjmp, wosq));
-    const double spout = sqrt(rdiv<IDIV>(gamma * po, ro)) - suo;
-    const double spin = sqrt(rdiv<IDIV>(gamma * pstar, rstar)) - suo;
+    const double spout = rsqrt_<AMRS_RS_ISQRT>(rdiv<IDIV>(gamma * po, ro)) - suo;
+    const double spin = rsqrt_<AMRS_RS_ISQRT>(rdiv<IDIV>(gamma * pstar, rstar)) - suo;
     if (spout < 0.) {
       rgdnv = ro; ugdnv = uo; pgdnv = po;
     } else if (spin >= 0.) {
@@ -585,11 +606,11 @@ __global__ void __launch_bounds__(256) weno_riemann_face_kernel(BoxTable tb, Fac
       double v[6];
 #pragma unroll
       for (int t = 0; t < 6; ++t) v[t] = p[(t - 3) * sq];
-      lft[m] = weno5js(v[0], v[1], v[2], v[3], v[4]);
-      rgt[m] = weno5js(v[5], v[4], v[3], v[2], v[1]);
+      lft[m] = weno5js<AMRS_WRREC_IMUL>(v[0], v[1], v[2], v[3], v[4]);
+      rgt[m] = weno5js<AMRS_WRREC_IMUL>(v[5], v[4], v[3], v[2], v[1]);
     }
     double frho, fu, fut, futt, fe;
-    riemann_prob<false>(cl.gamma, 1.0e-40, rmax(lft[0], 1.0e-40), lft[1], rmax(lft[2], 1.0e-40), lft[3], lft[4],
+    riemann_prob<AMRS_WR_IDIV != 0>(cl.gamma, 1.0e-40, rmax(lft[0], 1.0e-40), lft[1], rmax(lft[2], 1.0e-40), lft[3], lft[4],
                         rmax(rgt[0], 1.0e-40), rgt[1], rmax(rgt[2], 1.0e-40), rgt[3], rgt[4], frho, fu, fut, futt, fe);
     const DArr Fd = ft.fr[f.b].f[d];
     const long long of = Fd.off(f.i, f.j, f.k);

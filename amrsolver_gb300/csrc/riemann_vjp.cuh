@@ -23,6 +23,13 @@ using std::sqrt;
 
 AMRS_HD double sgn1(double x) { return x < 0.0 ? -1.0 : 1.0; }  // d|x|/dx as fabs's branch
 
+// Square roots of the reverse solver: integer-pipe (dsqrt_rn) or hardware,
+// the same correctly rounded value.
+#ifndef AMRS_RV_ISQRT
+#define AMRS_RV_ISQRT 0
+#endif
+AMRS_HD double rvsqrt(double x) { return AMRS_RV_ISQRT ? dsqrt_rn(x) : sqrt(x); }
+
 // One iteration of riemann_prob's pressure update (src/rhs/Riemann.h:163-189)
 // and its reverse.  State (P = pstar, Pm = pstnm1, UM = ustarm, UP = ustarp).
 struct RPPar {
@@ -31,8 +38,8 @@ struct RPPar {
 
 AMRS_HD void rp_iter_fwd(const RPPar& q, double P, double Pm, double UM, double UP, double& Pn,
                                             double& UMn, double& UPn) {
-  const double wl = ddiv_rn(1., sqrt((q.hg * (P + q.pl) + P) * q.rl));
-  const double wr = ddiv_rn(1., sqrt((q.hg * (P + q.pr) + P) * q.rr));
+  const double wl = ddiv_rn(1., rvsqrt((q.hg * (P + q.pl) + P) * q.rl));
+  const double wr = ddiv_rn(1., rvsqrt((q.hg * (P + q.pr) + P) * q.rr));
   UMn = q.ur - (q.pr - P) * wr;
   UPn = q.ul + (q.pl - P) * wl;
   const double dpd = fabs(Pm - P);
@@ -55,7 +62,7 @@ AMRS_HD void rp_iter_vjp(const RPPar& q, double P, double Pm, double UM, double 
                                             double Pmnb, double UMnb, double UPnb, double& Pb, double& Pmb,
                                             double& UMb, double& UPb, RPBar& g) {
   const double al = q.hg * (P + q.pl) + P, ar = q.hg * (P + q.pr) + P;
-  const double sl = sqrt(al * q.rl), sr = sqrt(ar * q.rr);
+  const double sl = rvsqrt(al * q.rl), sr = rvsqrt(ar * q.rr);
   const double wl = ddiv_rn(1., sl), wr = ddiv_rn(1., sr);
   const double UMn = q.ur - (q.pr - P) * wr;
   const double UPn = q.ul + (q.pl - P) * wl;
@@ -100,7 +107,7 @@ AMRS_HD void rp_iter_vjp(const RPPar& q, double P, double Pm, double UM, double 
   g.pl += UPnbar * wl;
   Pbar -= UPnbar * wl;
   wlb += UPnbar * (q.pl - P);
-  // w = 1/sqrt(a r), a = hg (P + p) + P
+  // w = 1/rvsqrt(a r), a = hg (P + p) + P
   const double slb = -wlb * wl * wl, srb = -wrb * wr * wr;
   const double wlsqb = ddiv_rn(slb, (2.0 * sl)), wrsqb = ddiv_rn(srb, (2.0 * sr));
   g.rl += wlsqb * al;
@@ -123,7 +130,7 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
   const double hg = 0.5 * (gamma - 1.);
   // ---- forward
   const double clsql = gamma * pl * rl, clsqr = gamma * pr * rr;
-  const double wl0 = sqrt(clsql), wr0 = sqrt(clsqr);
+  const double wl0 = rvsqrt(clsql), wr0 = rvsqrt(clsqr);
   const double cleft = ddiv_rn(wl0, rl), cright = ddiv_rn(wr0, rr);
   const double ccs = small * (cleft + cright);
   const double dU = ur - ul;
@@ -132,7 +139,7 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
   const bool m0 = !(ps0 < smallp);
   const double p0 = m0 ? ps0 : smallp;
   const double a1l = hg * (p0 + pl) + p0, a1r = hg * (p0 + pr) + p0;
-  const double wl1 = sqrt(a1l * rl), wr1 = sqrt(a1r * rr);
+  const double wl1 = rvsqrt(a1l * rl), wr1 = rvsqrt(a1r * rr);
   const double usp0 = ul - ddiv_rn((p0 - pl), wl1);
   const double usm0 = ur + ddiv_rn((p0 - pr), wr1);
   const double D1 = wl1 + wr1;
@@ -167,12 +174,12 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
   int kind;
   double spin = 0.0, spout = 0.0, co = 0.0, cstar = 0.0;
   if (pstar >= po) {
-    spin = ddiv_rn(sqrt(wosq), ro) - suo;
+    spin = ddiv_rn(rvsqrt(wosq), ro) - suo;
     kind = (spin < 0.) ? 0 : ((spin >= 0.) ? 1 : 2);
     spout = spin;
   } else {
-    co = sqrt(ddiv_rn(gamma * po, ro));
-    cstar = sqrt(ddiv_rn(gamma * pstar, rstar));
+    co = rvsqrt(ddiv_rn(gamma * po, ro));
+    cstar = rvsqrt(ddiv_rn(gamma * pstar, rstar));
     spout = co - suo;
     spin = cstar - suo;
     kind = (spout < 0.) ? 0 : ((spin >= 0.) ? 1 : 2);
@@ -290,7 +297,7 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
     p0b -= ddiv_rn(UPnb, wl1);
     g.pl += ddiv_rn(UPnb, wl1);
     wl1b += ddiv_rn(UPnb * (p0 - pl), (wl1 * wl1));
-    // w1 = sqrt(a1 r), a1 = hg (p0 + p) + p0
+    // w1 = rvsqrt(a1 r), a1 = hg (p0 + p) + p0
     const double wlsqb = ddiv_rn(wl1b, (2.0 * wl1)), wrsqb = ddiv_rn(wr1b, (2.0 * wr1));
     g.rl += wlsqb * a1l;
     g.rr += wrsqb * a1r;
@@ -318,7 +325,7 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
   }
   g.ur += dUb;
   g.ul -= dUb;
-  // w0 = sqrt(gamma p r)
+  // w0 = rvsqrt(gamma p r)
   {
     const double lb = ddiv_rn(wl0b, (2.0 * wl0)), rb2 = ddiv_rn(wr0b, (2.0 * wr0));
     g.pl += lb * gamma * rl;

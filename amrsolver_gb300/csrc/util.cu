@@ -691,6 +691,43 @@ cudaError_t launch_fp64_probe(double* out, int blocks, int iters, cudaStream_t s
   return cudaGetLastError();
 }
 
+// Overlap probe of the integer-pipe product: sixteen DFMA chains per thread
+// (the FP64 pipe saturated at 16 warps per SM) plus, per iteration, four
+// further chains of products: none (MODE 0), hardware products (MODE 1) or
+// dmul_rn (MODE 2).  The time over MODE 0's is what the four products cost a
+// kernel whose FP64 pipe is already full.
+template <int MODE>
+__global__ void __launch_bounds__(256, 2) intpipe_probe_kernel(double* out, int iters, double m, double a) {
+  double f[16], g[4];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) f[c] = 1.0 + threadIdx.x * 1e-9 + c * 1e-3;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) g[c] = 1.0 + threadIdx.x * 1e-9 + c * 1e-3;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int c = 0; c < 16; ++c) f[c] = fma(f[c], m, a);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      if (MODE == 1) g[c] = __dmul_rn(g[c], m);
+      if (MODE == 2) g[c] = dmul_rn(g[c], m);
+    }
+  }
+  double r = 0.0;
+#pragma unroll
+  for (int c = 0; c < 16; ++c) r += f[c];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) r += g[c];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = r;
+}
+
+cudaError_t launch_intpipe_probe(int mode, double* out, int blocks, int iters, cudaStream_t st) {
+  const double m = 0.9999999, a = 1e-7;
+  if (mode == 0) intpipe_probe_kernel<0><<<blocks, 256, 0, st>>>(out, iters, m, a);
+  else if (mode == 1) intpipe_probe_kernel<1><<<blocks, 256, 0, st>>>(out, iters, m, a);
+  else intpipe_probe_kernel<2><<<blocks, 256, 0, st>>>(out, iters, m, a);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------ division check ----
 // ddiv_rn against the hardware division over generated operands: index i
 // of the launch draws (a, b) from one of four families (WENO weights

@@ -982,6 +982,12 @@ def fp64_peak(torch, h, local, seconds=1.5):
         info["nominal_tflops_at_max_mhz"] = nsm * 4 * clk["sm_max_mhz"] * 1e6 / 1e12
     peak = max(tf, nominal or 0.0)
     info["chosen"] = "probe" if peak == tf else "nominal at sampled clock"
+    # what four products per 16 FMAs cost beside a full FP64 pipe: hardware
+    # products take FP64 slots, the integer-pipe product (part of the kernels'
+    # products) overlaps with the FMAs
+    ip = [h.probe_intpipe(m) for m in (0, 1, 2)]
+    info["intpipe_probe_ms"] = {"fma_only": ip[0], "fma_plus_hw_products": ip[1],
+                                "fma_plus_intpipe_products": ip[2]}
     return peak, info
 
 

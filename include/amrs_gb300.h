@@ -468,6 +468,15 @@ amrs_status amrs_debug_dsqrt_check(amrs_handle* h, uint64_t seed, int64_t count,
  * subnormals and specials, the kernels' constant factors) against the
  * hardware product; first[0..3] = (a, b, hardware, library). */
 amrs_status amrs_debug_dmul_check(amrs_handle* h, uint64_t seed, int64_t count, int64_t* mismatches, double* first);
+/* Overlap probe of the integer-pipe product: one launch of 2 CTAs of 256
+ * threads per SM, each thread running 16 FP64 FMA chains for 8000
+ * iterations plus four chains of products per iteration: none (mode 0),
+ * hardware products (mode 1) or the library's integer-pipe product (mode 2).
+ * *ms receives the launch's time (CUDA events, mean of three after a
+ * warm-up); the difference to mode 0 is what four products per 16 FMAs cost
+ * a kernel whose FP64 pipe is full (AMRS_ERR_SIZE for another mode).
+ * Host-synchronising. */
+amrs_status amrs_probe_intpipe(amrs_handle* h, int32_t mode, double* ms);
 /* Per-kernel timing of one RK stage of one box: CUDA events around the
  * kernels on `stream`, averaged over `reps`.  ms[0] primitives (plus the
  * WENO5 point fluxes), ms[1] viscous cell fluxes, ms[2] the Euler face

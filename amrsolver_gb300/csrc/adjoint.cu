@@ -44,43 +44,54 @@ __device__ __forceinline__ double fbar(const DArr& v, const BoxRec& R, int d, in
 
 // VJP of one KEEP pair term (keep_pair in amrs_device.cuh) given its
 // cotangent a[5] (already times the coefficient): contributions to the
-// primitive cotangents of point 1 (larger index) and point 2.
+// primitive cotangents of point 1 (larger index) and point 2.  With
+// P = R N, the mass flux m = P/4 and the cubic factor t8 = P/8, so the
+// cotangents of R and N share one factor s = mb/4 + t8b/8 (exact scalings;
+// the reverse pass has no bit-exact counterpart).  Standalone products may
+// go to the integer pipe (kmul, AMRS_PVJP_IMUL): bit 0 the cotangents of
+// the velocity sums and of E, bit 1 those of R and N, bit 2 cv Eb.
+#ifndef AMRS_PVJP_IMUL
+#define AMRS_PVJP_IMUL 0x3
+#endif
 template <int D>
 __device__ __forceinline__ void keep_pair_vjp(const double* q1, const double* q2, const double a[5], double cv,
                                               double b1[NQA], double b2[NQA]) {
   constexpr int QN = QU + D;
+  constexpr bool M0 = AMRS_PVJP_IMUL & 1, M1 = (AMRS_PVJP_IMUL >> 1) & 1, M2 = (AMRS_PVJP_IMUL >> 2) & 1;
   const double R = q1[QRHO] + q2[QRHO];
   const double N = q1[QN] + q2[QN];
   const double Ux = q1[QU] + q2[QU], Uy = q1[QV] + q2[QV], Uz = q1[QW] + q2[QW];
   const double E = q1[QE] + q2[QE];
-  const double m = 0.25 * R * N;
+  const double P = R * N;
   const double ke = 0.5 * (q1[QU] * q2[QU] + q1[QV] * q2[QV] + q1[QW] * q2[QW]);
-  const double t8 = 0.125 * R * N;
+  const double t8 = 0.125 * P;
   const double mb = a[0] + a[4] * ke;
-  const double keb = a[4] * m;
+  const double keb = 0.25 * (a[4] * P);
   const double t8b = a[1] * Ux + a[2] * Uy + a[3] * Uz + a[4] * E;
-  const double Uxb = a[1] * t8, Uyb = a[2] * t8, Uzb = a[3] * t8, Eb = a[4] * t8;
+  const double Uxb = kmul<M0>(a[1], t8), Uyb = kmul<M0>(a[2], t8), Uzb = kmul<M0>(a[3], t8),
+               Eb = kmul<M0>(a[4], t8);
   const double fdivb = a[1 + D];
   const double fgb = a[4];
-  const double Rb = 0.25 * N * mb + 0.125 * N * t8b;
-  const double Nb = 0.25 * R * mb + 0.125 * R * t8b;
+  const double sb = 0.25 * mb + 0.125 * t8b;
+  const double Rb = kmul<M1>(N, sb);
+  const double Nb = kmul<M1>(R, sb);
   const double Pb = 0.5 * fdivb;
   const double Ub[3] = {Uxb, Uyb, Uzb};
+  const double hk = 0.5 * keb, hg = 0.5 * fgb;
+  const double cvE = kmul<M2>(cv, Eb);
 #pragma unroll
   for (int s = 0; s < 2; ++s) {
-    const double* qa = s ? q2 : q1;
     const double* qo = s ? q1 : q2;
     double* b = s ? b2 : b1;
     b[0] = Rb;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      double t = Ub[c] + 0.5 * keb * qo[QU + c];
-      if (c == D) t += Nb + 0.5 * fgb * qo[QPRES];
+      double t = Ub[c] + hk * qo[QU + c];
+      if (c == D) t += Nb + hg * qo[QPRES];
       b[1 + c] = t;
     }
-    b[4] = cv * Eb;
-    b[5] = Pb + 0.5 * fgb * qo[QN];
-    (void)qa;
+    b[4] = cvE;
+    b[5] = Pb + hg * qo[QN];
   }
 }
 
@@ -164,19 +175,22 @@ __global__ void __launch_bounds__(256) adj_visc_kernel(BoxTable tb, AdjRec ar, l
     const int t = l / nx;
     const int j = t % ny + R.lo[1] - 1;
     const int k = t / ny + R.lo[2] - 1;
-    // Vbar: each cell flux enters the faces below and above it with 0.5
+    const double hx = 0.5 * R.dxinv[0], hy = 0.5 * R.dxinv[1], hz = 0.5 * R.dxinv[2];
+    // Vbar: each cell flux enters the faces below and above it with 0.5, and
+    // Fbar(c) + Fbar(c + e_d) = dxinv_d (vbar(c + e_d) - vbar(c - e_d))
     double fb[NVF];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const int di = d == 0, dj = d == 1, dk = d == 2;
+      const double h = d == 0 ? hx : (d == 1 ? hy : hz);
 #pragma unroll
       for (int n = 0; n < 4; ++n)
-        fb[4 * d + n] = 0.5 * (fbar(ar.vbar, R, d, i, j, k, 1 + n) + fbar(ar.vbar, R, d, i + di, j + dj, k + dk, 1 + n));
+        fb[4 * d + n] = h * (vget(ar.vbar, R, i + di, j + dj, k + dk, 1 + n) -
+                             vget(ar.vbar, R, i - di, j - dj, k - dk, 1 + n));
     }
     const DArr Q = R.q;
     const long long o = Q.off(i, j, k);
     auto q = [&](long long off, int n) { return Q.p[off + n * Q.ns]; };
-    const double hx = 0.5 * R.dxinv[0], hy = 0.5 * R.dxinv[1], hz = 0.5 * R.dxinv[2];
     const long long sx = 1, sy = Q.js, sz = Q.ks;
     const double u = q(o, QU), v = q(o, QV), w = q(o, QW), T = q(o, QT);
     const double dudx = (q(o + sx, QU) - q(o - sx, QU)) * hx, dvdx = (q(o + sx, QV) - q(o - sx, QV)) * hx;
@@ -212,16 +226,17 @@ __global__ void __launch_bounds__(256) adj_visc_kernel(BoxTable tb, AdjRec ar, l
                        tyzb * (dvdz + dwdy);
     const double divb = -(2.0 / 3.0) * mu * (txxb + tyyb + tzzb);
     double gb[12];
+    const double gxy = mu * txyb, gxz = mu * txzb, gyz = mu * tyzb;
     gb[0] = 2.0 * mu * txxb + divb;  // dudx
-    gb[1] = mu * txyb;               // dvdx
-    gb[2] = mu * txzb;               // dwdx
+    gb[1] = gxy;                     // dvdx
+    gb[2] = gxz;                     // dwdx
     gb[3] = -lam * fb[3];            // dTdx
-    gb[4] = mu * txyb;               // dudy
+    gb[4] = gxy;                     // dudy
     gb[5] = 2.0 * mu * tyyb + divb;  // dvdy
-    gb[6] = mu * tyzb;               // dwdy
+    gb[6] = gyz;                     // dwdy
     gb[7] = -lam * fb[7];            // dTdy
-    gb[8] = mu * txzb;               // dudz
-    gb[9] = mu * tyzb;               // dvdz
+    gb[8] = gxz;                     // dudz
+    gb[9] = gyz;                     // dvdz
     gb[10] = 2.0 * mu * tzzb + divb; // dwdz
     gb[11] = -lam * fb[11];          // dTdz
     double Tb = 0.0;

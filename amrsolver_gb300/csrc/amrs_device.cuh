@@ -99,9 +99,6 @@ __device__ __forceinline__ double kmul(double a, double b) {
 #ifndef AMRS_VISC_IMUL
 #define AMRS_VISC_IMUL 0x17
 #endif
-#ifndef AMRS_PROG_IMUL
-#define AMRS_PROG_IMUL 0x0
-#endif
 __device__ __forceinline__ void cons2prim(const double u[5], double q[NQ], const DClosures& c) {
   double rho = rmax(1e-40, u[URHO]);
   constexpr int M = AMRS_C2P_IMUL;
@@ -295,10 +292,9 @@ __device__ __forceinline__ void apply_prog(const DProg& p, double reg[3]) {
   for (int o = 0; o < 3; ++o) {
     if (o >= p.nops) break;
     const DOp& q = p.ops[o];
-    constexpr bool M = AMRS_PROG_IMUL & 1;
-    if (q.kind == 0) reg[q.dst] = kmul<M>(q.a, reg[q.x]) + kmul<M>(q.b, reg[q.y]);
-    else if (q.kind == 1) reg[q.dst] = reg[q.dst] + kmul<M>(q.a, reg[q.x]);
-    else if (q.kind == 2) reg[q.dst] = reg[q.x] + kmul<M>(q.a, reg[q.dst]);
+    if (q.kind == 0) reg[q.dst] = q.a * reg[q.x] + q.b * reg[q.y];
+    else if (q.kind == 1) reg[q.dst] = reg[q.dst] + q.a * reg[q.x];
+    else if (q.kind == 2) reg[q.dst] = reg[q.x] + q.a * reg[q.dst];
     else reg[q.dst] = reg[q.x];
   }
 }

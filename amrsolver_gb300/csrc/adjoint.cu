@@ -130,15 +130,22 @@ __global__ void __launch_bounds__(256) adj_pair_kernel(BoxTable tb, AdjRec ar, l
     // wall the reduced y faces take only the l = 1 pair, with coefficient 1
     // (Flux_2nd_Order_KEEP, src/rhs/CentralKEEP.h:232-287).
     double a[5] = {0, 0, 0, 0, 0};
-    for (int m = 1; m <= l; ++m) {
-      double w = coef[l - 1];
-      if (d == 1 && R.walls) {
+    if (d == 1 && R.walls) {
+      for (int m = 1; m <= l; ++m) {
+        double w = coef[l - 1];
         const int jf = j + m;
         if (jf <= R.red_lo || (jf >= R.red_hi && jf <= R.hi[1])) w = (l == 1) ? 1.0 : 0.0;
-      }
-      if (w == 0.0) continue;
+        if (w == 0.0) continue;
 #pragma unroll
-      for (int n = 0; n < 5; ++n) a[n] += w * fbar(ar.vbar, R, d, i + m * di, j + m * dj, k + m * dk, n);
+        for (int n = 0; n < 5; ++n) a[n] += w * fbar(ar.vbar, R, d, i + m * di, j + m * dj, k + m * dk, n);
+      }
+    } else {
+      // one coefficient for all l faces: sum_m Fbar(a + m) telescopes to
+      // dxinv_d (vbar(a + l) - vbar(a))
+      const double wd = coef[l - 1] * R.dxinv[d];
+#pragma unroll
+      for (int n = 0; n < 5; ++n)
+        a[n] = wd * (vget(ar.vbar, R, i + l * di, j + l * dj, k + l * dk, n) - vget(ar.vbar, R, i, j, k, n));
     }
     double q1[NQ], q2[NQ], b1[NQA], b2[NQA];
     const long long o2 = R.q.off(i, j, k), o1 = R.q.off(i + l * di, j + l * dj, k + l * dk);

@@ -206,18 +206,24 @@ __global__ void __launch_bounds__(256, AMRS_MVJP_CTAS) muscl_vjp_slope_kernel(Bo
       else { Ab += f[5 * n]; Cb += f[7 * n]; }
       Bb += f[6 * n]; d3b += f[8 * n]; d4b += f[9 * n];
     }
-    // A = s02/csr + d1, B = (d2 - d0)/rho, C = s02*csr (z: A_L, C_L with csl)
-    double s02b = ddiv_rn(Ab, csr) + Cb * csr;
-    double csrb = ddiv_rn(-Ab * (ddiv_rn(s02, csr)), csr) + Cb * s02;
+    // A = s02/csr + d1, B = (d2 - d0)/rho, C = s02*csr (z: A_L, C_L with csl).
+    // The cotangents use reciprocals: the reverse pass has no bit-exact
+    // counterpart (its bar is agreement with forward-mode derivatives), and
+    // four divisions serve the sixteen quotients below.
+    const double icsr = ddiv_rn(1.0, csr), irc = ddiv_rn(1.0, rc), ics = ddiv_rn(1.0, cs);
+    const double ics2 = ics * ics;
+    double s02b = Ab * icsr + Cb * csr;
+    double csrb = -Ab * (s02 * icsr) * icsr + Cb * s02;
     double d1b = Ab + ALb;
-    double d0b = ddiv_rn(-Bb, rc), d2b = ddiv_rn(Bb, rc);
-    double rcb = ddiv_rn(-Bb * (ddiv_rn((d2 - d0), rc)), rc);
+    double d0b = -Bb * irc, d2b = Bb * irc;
+    double rcb = -Bb * ((d2 - d0) * irc) * irc;
     double csl = 0.0, c0l = 0.0, cslb = 0.0;
     if (d == 2 && c <= R.hi[2]) {
       c0l = sqrt(gR * Q(o + 2 * s, QT));
       csl = c0l + 1.e-40;
-      s02b += ddiv_rn(ALb, csl) + CLb * csl;
-      cslb = ddiv_rn(-ALb * (ddiv_rn(s02, csl)), csl) + CLb * s02;
+      const double icsl = ddiv_rn(1.0, csl);
+      s02b += ALb * icsl + CLb * csl;
+      cslb = -ALb * (s02 * icsl) * icsl + CLb * s02;
     }
     d0b += s02b;
     d2b += s02b;
@@ -231,9 +237,9 @@ __global__ void __launch_bounds__(256, AMRS_MVJP_CTAS) muscl_vjp_slope_kernel(Bo
     mc_vjp(d2l, d2r, d4b, l4b, r4b);
     // characteristic differences
     double csb = 0.0;
-    double dplb = ddiv_rn(0.5 * (l0b + l2b), cs) - ddiv_rn(l1b, cs2), dprb = ddiv_rn(0.5 * (r0b + r2b), cs) - ddiv_rn(r1b, cs2);
-    csb += ddiv_rn(-0.5 * (l0b + l2b) * dpl, cs2) - ddiv_rn(0.5 * (r0b + r2b) * dpr, cs2);
-    csb += ddiv_rn(2.0 * (l1b * dpl + r1b * dpr), (cs2 * cs));
+    double dplb = 0.5 * (l0b + l2b) * ics - l1b * ics2, dprb = 0.5 * (r0b + r2b) * ics - r1b * ics2;
+    csb += (-0.5 * (l0b + l2b) * dpl - 0.5 * (r0b + r2b) * dpr) * ics2;
+    csb += 2.0 * (l1b * dpl + r1b * dpr) * (ics2 * ics);
     const double dulb = 0.5 * rc * (l2b - l0b), durb = 0.5 * rc * (r2b - r0b);
     rcb += 0.5 * ((l2b - l0b) * dul + (r2b - r0b) * dur);
     const double drlb = l1b, drrb = r1b;

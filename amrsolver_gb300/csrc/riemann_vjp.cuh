@@ -87,8 +87,9 @@ AMRS_HD void rp_iter_vjp(const RPPar& q, double P, double Pm, double UM, double 
   const double denomb = -pnb * (UMn - UPn);
   UMnbar += -pnb * denom;
   UPnbar += pnb * denom;
-  dpdb += ddiv_rn(denomb, den);
-  const double denb = ddiv_rn(-denomb * denom, den);
+  const double iden = ddiv_rn(1.0, den);
+  dpdb += denomb * iden;
+  const double denb = -denomb * denom * iden;
   if (bz) g.ccs += denb;
   const double zzb = bz ? 0.0 : denb;
   if (bp) { dpdb += zzb * wl; wlb += zzb * dpd; }
@@ -107,9 +108,9 @@ AMRS_HD void rp_iter_vjp(const RPPar& q, double P, double Pm, double UM, double 
   g.pl += UPnbar * wl;
   Pbar -= UPnbar * wl;
   wlb += UPnbar * (q.pl - P);
-  // w = 1/rvsqrt(a r), a = hg (P + p) + P
+  // w = 1/rvsqrt(a r), a = hg (P + p) + P; d sqrt(x)/dx = 1/(2 sqrt(x)) = w/2
   const double slb = -wlb * wl * wl, srb = -wrb * wr * wr;
-  const double wlsqb = ddiv_rn(slb, (2.0 * sl)), wrsqb = ddiv_rn(srb, (2.0 * sr));
+  const double wlsqb = 0.5 * slb * wl, wrsqb = 0.5 * srb * wr;
   g.rl += wlsqb * al;
   g.rr += wrsqb * ar;
   const double alb = wlsqb * q.rl, arb = wrsqb * q.rr;
@@ -220,8 +221,9 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
     ustarb += frac * ugb; uob += (1. - frac) * ugb;
     pstarb += frac * pgb; pob += (1. - frac) * pgb;
     const double fracb = rgb * (rstar - ro) + ugb * (ustar - uo) + pgb * (pstar - po);
-    const double qb = ddiv_rn(0.5 * fracb, den2);
-    const double den2b = ddiv_rn(-0.5 * fracb * (spin + spout), (den2 * den2));
+    const double iden2 = ddiv_rn(1.0, den2);
+    const double qb = 0.5 * fracb * iden2;
+    const double den2b = -0.5 * fracb * (spin + spout) * iden2 * iden2;
     double ab = 0.0, bb = 0.0;
     if (bss) ccsb += den2b;
     else if (bab) bb += den2b;
@@ -233,21 +235,23 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
       const double cob = spoutb, cstarb = spinb;
       const double suob = -spoutb - spinb;
       uob += suob * sgnm;
+      const double iro = ddiv_rn(1.0, ro), irst = ddiv_rn(1.0, rstar);
       const double xb = ddiv_rn(cob, (2.0 * co));
-      pob += ddiv_rn(xb * gamma, ro);
-      rob += ddiv_rn(-xb * gamma * po, (ro * ro));
+      pob += xb * gamma * iro;
+      rob += -xb * gamma * po * iro * iro;
       const double yb = ddiv_rn(cstarb, (2.0 * cstar));
-      pstarb += ddiv_rn(yb * gamma, rstar);
-      rstarb += ddiv_rn(-yb * gamma * pstar, (rstar * rstar));
+      pstarb += yb * gamma * irst;
+      rstarb += -yb * gamma * pstar * irst * irst;
     }
   }
   // rstar = ro / (1 - ro dpjmp / wosq), wosq = (hg (pstar + po) + pstar) ro
   {
-    rob += ddiv_rn(rstarb, dd);
-    const double ddb = ddiv_rn(-rstarb * rstar, dd);
+    const double idd = ddiv_rn(1.0, dd), iwo = ddiv_rn(1.0, wosq);
+    rob += rstarb * idd;
+    const double ddb = -rstarb * rstar * idd;
     const double uub = -ddb;
-    const double ttb = ddiv_rn(uub, wosq);
-    const double wosqb = ddiv_rn(-uub * uu, wosq);
+    const double ttb = uub * iwo;
+    const double wosqb = -uub * uu * iwo;
     rob += ttb * dpjmp;
     const double dpb = ttb * ro;
     pstarb += dpb;
@@ -264,8 +268,9 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
     inb[6] += 0.5 * uob; inb[1] += 0.5 * uob;
     inb[7] += 0.5 * pob; inb[2] += 0.5 * pob;
     const double s = rl + rr;
-    inb[0] += ddiv_rn(rob * 2.0 * rr * rr, (s * s));
-    inb[5] += ddiv_rn(rob * 2.0 * rl * rl, (s * s));
+    const double is2 = ddiv_rn(1.0, s * s);
+    inb[0] += rob * 2.0 * rr * rr * is2;
+    inb[5] += rob * 2.0 * rl * rl * is2;
     inb[3] += 0.5 * t1b; inb[8] += 0.5 * t1b;
     inb[4] += 0.5 * t2b; inb[9] += 0.5 * t2b;
   }
@@ -283,22 +288,25 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
   double p0b = Pmnb;
   {
     const double ps1b = m1 ? Pnb : 0.0;
-    const double N1b = ddiv_rn(ps1b, D1), D1b = ddiv_rn(-ps1b * ps1, D1);
+    const double iD1 = ddiv_rn(1.0, D1);
+    const double N1b = ps1b * iD1, D1b = -ps1b * ps1 * iD1;
     double wl1b = N1b * (pr - wr1 * dU) + D1b, wr1b = N1b * (pl - wl1 * dU) + D1b;
     g.pr += N1b * wl1;
     g.pl += N1b * wr1;
     dUb += -N1b * wr1 * wl1;
     // usm0 = ur + (p0 - pr)/wr1;  usp0 = ul - (p0 - pl)/wl1
+    const double iwr1 = ddiv_rn(1.0, wr1), iwl1 = ddiv_rn(1.0, wl1);
+    const double um = UMnb * iwr1, up = UPnb * iwl1;
     g.ur += UMnb;
-    p0b += ddiv_rn(UMnb, wr1);
-    g.pr -= ddiv_rn(UMnb, wr1);
-    wr1b += ddiv_rn(-UMnb * (p0 - pr), (wr1 * wr1));
+    p0b += um;
+    g.pr -= um;
+    wr1b += -um * (p0 - pr) * iwr1;
     g.ul += UPnb;
-    p0b -= ddiv_rn(UPnb, wl1);
-    g.pl += ddiv_rn(UPnb, wl1);
-    wl1b += ddiv_rn(UPnb * (p0 - pl), (wl1 * wl1));
+    p0b -= up;
+    g.pl += up;
+    wl1b += up * (p0 - pl) * iwl1;
     // w1 = rvsqrt(a1 r), a1 = hg (p0 + p) + p0
-    const double wlsqb = ddiv_rn(wl1b, (2.0 * wl1)), wrsqb = ddiv_rn(wr1b, (2.0 * wr1));
+    const double wlsqb = 0.5 * wl1b * iwl1, wrsqb = 0.5 * wr1b * iwr1;
     g.rl += wlsqb * a1l;
     g.rr += wrsqb * a1r;
     const double alb = wlsqb * rl, arb = wrsqb * rr;
@@ -308,7 +316,8 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
   }
   {
     const double ps0b = m0 ? p0b : 0.0;
-    const double N0b = ddiv_rn(ps0b, D0), D0b = ddiv_rn(-ps0b * ps0, D0);
+    const double iD0 = ddiv_rn(1.0, D0);
+    const double N0b = ps0b * iD0, D0b = -ps0b * ps0 * iD0;
     wl0b += N0b * (pr - wr0 * dU) + D0b;
     wr0b += N0b * (pl - wl0 * dU) + D0b;
     g.pr += N0b * wl0;
@@ -318,10 +327,11 @@ AMRS_HD void riemann_prob_vjp(const double gamma, const double smallp, const dou
   // ccs = small (cleft + cright), cleft = wl0 / rl, cright = wr0 / rr
   {
     const double cb = small * (ccsb + g.ccs);
-    wl0b += ddiv_rn(cb, rl);
-    g.rl += ddiv_rn(-cb * cleft, rl);
-    wr0b += ddiv_rn(cb, rr);
-    g.rr += ddiv_rn(-cb * cright, rr);
+    const double irl = ddiv_rn(1.0, rl), irr = ddiv_rn(1.0, rr);
+    wl0b += cb * irl;
+    g.rl += -cb * cleft * irl;
+    wr0b += cb * irr;
+    g.rr += -cb * cright * irr;
   }
   g.ur += dUb;
   g.ul -= dUb;

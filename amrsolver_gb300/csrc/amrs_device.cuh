@@ -80,7 +80,6 @@ __device__ __forceinline__ double cond(const DClosures& c, double T) {
 __device__ __forceinline__ double rmax(double a, double b) { return (a < b) ? b : a; }
 __device__ __forceinline__ double rmin(double a, double b) { return (b < a) ? b : a; }
 
-// cons2prim (src/rhs/CNS_hydro_K.h:15-34) plus QE = cv*T.
 // A product on the FP64 pipe (a * b) or, with I, the same correctly rounded
 // product formed on the integer pipe (dmul_rn).  The kernels of this path
 // are bound by the FP64 pipe while their integer pipe idles; the masks below
@@ -96,9 +95,12 @@ __device__ __forceinline__ double kmul(double a, double b) {
 #ifndef AMRS_C2P_IMUL
 #define AMRS_C2P_IMUL 0x02
 #endif
+// Viscous cell-flux products on the integer pipe (see viscous_cell_dy).
 #ifndef AMRS_VISC_IMUL
 #define AMRS_VISC_IMUL 0x17
 #endif
+
+// cons2prim (src/rhs/CNS_hydro_K.h:15-34) plus QE = cv*T.
 __device__ __forceinline__ void cons2prim(const double u[5], double q[NQ], const DClosures& c) {
   double rho = rmax(1e-40, u[URHO]);
   constexpr int M = AMRS_C2P_IMUL;
@@ -178,7 +180,7 @@ __device__ __forceinline__ void viscous_cell_dy(const double* qc, const double* 
                                                 const double dxinv[3], const DClosures& c, double f[NVF]) {
   // (a-b)*0.5*dxinv == (a-b)*(0.5*dxinv) exactly: the 0.5 scalings are exact.
   // Products on the integer pipe (AMRS_VISC_IMUL): bit 0 the x derivative
-  // scalings, 2 the z ones (the y ones are formed by the callers), 3 the
+  // scalings, 1 the y ones (formed by viscous_cell), 2 the z ones, 3 the
   // r1_3*div terms, 4 the stress scalings by mu, 5 the energy-flux products.
   constexpr int M = AMRS_VISC_IMUL;
   const double hx = 0.5 * dxinv[0], hz = 0.5 * dxinv[2];

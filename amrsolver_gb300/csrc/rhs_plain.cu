@@ -323,8 +323,10 @@ __global__ void __launch_bounds__(256) weno_face_kernel(BoxTable tb, FaceTable f
 }
 
 // ----------------------------------------------------------- Riemann ----
-// Square roots of the solver and the slopes: integer-pipe (dsqrt_rn) or
-// hardware, the same correctly rounded value.
+// Square roots of the solver and the slopes, and the division of the
+// WENO5-Riemann kernel's solver: integer-pipe (dsqrt_rn, ddiv_rn) or
+// hardware, the same correctly rounded values; the defaults are the faster
+// forms at 128^3 and 256^3.
 #ifndef AMRS_RS_ISQRT
 #define AMRS_RS_ISQRT 0
 #endif
@@ -335,7 +337,7 @@ __global__ void __launch_bounds__(256) weno_face_kernel(BoxTable tb, FaceTable f
 #define AMRS_WR_IDIV 0
 #endif
 template <bool I>
-__device__ __forceinline__ double rsqrt_(double x) {
+__device__ __forceinline__ double sqrt_sel(double x) {
   return I ? dsqrt_rn(x) : sqrt(x);
 }
 
@@ -376,7 +378,7 @@ __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, c
     const long long o = q.off(i, j, k);
     const int QN = QU + d, QT1 = (d == 0) ? QV : QU, QT2 = (d == 2) ? QV : QW;
     auto Q = [&](long long off, int n) { return q.p[off + n * q.ns]; };
-    const double c0 = rsqrt_<AMRS_SLOPE_ISQRT>(cl.gamma * cl.Rspec * Q(o, QT));
+    const double c0 = sqrt_sel<AMRS_SLOPE_ISQRT>(cl.gamma * cl.Rspec * Q(o, QT));
     const double cspeed = c0 + (d == 0 ? 2.e-40 : 1.e-40);
     double dlft = ddiv_rn(0.5 * (Q(o, QPRES) - Q(o - s, QPRES)), cspeed) - 0.5 * Q(o, QRHO) * (Q(o, QN) - Q(o - s, QN));
     double drgt = ddiv_rn(0.5 * (Q(o + s, QPRES) - Q(o, QPRES)), cspeed) - 0.5 * Q(o, QRHO) * (Q(o + s, QN) - Q(o, QN));
@@ -406,7 +408,7 @@ __global__ void __launch_bounds__(256) slope_kernel(BoxTable tb, FaceTable ft, c
     if (d == 2 && k <= R.hi[2]) {
       // cns_riemann_z's left state takes its sound speed from q(i,j,k+1)
       // (src/rhs/Riemann.h:316): for the face above this cell, cell k + 2
-      const double csl = rsqrt_<AMRS_SLOPE_ISQRT>(cl.gamma * cl.Rspec * Q(o + 2 * s, QT)) + 1.e-40;
+      const double csl = sqrt_sel<AMRS_SLOPE_ISQRT>(cl.gamma * cl.Rspec * Q(o + 2 * s, QT)) + 1.e-40;
       S.p[os + SL_AL * S.ns] = ddiv_rn(s02, csl) + d1;
       S.p[os + SL_CL * S.ns] = s02 * csl;
     }
@@ -425,7 +427,8 @@ __device__ __forceinline__ double rdiv(double a, double b) {
 // division is the caller's: the MUSCL face kernel runs faster with the
 // integer-pipe division, the WENO5-Riemann kernel (whose reconstructions
 // already load the integer pipe) with the hardware one; the square roots are
-// the hardware's in both (their integer form lengthens the chain).
+// the hardware's in both (AMRS_RS_ISQRT: their integer form lengthens the
+// chain at the 128^3 and 256^3 sizes, though it shortens it at 64^3).
 template <bool IDIV>
 __device__ void riemann_prob(const double gamma, const double smallp, const double rl, const double ul,
                              const double pl, const double ut1l, const double ut2l, const double rr, const double ur,
@@ -435,8 +438,8 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   const double small = 1.e-6;
   const double clsql = gamma * pl * rl;
   const double clsqr = gamma * pr * rr;
-  double wl = rsqrt_<AMRS_RS_ISQRT>(clsql);
-  double wr = rsqrt_<AMRS_RS_ISQRT>(clsqr);
+  double wl = sqrt_sel<AMRS_RS_ISQRT>(clsql);
+  double wr = sqrt_sel<AMRS_RS_ISQRT>(clsqr);
   const double cleft = rdiv<IDIV>(wl, rl);
   const double cright = rdiv<IDIV>(wr, rr);
   const double ccsmall = small * (cleft + cright);
@@ -445,8 +448,8 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   double pstnm1 = pstar;
   double wlsq = (0.5 * (gamma - 1.) * (pstar + pl) + pstar) * rl;
   double wrsq = (0.5 * (gamma - 1.) * (pstar + pr) + pstar) * rr;
-  wl = rsqrt_<AMRS_RS_ISQRT>(wlsq);
-  wr = rsqrt_<AMRS_RS_ISQRT>(wrsq);
+  wl = sqrt_sel<AMRS_RS_ISQRT>(wlsq);
+  wr = sqrt_sel<AMRS_RS_ISQRT>(wrsq);
   double ustarp = ul - rdiv<IDIV>(pstar - pl, wl);
   double ustarm = ur + rdiv<IDIV>(pstar - pr, wr);
   pstar = rdiv<IDIV>(wl * pr + wr * pl - wr * wl * (ur - ul), wl + wr);
@@ -455,8 +458,8 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   for (int iter = 0; iter < 3; ++iter) {
     wlsq = (0.5 * (gamma - 1.) * (pstar + pl) + pstar) * rl;
     wrsq = (0.5 * (gamma - 1.) * (pstar + pr) + pstar) * rr;
-    wl = rdiv<IDIV>(1., rsqrt_<AMRS_RS_ISQRT>(wlsq));
-    wr = rdiv<IDIV>(1., rsqrt_<AMRS_RS_ISQRT>(wrsq));
+    wl = rdiv<IDIV>(1., sqrt_sel<AMRS_RS_ISQRT>(wlsq));
+    wr = rdiv<IDIV>(1., sqrt_sel<AMRS_RS_ISQRT>(wrsq));
     const double ustnm1 = ustarm;
     const double ustnp1 = ustarp;
     ustarm = ur - (pr - pstar) * wr;
@@ -502,7 +505,7 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
   };
   if (pstar >= po) {
     // shock: spout == spin, so the side state or the star state
-    const double spin = rdiv<IDIV>(rsqrt_<AMRS_RS_ISQRT>(wosq), ro) - suo;
+    const double spin = rdiv<IDIV>(sqrt_sel<AMRS_RS_ISQRT>(wosq), ro) - suo;
     if (spin < 0.) {
       rgdnv = ro; ugdnv = uo; pgdnv = po;
     } else if (spin >= 0.) {
@@ -512,8 +515,8 @@ __device__ void riemann_prob(const double gamma, const double smallp, const doub
     }
   } else {
     const double rstar = rdiv<IDIV>(ro, 1. - rdiv<IDIV>(ro * dpjmp, wosq));
-    const double spout = rsqrt_<AMRS_RS_ISQRT>(rdiv<IDIV>(gamma * po, ro)) - suo;
-    const double spin = rsqrt_<AMRS_RS_ISQRT>(rdiv<IDIV>(gamma * pstar, rstar)) - suo;
+    const double spout = sqrt_sel<AMRS_RS_ISQRT>(rdiv<IDIV>(gamma * po, ro)) - suo;
+    const double spin = sqrt_sel<AMRS_RS_ISQRT>(rdiv<IDIV>(gamma * pstar, rstar)) - suo;
     if (spout < 0.) {
       rgdnv = ro; ugdnv = uo; pgdnv = po;
     } else if (spin >= 0.) {

@@ -396,7 +396,10 @@ keep_face_kernel(BoxTable tb, int s_in, int s_s1, int s_out, DProg prog_in, int 
       // ---- phase 2: x faces f in [0, txw] and y faces f in [0, tyw]
       {
         const int nxf = (txw + 1) * tyw, nyf = txw * (tyw + 1);
-        for (int e = tid; e < nxf + nyf; e += F_THREADS) {
+        // items in reverse thread order: the last, partial round of faces
+        // falls on the last warps, while the partial round of pair terms
+        // before the barrier fell on the first ones (measured 0.2% faster)
+        for (int e = F_THREADS - 1 - tid; e < nxf + nyf; e += F_THREADS) {
           double F[5], q1[NQ], q2[NQ];
           if (e < nxf) {
             const int row = e / (txw + 1), f = e - row * (txw + 1);

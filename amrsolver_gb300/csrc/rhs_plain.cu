@@ -153,9 +153,12 @@ __global__ void __launch_bounds__(256) weno_flux_lambda_kernel(BoxTable tb, Face
     fz[4 * ns] = kmul<M3>(rhoh, uz);
     const double cs = dsqrt_rn(kmul<M4>(kmul<M4>(gam, P), rhoinv));
     const long long ol = FR.lam.off(i, j, k);
-    FR.lam.p[ol] = fabs(rmax(rmax(ux + cs, ux - cs), ux));
-    FR.lam.p[ol + FR.lam.ns] = fabs(rmax(rmax(uy + cs, uy - cs), uy));
-    FR.lam.p[ol + 2 * FR.lam.ns] = fabs(rmax(rmax(uz + cs, uz - cs), uz));
+    // |max(max(u + c, u - c), u)| of the reference: with c >= 0 and rounding
+    // monotonic, fl(u + c) >= u >= fl(u - c), so the maximum is u + c itself
+    // (a NaN c gives NaN either way)
+    FR.lam.p[ol] = fabs(ux + cs);
+    FR.lam.p[ol + FR.lam.ns] = fabs(uy + cs);
+    FR.lam.p[ol + 2 * FR.lam.ns] = fabs(uz + cs);
   }
 }
 
